@@ -1,0 +1,455 @@
+// Smoothed-aggregation algebraic multigrid: the preconditioner the reference
+// takes from CUSP (cusp::precond::aggregation::smoothed_aggregation, selected by
+// "preconditioner: SMOOTHED_AGGREGATION", src/preconditioner.h:84-113).
+//
+// Setup (host, once per operator):
+//   strength   all off-diagonal entries are strong (CUSP's default theta = 0)
+//   aggregates standard three-phase greedy aggregation over the matrix graph
+//   tentative  T: piecewise-constant prolongator, columns normalised
+//   smoothing  P = (I - w D^-1 A) T,  w = 4 / (3 rho(D^-1 A)), rho by power iteration
+//   Galerkin   A_c = R A P with R = P^T; repeat until <= kCoarse unknowns
+//   coarsest   dense inverse
+// V-cycle (device): one damped-Jacobi sweep down (from a zero guess) and one up;
+// with R = P^T and Jacobi smoothing the cycle is symmetric, so it also
+// preconditions CG.  Level 0 is the matrix-free structured operator; coarse
+// levels are CSR.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "operators.cuh"
+#include "solver.h"
+
+namespace cuibm {
+
+constexpr int kCoarse = 256;
+
+struct HostCsr {
+    int n = 0, m = 0;  // rows, cols
+    std::vector<int> ptr, col;
+    std::vector<double> val;
+};
+
+struct DevCsr {
+    int n = 0;
+    int *ptr = nullptr, *col = nullptr;
+    double *val = nullptr;
+};
+
+struct SaLevel {
+    int n = 0;
+    double omega = 0;
+    DevCsr A, P, R;      // A unused on level 0 (structured operator)
+    double *dinv = nullptr;
+    double *x = nullptr, *b = nullptr, *r = nullptr, *t = nullptr;
+    double *coarse_inv = nullptr;  // dense inverse on the coarsest level
+};
+
+// ---------------------------------------------------------------------------
+// host sparse helpers
+// ---------------------------------------------------------------------------
+static HostCsr transpose(const HostCsr &A)
+{
+    HostCsr T;
+    T.n = A.m;
+    T.m = A.n;
+    T.ptr.assign(T.n + 1, 0);
+    for (int c : A.col) T.ptr[c + 1]++;
+    for (int i = 0; i < T.n; ++i) T.ptr[i + 1] += T.ptr[i];
+    T.col.resize(A.col.size());
+    T.val.resize(A.val.size());
+    std::vector<int> pos(T.ptr.begin(), T.ptr.end() - 1);
+    for (int i = 0; i < A.n; ++i)
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            int d = pos[A.col[k]]++;
+            T.col[d] = i;
+            T.val[d] = A.val[k];
+        }
+    return T;
+}
+
+static HostCsr multiply(const HostCsr &A, const HostCsr &B)
+{
+    HostCsr C;
+    C.n = A.n;
+    C.m = B.m;
+    C.ptr.assign(C.n + 1, 0);
+    std::vector<int> mark(B.m, -1);
+    std::vector<double> acc(B.m, 0.0);
+    std::vector<int> cols;
+    for (int i = 0; i < A.n; ++i) {
+        cols.clear();
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            int a = A.col[k];
+            double av = A.val[k];
+            for (int q = B.ptr[a]; q < B.ptr[a + 1]; ++q) {
+                int j = B.col[q];
+                if (mark[j] != i) {
+                    mark[j] = i;
+                    acc[j] = 0;
+                    cols.push_back(j);
+                }
+                acc[j] += av * B.val[q];
+            }
+        }
+        std::sort(cols.begin(), cols.end());
+        for (int j : cols) {
+            C.col.push_back(j);
+            C.val.push_back(acc[j]);
+        }
+        C.ptr[i + 1] = (int)C.col.size();
+    }
+    return C;
+}
+
+static std::vector<double> diagonal(const HostCsr &A)
+{
+    std::vector<double> d(A.n, 0.0);
+    for (int i = 0; i < A.n; ++i)
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (A.col[k] == i) d[i] += A.val[k];
+    return d;
+}
+
+// spectral radius of D^-1 A by power iteration from a fixed start vector
+static double rho_dinv_a(const HostCsr &A, const std::vector<double> &d)
+{
+    std::vector<double> x(A.n), y(A.n);
+    for (int i = 0; i < A.n; ++i) x[i] = 1.0 + 0.25 * std::sin(0.37 * i);
+    double lam = 1.0;
+    for (int it = 0; it < 20; ++it) {
+        double nrm = 0;
+        for (int i = 0; i < A.n; ++i) {
+            double s = 0;
+            for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) s += A.val[k] * x[A.col[k]];
+            y[i] = s / d[i];
+            nrm += y[i] * y[i];
+        }
+        nrm = std::sqrt(nrm);
+        double xn = 0;
+        for (double v : x) xn += v * v;
+        lam = nrm / std::sqrt(xn);
+        for (int i = 0; i < A.n; ++i) x[i] = y[i] / nrm;
+    }
+    return lam;
+}
+
+// three-phase greedy aggregation; returns aggregate id per node and the count
+static int aggregate(const HostCsr &A, std::vector<int> &agg)
+{
+    const int n = A.n;
+    agg.assign(n, -1);
+    int na = 0;
+    // phase 1: a node whose neighbours are all free seeds an aggregate with them
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        bool free_ = true;
+        for (int k = A.ptr[i]; k < A.ptr[i + 1] && free_; ++k)
+            if (A.col[k] != i && A.val[k] != 0 && agg[A.col[k]] >= 0) free_ = false;
+        if (!free_) continue;
+        agg[i] = na;
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (A.val[k] != 0) agg[A.col[k]] = na;
+        ++na;
+    }
+    // phase 2: free nodes join a neighbouring aggregate (the strongest link)
+    std::vector<int> agg1 = agg;
+    for (int i = 0; i < n; ++i) {
+        if (agg1[i] >= 0) continue;
+        double best = 0;
+        int ba = -1;
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            int j = A.col[k];
+            if (j != i && agg1[j] >= 0 && std::fabs(A.val[k]) > best) {
+                best = std::fabs(A.val[k]);
+                ba = agg1[j];
+            }
+        }
+        if (ba >= 0) agg[i] = ba;
+    }
+    // phase 3: leftovers form aggregates with their free neighbours
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        agg[i] = na;
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (agg[A.col[k]] < 0) agg[A.col[k]] = na;
+        ++na;
+    }
+    return na;
+}
+
+static void dense_inverse(const HostCsr &A, std::vector<double> &inv)
+{
+    const int n = A.n;
+    std::vector<double> a(n * n, 0.0);
+    inv.assign(n * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) a[i * n + A.col[k]] += A.val[k];
+        inv[i * n + i] = 1.0;
+    }
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
+        if (piv != c)
+            for (int k = 0; k < n; ++k) {
+                std::swap(a[c * n + k], a[piv * n + k]);
+                std::swap(inv[c * n + k], inv[piv * n + k]);
+            }
+        double d = a[c * n + c];
+        if (d == 0) d = 1e-300;
+        for (int k = 0; k < n; ++k) {
+            a[c * n + k] /= d;
+            inv[c * n + k] /= d;
+        }
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            double f = a[r * n + c];
+            if (f == 0) continue;
+            for (int k = 0; k < n; ++k) {
+                a[r * n + k] -= f * a[c * n + k];
+                inv[r * n + k] -= f * inv[c * n + k];
+            }
+        }
+    }
+}
+
+// host CSR of the level-0 operator, identical to the device rows (weights applied)
+void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
+                       std::vector<double> &val);
+
+static DevCsr upload(Context &c, const HostCsr &H)
+{
+    DevCsr D;
+    D.n = H.n;
+    D.ptr = c.carve<int>(H.ptr.size());
+    D.col = c.carve<int>(std::max<size_t>(1, H.col.size()));
+    D.val = c.carve<double>(std::max<size_t>(1, H.val.size()));
+    CUIBM_TRY(cudaMemcpyAsync(D.ptr, H.ptr.data(), H.ptr.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    if (!H.col.empty()) {
+        CUIBM_TRY(cudaMemcpyAsync(D.col, H.col.data(), H.col.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        CUIBM_TRY(cudaMemcpyAsync(D.val, H.val.data(), H.val.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    }
+    return D;
+}
+
+void build_sa_hierarchy(Context &c, LinearSystem &S)
+{
+    std::vector<double> wh;
+    if (S.w) {
+        wh.resize(S.n);
+        CUIBM_TRY(cudaMemcpyAsync(wh.data(), S.w, S.n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    }
+    HostCsr A;
+    A.n = A.m = S.n;
+    host_operator_csr(c, S.which, S.w ? wh.data() : nullptr, A.ptr, A.col, A.val);
+    std::vector<HostCsr> hostA;
+    hostA.push_back(A);
+    // host buffers are kept alive until the uploads below have been issued and synchronised
+    std::vector<HostCsr> keepP, keepR;
+    std::vector<std::vector<double>> keepD;
+    for (int lev = 0; lev < 25; ++lev) {
+        const HostCsr &Al = hostA.back();
+        SaLevel *L = new SaLevel();
+        L->n = Al.n;
+        std::vector<double> d = diagonal(Al);
+        for (double &v : d)
+            if (v == 0) v = 1.0;
+        std::vector<double> dinv(d.size());
+        for (size_t i = 0; i < d.size(); ++i) dinv[i] = 1.0 / d[i];
+        L->dinv = c.carve<double>(L->n);
+        keepD.push_back(dinv);
+        CUIBM_TRY(cudaMemcpyAsync(L->dinv, keepD.back().data(), L->n * sizeof(double), cudaMemcpyHostToDevice,
+                                  c.stream));
+        L->x = c.carve<double>(L->n);
+        L->b = c.carve<double>(L->n);
+        L->r = c.carve<double>(L->n);
+        L->t = c.carve<double>(L->n);
+        if (lev > 0) L->A = upload(c, Al);
+        if (Al.n <= kCoarse || lev == 24) {
+            std::vector<double> inv;
+            dense_inverse(Al, inv);
+            L->coarse_inv = c.carve<double>((size_t)Al.n * Al.n);
+            keepD.push_back(inv);
+            CUIBM_TRY(cudaMemcpyAsync(L->coarse_inv, keepD.back().data(), inv.size() * sizeof(double),
+                                      cudaMemcpyHostToDevice, c.stream));
+            S.amg.push_back(L);
+            break;
+        }
+        double rho = rho_dinv_a(Al, d);
+        L->omega = 4.0 / (3.0 * rho);
+        std::vector<int> agg;
+        int na = aggregate(Al, agg);
+        std::vector<int> size(na, 0);
+        for (int a : agg) size[a]++;
+        HostCsr T;
+        T.n = Al.n;
+        T.m = na;
+        T.ptr.resize(T.n + 1);
+        for (int i = 0; i < T.n; ++i) {
+            T.ptr[i] = i;
+            T.col.push_back(agg[i]);
+            T.val.push_back(1.0 / std::sqrt((double)size[agg[i]]));
+        }
+        T.ptr[T.n] = T.n;
+        HostCsr AT = multiply(Al, T);
+        HostCsr P = T;  // P = T - w D^-1 A T (same sparsity as A T, which contains T's)
+        {
+            HostCsr Pn;
+            Pn.n = AT.n;
+            Pn.m = AT.m;
+            Pn.ptr.assign(Pn.n + 1, 0);
+            for (int i = 0; i < AT.n; ++i) {
+                for (int k = AT.ptr[i]; k < AT.ptr[i + 1]; ++k) {
+                    int j = AT.col[k];
+                    double v = -L->omega * AT.val[k] / d[i];
+                    if (j == agg[i]) v += T.val[i];
+                    Pn.col.push_back(j);
+                    Pn.val.push_back(v);
+                }
+                Pn.ptr[i + 1] = (int)Pn.col.size();
+            }
+            P = Pn;
+        }
+        HostCsr R = transpose(P);
+        HostCsr Ac = multiply(R, multiply(Al, P));
+        keepP.push_back(P);
+        keepR.push_back(R);
+        L->P = upload(c, keepP.back());
+        L->R = upload(c, keepR.back());
+        S.amg.push_back(L);
+        hostA.push_back(Ac);
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));  // host vectors may be reallocated
+    }
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+}
+
+void free_sa_hierarchy(LinearSystem &S)
+{
+    for (SaLevel *L : S.amg) delete L;  // device memory belongs to the context arena
+    S.amg.clear();
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle kernels
+// ---------------------------------------------------------------------------
+struct Lvl0 {
+    int which;
+    Lhs1Coef c1;
+    Lhs2Coef c2;
+    Grid g;
+    const double *w;
+    template <class X>
+    __device__ __forceinline__ double row(int i, const X &x) const
+    {
+        double y = which == 1 ? lhs1_row_f(c1, g, i, x) : lhs2_row_f(c2, g, i, x);
+        return w ? w[i] * y : y;
+    }
+};
+
+struct CsrRow {
+    DevCsr A;
+    template <class X>
+    __device__ __forceinline__ double row(int i, const X &x) const
+    {
+        double s = 0;
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) s += A.val[k] * x(A.col[k]);
+        return s;
+    }
+};
+
+struct JacAccess {
+    const double *__restrict__ b, *__restrict__ d;
+    double w;
+    __device__ __forceinline__ double operator()(int j) const { return w * d[j] * b[j]; }
+};
+
+// x = w D^-1 b (first sweep from zero) and r = b - A x, fused
+template <class Op>
+__global__ void k_sa_down(Op A, int n, const double *__restrict__ b, const double *__restrict__ dinv, double w,
+                          double *__restrict__ x, double *__restrict__ r, const int *gate)
+{
+    if (gate && *gate != KS_RUNNING) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = w * dinv[i] * b[i];
+    r[i] = b[i] - A.row(i, JacAccess{b, dinv, w});
+}
+
+// y = M v for a CSR matrix (restriction R r, or prolongation added: y += P v)
+template <bool ADD>
+__global__ void k_csr_mv(DevCsr M, const double *__restrict__ v, double *__restrict__ y, const int *gate)
+{
+    if (gate && *gate != KS_RUNNING) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.n) return;
+    double s = 0;
+    for (int k = M.ptr[i]; k < M.ptr[i + 1]; ++k) s += M.val[k] * v[M.col[k]];
+    y[i] = ADD ? y[i] + s : s;
+}
+
+// out = x + w D^-1 (b - A x)
+template <class Op>
+__global__ void k_sa_up(Op A, int n, const double *__restrict__ b, const double *__restrict__ dinv, double w,
+                        const double *__restrict__ x, double *__restrict__ out, const int *gate)
+{
+    if (gate && *gate != KS_RUNNING) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = x[i] + w * dinv[i] * (b[i] - A.row(i, PtrAccess{x}));
+}
+
+// coarsest level: x = A^-1 b with the dense inverse (one warp per row)
+__global__ void k_dense_mv(int n, const double *__restrict__ inv, const double *__restrict__ b,
+                           double *__restrict__ x, const int *gate)
+{
+    if (gate && *gate != KS_RUNNING) return;
+    const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s = 0;
+    for (int k = lane; k < n; k += 32) s += inv[(size_t)row * n + k] * b[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) x[row] = s;
+}
+
+// z = V(r): r on level 0 is the Krylov residual, z the preconditioned vector
+void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z)
+{
+    const int nl = (int)S.amg.size();
+    const int *gate = &S.ks->status;
+    Lvl0 A0{S.which, c.l1, c.l2, c.g, S.w};
+    // downward
+    const double *bl = r;
+    for (int l = 0; l < nl - 1; ++l) {
+        SaLevel *L = S.amg[l];
+        if (l == 0)
+            k_sa_down<<<blocks_for(L->n), kBlock, 0, c.stream>>>(A0, L->n, bl, L->dinv, L->omega, L->x, L->r, gate);
+        else
+            k_sa_down<<<blocks_for(L->n), kBlock, 0, c.stream>>>(CsrRow{L->A}, L->n, bl, L->dinv, L->omega, L->x,
+                                                                 L->r, gate);
+        k_csr_mv<false><<<blocks_for(L->R.n), kBlock, 0, c.stream>>>(L->R, L->r, S.amg[l + 1]->b, gate);
+        bl = S.amg[l + 1]->b;
+    }
+    SaLevel *C = S.amg[nl - 1];
+    double *xc = (nl == 1) ? z : C->x;
+    k_dense_mv<<<(C->n + 7) / 8, 256, 0, c.stream>>>(C->n, C->coarse_inv, nl == 1 ? r : C->b, xc, gate);
+    // upward: level l result goes to t_l (l > 0) or z (l = 0)
+    const double *xup = xc;
+    for (int l = nl - 2; l >= 0; --l) {
+        SaLevel *L = S.amg[l];
+        k_csr_mv<true><<<blocks_for(L->P.n), kBlock, 0, c.stream>>>(L->P, xup, L->x, gate);
+        double *out = (l == 0) ? z : L->t;
+        const double *bb = (l == 0) ? r : L->b;
+        if (l == 0)
+            k_sa_up<<<blocks_for(L->n), kBlock, 0, c.stream>>>(A0, L->n, bb, L->dinv, L->omega, L->x, out, gate);
+        else
+            k_sa_up<<<blocks_for(L->n), kBlock, 0, c.stream>>>(CsrRow{L->A}, L->n, bb, L->dinv, L->omega, L->x, out,
+                                                               gate);
+        xup = out;
+    }
+    CUIBM_TRY(cudaGetLastError());
+}
+
+}  // namespace cuibm

@@ -1,0 +1,660 @@
+// Context life cycle, step orchestration and the extern "C" entry points.
+//
+// The time step follows the reference's phase order exactly:
+//   NAVIER_STOKES  NavierStokesSolver::stepTime (NavierStokesSolver.cu:163-188)
+//   LUO (external) luo_base::stepTime (luo_base.cu:208-233) with luoIBM's phases
+//                  (luoIBM.cu:91-102, luoIBM/intermediateVelocity.cu:128-167,
+//                  luoIBM/intermediatePressure.cu:280-342, luo_base/projectVelocity.cu:237-279,
+//                  luo_base.cu:255-264 update body)
+// and is recorded once into a CUDA graph whose linear solves are WHILE
+// conditional nodes: one graph launch per step, no host synchronisation inside a
+// step.  cuibm_step checks the solver status once at the end of the call.
+#include <cstdio>
+#include <cstring>
+#include <sys/stat.h>
+
+#include "../../include/cuibm.h"
+#include "solver.h"
+
+namespace cuibm {
+
+static int *g_err_word_of(Context &c) { return c.err_word; }
+
+static void alloc_fields(Context &c)
+{
+    const Grid &g = c.g;
+    const size_t nUV = g.nUV, nP = g.nP, nx = g.nx, ny = g.ny;
+    size_t est = (nUV + nP) * 1800 + (size_t)96 << 20;
+    if (c.has_body) est += (nUV + nP) * 400;
+    CUIBM_TRY(cudaMalloc(&c.arena, est));
+    c.arena_bytes = est;
+    c.arena_used = 0;
+    CUIBM_TRY(cudaMemsetAsync(c.arena, 0, est, c.stream));
+    c.u = c.carve<double>(nUV);
+    c.uhat = c.carve<double>(nUV);
+    c.uold = c.carve<double>(nUV);
+    c.N = c.carve<double>(nUV);
+    c.Nold = c.carve<double>(nUV);
+    c.L = c.carve<double>(nUV);
+    c.bc1 = c.carve<double>(nUV);
+    c.rhs1 = c.carve<double>(nUV);
+    c.p = c.carve<double>(nP);
+    c.p_old = c.carve<double>(nP);
+    c.rhs2 = c.carve<double>(nP);
+    c.cfl = c.carve<double>(nP);
+    c.work_x = c.carve<double>(nUV > nP ? nUV : nP);
+    c.work_y = c.carve<double>(nUV > nP ? nUV : nP);
+    c.bc[XMINUS] = c.carve<double>(2 * ny - 1);
+    c.bc[XPLUS] = c.carve<double>(2 * ny - 1);
+    c.bc[YMINUS] = c.carve<double>(2 * nx - 1);
+    c.bc[YPLUS] = c.carve<double>(2 * nx - 1);
+    c.x = c.carve<double>(nx);
+    c.dx = c.carve<double>(nx);
+    c.xu = c.carve<double>(nx - 1);
+    c.xv = c.carve<double>(nx);
+    c.y = c.carve<double>(ny);
+    c.dy = c.carve<double>(ny);
+    c.yu = c.carve<double>(ny);
+    c.yv = c.carve<double>(ny - 1);
+    c.err_word = c.carve<int>(4);
+    c.step_counter_dev = c.carve<int>(4);
+    auto up = [&](double *d, const std::vector<double> &h) {
+        CUIBM_TRY(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    };
+    up(c.x, c.gx.centre);
+    up(c.dx, c.gx.width);
+    up(c.xu, c.gx.face);
+    up(c.xv, c.gx.centre);
+    up(c.y, c.gy.centre);
+    up(c.dy, c.gy.width);
+    up(c.yu, c.gy.centre);
+    up(c.yv, c.gy.face);
+}
+
+// boundary arrays from the flow BCs (NavierStokesSolver.cu:104-128)
+static void init_boundary_arrays(Context &c)
+{
+    const int nx = c.g.nx, ny = c.g.ny;
+    std::vector<double> xm(2 * ny - 1), xp(2 * ny - 1), ym(2 * nx - 1), yp(2 * nx - 1);
+    const BC(*b)[2] = c.P.bc;
+    for (int i = 0; i < nx - 1; ++i) {
+        ym[i] = b[YMINUS][0].value;
+        yp[i] = b[YPLUS][0].value;
+        ym[i + nx - 1] = b[YMINUS][1].value;
+        yp[i + nx - 1] = b[YPLUS][1].value;
+    }
+    ym[2 * nx - 2] = b[YMINUS][1].value;
+    yp[2 * nx - 2] = b[YPLUS][1].value;
+    for (int i = 0; i < ny - 1; ++i) {
+        xm[i] = b[XMINUS][0].value;
+        xp[i] = b[XPLUS][0].value;
+        xm[i + ny] = b[XMINUS][1].value;
+        xp[i + ny] = b[XPLUS][1].value;
+    }
+    xm[ny - 1] = b[XMINUS][0].value;
+    xp[ny - 1] = b[XPLUS][0].value;
+    auto up = [&](double *d, const std::vector<double> &h) {
+        CUIBM_TRY(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    };
+    up(c.bc[XMINUS], xm);
+    up(c.bc[XPLUS], xp);
+    up(c.bc[YMINUS], ym);
+    up(c.bc[YPLUS], yp);
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+}
+
+struct PhaseTimer {
+    Context &c;
+    const char *name;
+    bool on;
+    PhaseTimer(Context &c_, const char *n) : c(c_), name(n), on(c_.profile_phases)
+    {
+        if (on) CUIBM_TRY(cudaEventRecord(c.ev0, c.stream));
+    }
+    ~PhaseTimer()
+    {
+        if (!on) return;
+        cudaEventRecord(c.ev1, c.stream);
+        cudaEventSynchronize(c.ev1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+        Timer &t = c.timers[name];
+        t.ms += ms;
+        t.count++;
+    }
+};
+
+// ---- phases ---------------------------------------------------------------------
+static bool is_luo(const Context &c) { return c.P.solverType == ST_LUO && c.has_body; }
+
+static void phase_generate_rhs1(Context &c)
+{
+    PhaseTimer t(c, "Intermediate Velocity Setup");
+    if (is_luo(c)) {
+        launch_robin(c);                    // updateRobinBoundary
+        launch_ghost_velocity(c, c.u, true);  // rhs1GNInterpolation
+        launch_set_inside(c, c.u);          // zeroVelocity
+        launch_hybrid_velocity(c, c.u);     // rhs1HNInterpolation
+    }
+    launch_rhs1(c, false);
+}
+
+static void phase_solve_velocity(Context &c, bool in_graph)
+{
+    PhaseTimer t(c, "Intermediate Velocity Solve");
+    launch_solve(c, c.sys1, c.rhs1, c.uhat, in_graph);
+}
+
+static void phase_generate_rhs2(Context &c)
+{
+    PhaseTimer t(c, "Poisson Setup");
+    if (is_luo(c)) launch_ghost_velocity(c, c.uhat, true);  // preRHS2Interpolation
+    launch_rhs2(c, c.uhat);
+}
+
+static void phase_solve_poisson(Context &c, bool in_graph)
+{
+    PhaseTimer t(c, "Poisson Solve");
+    launch_solve(c, c.sys2, c.rhs2, c.p, in_graph);
+}
+
+static void phase_project(Context &c)
+{
+    PhaseTimer t(c, "Velocity Projection");
+    launch_project(c);
+    if (is_luo(c)) {
+        launch_ghost_velocity(c, c.u, true);
+        launch_set_inside(c, c.u);
+    }
+}
+
+static void phase_update_body(Context &c)
+{
+    if (!is_luo(c)) return;
+    {
+        PhaseTimer t(c, "Calculate Force");
+        launch_force(c);
+    }
+    {
+        PhaseTimer t(c, "Move Body");
+        launch_body_motion(c, -1.0);  // time taken from the device step counter
+    }
+    {
+        PhaseTimer t(c, "Update Solver");
+        launch_tag_points(c);
+    }
+}
+
+static void record_step(Context &c, bool in_graph)
+{
+    if (is_luo(c)) {
+        launch_copy(c, c.p_old, c.p, c.g.nP);    // _pre_step: pressure_old = pressure
+        launch_copy(c, c.uold, c.u, c.g.nUV);    //            uold = u
+        launch_body_pre_step(c);                 //            uB0 = uB, ...
+    }
+    phase_generate_rhs1(c);
+    phase_solve_velocity(c, in_graph);
+    if (is_luo(c)) {
+        PhaseTimer t(c, "Intermediate Velocity Weight");
+        launch_weight_uhat(c);
+    }
+    phase_generate_rhs2(c);
+    phase_solve_poisson(c, in_graph);
+    if (is_luo(c)) {
+        PhaseTimer t(c, "Poisson Weight");
+        launch_hybrid_pressure(c);
+        launch_weight_pressure(c);
+        launch_ghost_pressure(c, true);
+    }
+    phase_project(c);
+    launch_step_counter(c);  // timeStep++ on the device (read by motion)
+    phase_update_body(c);
+    {
+        PhaseTimer t(c, "CFL");
+        launch_cfl(c);
+    }
+}
+
+static void build_step_graph(Context &c)
+{
+    if (c.step_exec) {
+        cudaGraphExecDestroy(c.step_exec);
+        cudaGraphDestroy(c.step_graph);
+        c.step_exec = nullptr;
+    }
+    CUIBM_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed));
+    try {
+        record_step(c, true);
+    } catch (...) {
+        cudaGraph_t g;
+        cudaStreamEndCapture(c.stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    CUIBM_TRY(cudaStreamEndCapture(c.stream, &c.step_graph));
+    CUIBM_TRY(cudaGraphInstantiate(&c.step_exec, c.step_graph, 0));
+}
+
+}  // namespace cuibm
+
+using namespace cuibm;
+
+struct cuibm_ctx {
+    Context c;
+};
+
+static int fail(cuibm_ctx *h, int code, const std::string &msg)
+{
+    if (h) h->c.err = msg;
+    return code;
+}
+
+#define CUIBM_GUARD(h, ...)                                                       \
+    try {                                                                         \
+        __VA_ARGS__;                                                              \
+    } catch (const CudaError &e) {                                                \
+        return fail(h, CUIBM_ERR_CUDA, e.msg);                                    \
+    } catch (const InputError &e) {                                               \
+        return fail(h, CUIBM_ERR_BAD_INPUT, e.msg);                               \
+    } catch (const std::exception &e) {                                           \
+        return fail(h, CUIBM_ERR_BAD_INPUT, e.what());                            \
+    }
+
+static std::string g_create_error;
+
+extern "C" {
+
+int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx **out)
+{
+    if (!out) return CUIBM_ERR_BAD_INPUT;
+    *out = nullptr;
+    cuibm_ctx *h = new cuibm_ctx();
+    Context &c = h->c;
+    std::string err = load_case(case_folder ? case_folder : ".", argc, argv, c.P);
+    if (!err.empty()) {
+        g_create_error = err;
+        delete h;
+        return err.rfind("cannot open", 0) == 0 ? CUIBM_ERR_IO : CUIBM_ERR_BAD_INPUT;
+    }
+    if (c.P.solverType == ST_FSI) {
+        g_create_error = "SolverType FSI is not implemented by the reference either";
+        delete h;
+        return CUIBM_ERR_UNSUPPORTED;
+    }
+    try {
+        if (!(err = build_axis(c.P.axis[0], c.gx)).empty()) throw InputError(err);
+        if (!(err = build_axis(c.P.axis[1], c.gy)).empty()) throw InputError(err);
+        if (!(err = build_bodies(c.P.bodies, c.body)).empty()) throw InputError(err);
+        Grid &g = c.g;
+        g.nx = c.gx.n;
+        g.ny = c.gy.n;
+        g.nU = (g.nx - 1) * g.ny;
+        g.nV = g.nx * (g.ny - 1);
+        g.nUV = g.nU + g.nV;
+        g.nP = g.nx * g.ny;
+        c.has_body = c.body.total > 0 && c.P.solverType != ST_NAVIERSTOKES;
+        if (c.P.solverType != ST_NAVIERSTOKES && c.P.solverType != ST_LUO)
+            throw InputError("SolverType FADLUN / OSC_CYLINDER is not implemented by this build yet");
+        if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
+            throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
+        if (c.has_body) {
+            c.bb = bounding_box(c.body.x.data(), c.body.y.data(), c.body.total, c.gx, c.gy, c.P.scaleCV);
+            if (c.bb.i0 < 6 || c.bb.j0 < 6 || c.bb.i0 + c.bb.ncx > g.nx - 7 || c.bb.j0 + c.bb.ncy > g.ny - 7)
+                throw InputError("the body's scaled bounding box reaches the domain boundary");
+        }
+        CUIBM_TRY(cudaSetDevice(c.P.deviceNumber));
+        c.device = c.P.deviceNumber;
+        CUIBM_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        CUIBM_TRY(cudaStreamCreateWithFlags(&c.side_stream, cudaStreamNonBlocking));
+        CUIBM_TRY(cudaEventCreate(&c.ev0));
+        CUIBM_TRY(cudaEventCreate(&c.ev1));
+        CUIBM_TRY(cudaHostAlloc(&c.h_scalars, 64 * sizeof(double), cudaHostAllocDefault));
+        alloc_fields(c);
+        upload_ns_tables(c);
+        c.sys1.which = 1;
+        c.sys2.which = 2;
+        setup_system(c, c.sys1);
+        setup_system(c, c.sys2);
+        if (c.has_body) setup_ib(c);
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        const char *ev = getenv("CUIBM_GRAPH");
+        c.use_graph = !(ev && ev[0] == '0');
+        c.created = true;
+    } catch (const CudaError &e) {
+        g_create_error = e.msg;
+        cuibm_destroy(h);
+        return CUIBM_ERR_CUDA;
+    } catch (const InputError &e) {
+        g_create_error = e.msg;
+        cuibm_destroy(h);
+        return CUIBM_ERR_BAD_INPUT;
+    }
+    *out = h;
+    return CUIBM_OK;
+}
+
+const char *cuibm_last_error(const cuibm_ctx *h) { return h ? h->c.err.c_str() : g_create_error.c_str(); }
+
+int cuibm_initialise(cuibm_ctx *h)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        CUIBM_TRY(cudaSetDevice(c.device));
+        c.timeStep = c.P.startStep;
+        // initialiseNoBody: rhs2 = uhat = Nold = N = 0, initial velocity, uhat = u, boundary arrays
+        CUIBM_TRY(cudaMemsetAsync(c.rhs2, 0, c.g.nP * sizeof(double), c.stream));
+        CUIBM_TRY(cudaMemsetAsync(c.N, 0, c.g.nUV * sizeof(double), c.stream));
+        CUIBM_TRY(cudaMemsetAsync(c.Nold, 0, c.g.nUV * sizeof(double), c.stream));
+        CUIBM_TRY(cudaMemsetAsync(c.p, 0, c.g.nP * sizeof(double), c.stream));
+        launch_initial_velocity(c);
+        launch_copy(c, c.uhat, c.u, c.g.nUV);
+        init_boundary_arrays(c);
+        int zero[2] = {0, 0};
+        CUIBM_TRY(cudaMemcpyAsync(c.step_counter_dev, &c.timeStep, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        CUIBM_TRY(cudaMemcpyAsync(g_err_word_of(c), zero, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        if (c.has_body) {
+            initialise_body(c);       // luo_base::initialise movement at t = dt*timeStep
+            launch_tag_points(c);     // tagPoints()
+            launch_set_inside(c, c.u);  // luoIBM::zeroVelocity
+        }
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        c.cfl_max = 0;
+        if (c.P.writeOutput) {
+            mkdir(c.P.caseFolder.c_str(), 0755);
+            std::string f = c.P.caseFolder + "/iterations";
+            c.iterationsFile = fopen(f.c_str(), "w");
+            if (c.has_body) {
+                c.forceFile = fopen((c.P.caseFolder + "/forces").c_str(), "w");
+                c.midPositionFile = fopen((c.P.caseFolder + "/midPosition").c_str(), "w");
+            }
+            write_grid_file(c);
+        }
+        if (c.use_graph) build_step_graph(c);
+        c.initialised = true;
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_step(cuibm_ctx *h, int nsteps)
+{
+    if (!h || !h->c.initialised) return CUIBM_ERR_STATE;
+    if (nsteps < 0) return fail(h, CUIBM_ERR_BAD_INPUT, "nsteps < 0");
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        for (int s = 0; s < nsteps; ++s) {
+            if (c.use_graph && !c.profile_phases)
+                CUIBM_TRY(cudaGraphLaunch(c.step_exec, c.stream));
+            else
+                record_step(c, false);
+            c.timeStep++;
+        }
+        int errw = 0;
+        CUIBM_TRY(cudaMemcpyAsync(&errw, g_err_word_of(c), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        if (errw) {
+            int sys = errw / 16, st = errw % 16;
+            char msg[256];
+            snprintf(msg, sizeof msg, "ERROR: Solve for %s failed (%s) by time step %d",
+                     sys == 1 ? "uhat" : "pressure", st == KS_NAN ? "non-finite residual" : "maxIterations reached",
+                     c.timeStep);
+            c.err = msg;
+            return st == KS_NAN ? CUIBM_ERR_NAN : CUIBM_ERR_NOT_CONVERGED;
+        }
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_finished(const cuibm_ctx *h)
+{
+    if (!h) return 1;
+    return h->c.timeStep < h->c.P.nt ? 0 : 1;
+}
+
+int cuibm_get_info(const cuibm_ctx *h, cuibm_info *info)
+{
+    if (!h || !info || !h->c.created) return CUIBM_ERR_STATE;
+    const Context &c = h->c;
+    std::memset(info, 0, sizeof *info);
+    info->nx = c.g.nx;
+    info->ny = c.g.ny;
+    info->numU = c.g.nU;
+    info->numV = c.g.nV;
+    info->numUV = c.g.nUV;
+    info->numP = c.g.nP;
+    info->solver_type = c.P.solverType;
+    info->time_step = c.timeStep;
+    info->nt = c.P.nt;
+    info->nsave = c.P.nsave;
+    info->dt = c.P.dt;
+    info->nu = c.P.nu;
+    info->total_points = c.body.total;
+    info->bb_start_i = c.bb.i0;
+    info->bb_start_j = c.bb.j0;
+    info->bb_ncx = c.bb.ncx;
+    info->bb_ncy = c.bb.ncy;
+    const int nx = c.g.nx, ny = c.g.ny;
+    info->nnz_lhs1 = (nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + (ny - 1) * nx * 5 - 2 * (ny - 1) - 2 * nx;
+    info->nnz_lhs2 = 5 * nx * ny - 2 * ny - 2 * nx;
+    info->velocity_precond = c.P.velocity.precond;
+    info->poisson_precond = c.P.poisson.precond;
+    info->velocity_krylov = c.P.krylovVelocity;
+    info->poisson_krylov = c.P.krylovPoisson;
+    info->amg_levels = (int)c.sys2.amg.size();
+    return CUIBM_OK;
+}
+
+int cuibm_get_field(cuibm_ctx *h, int field, void *dst, size_t bytes, int dst_on_device)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        size_t need = 0;
+        void *src = field_pointer(c, field, &need);
+        if (!src) return fail(h, CUIBM_ERR_BAD_INPUT, "unknown or unavailable field " + std::to_string(field));
+        if (bytes != need)
+            return fail(h, CUIBM_ERR_BAD_INPUT, "field " + std::to_string(field) + " needs " + std::to_string(need) +
+                                                    " bytes, got " + std::to_string(bytes));
+        CUIBM_TRY(cudaMemcpyAsync(dst, src, bytes, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                  c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_set_field(cuibm_ctx *h, int field, const void *src, size_t bytes, int src_on_device)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        size_t need = 0;
+        void *dst = field_pointer(c, field, &need);
+        if (!dst) return fail(h, CUIBM_ERR_BAD_INPUT, "unknown or unavailable field " + std::to_string(field));
+        if (bytes != need) return fail(h, CUIBM_ERR_BAD_INPUT, "wrong byte count for field " + std::to_string(field));
+        CUIBM_TRY(cudaMemcpyAsync(dst, src, bytes, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        field_changed(c, field);
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_get_forces(cuibm_ctx *h, double *fx, double *fy)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        double f[2] = {0, 0};
+        if (c.has_body) {
+            CUIBM_TRY(cudaMemcpyAsync(f, c.ib.forceOut, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        }
+        if (fx) *fx = f[0];
+        if (fy) *fy = f[1];
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_get_iterations(cuibm_ctx *h, int *it1, int *it2)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        int a = 0, b = 0;
+        read_solve_status(c, c.sys1, &a);
+        read_solve_status(c, c.sys2, &b);
+        if (it1) *it1 = a;
+        if (it2) *it2 = b;
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_get_matrix(cuibm_ctx *h, int system, int *row, int *col, double *val, size_t nnz)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        std::vector<int> r, cc;
+        std::vector<double> v;
+        if (system != 1 && system != 2) return fail(h, CUIBM_ERR_BAD_INPUT, "system must be 1 or 2");
+        host_matrix_coo(c, system, r, cc, v);
+        if (nnz != r.size()) return fail(h, CUIBM_ERR_BAD_INPUT, "nnz mismatch: need " + std::to_string(r.size()));
+        std::memcpy(row, r.data(), r.size() * sizeof(int));
+        std::memcpy(col, cc.data(), cc.size() * sizeof(int));
+        std::memcpy(val, v.data(), v.size() * sizeof(double));
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_run(cuibm_ctx *h, int op)
+{
+    if (!h || !h->c.created) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        bool ib = c.has_body;
+        auto need_ib = [&]() {
+            if (!ib) throw InputError("operation needs an immersed body");
+        };
+        switch (op) {
+        case CUIBM_OP_RHS1_TERMS: launch_rhs1(c, true); break;
+        case CUIBM_OP_GENERATE_RHS1: phase_generate_rhs1(c); break;
+        case CUIBM_OP_SOLVE_VELOCITY: phase_solve_velocity(c, false); break;
+        case CUIBM_OP_WEIGHT_UHAT: need_ib(); launch_weight_uhat(c); break;
+        case CUIBM_OP_GENERATE_RHS2: phase_generate_rhs2(c); break;
+        case CUIBM_OP_RHS2: launch_rhs2(c, c.uhat); break;
+        case CUIBM_OP_SOLVE_POISSON: phase_solve_poisson(c, false); break;
+        case CUIBM_OP_WEIGHT_PRESSURE:
+            need_ib();
+            launch_hybrid_pressure(c);
+            launch_weight_pressure(c);
+            launch_ghost_pressure(c, true);
+            break;
+        case CUIBM_OP_PROJECT: launch_project(c); break;
+        case CUIBM_OP_PROJECT_VELOCITY: phase_project(c); break;
+        case CUIBM_OP_UPDATE_BODY: need_ib(); phase_update_body(c); break;
+        case CUIBM_OP_APPLY_LHS1: launch_apply(c, 1, c.work_x, c.work_y); break;
+        case CUIBM_OP_APPLY_LHS2: launch_apply(c, 2, c.work_x, c.work_y); break;
+        case CUIBM_OP_TAG_POINTS: need_ib(); launch_tag_points(c); break;
+        case CUIBM_OP_GHOST_VELOCITY_U: need_ib(); launch_ghost_velocity(c, c.u, true); break;
+        case CUIBM_OP_GHOST_VELOCITY_UHAT: need_ib(); launch_ghost_velocity(c, c.uhat, true); break;
+        case CUIBM_OP_HYBRID_VELOCITY: need_ib(); launch_hybrid_velocity(c, c.u); break;
+        case CUIBM_OP_HYBRID_PRESSURE: need_ib(); launch_hybrid_pressure(c); break;
+        case CUIBM_OP_GHOST_PRESSURE: need_ib(); launch_ghost_pressure(c, true); break;
+        case CUIBM_OP_SET_INSIDE: need_ib(); launch_set_inside(c, c.u); break;
+        case CUIBM_OP_ROBIN_BOUNDARY: launch_robin(c); break;
+        case CUIBM_OP_FORCE: need_ib(); launch_force(c); break;
+        case CUIBM_OP_CFL: launch_cfl(c); break;
+        default: return fail(h, CUIBM_ERR_BAD_INPUT, "unknown operation " + std::to_string(op));
+        }
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        CUIBM_TRY(cudaGetLastError());
+        if (op == CUIBM_OP_SOLVE_VELOCITY || op == CUIBM_OP_SOLVE_POISSON) {
+            int it = 0;
+            int st = read_solve_status(c, op == CUIBM_OP_SOLVE_VELOCITY ? c.sys1 : c.sys2, &it);
+            if (st == KS_MAXIT) return fail(h, CUIBM_ERR_NOT_CONVERGED, "linear solve reached maxIterations");
+            if (st == KS_NAN) return fail(h, CUIBM_ERR_NAN, "linear solve produced a non-finite residual");
+        }
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_get_stream(cuibm_ctx *h, void **stream)
+{
+    if (!h || !stream) return CUIBM_ERR_BAD_INPUT;
+    *stream = (void *)h->c.stream;
+    return CUIBM_OK;
+}
+
+int cuibm_get_timer(cuibm_ctx *h, const char *name, double *ms, int *count)
+{
+    if (!h || !name) return CUIBM_ERR_BAD_INPUT;
+    auto it = h->c.timers.find(name);
+    if (it == h->c.timers.end()) {
+        if (ms) *ms = 0;
+        if (count) *count = 0;
+        return CUIBM_OK;
+    }
+    if (ms) *ms = it->second.ms;
+    if (count) *count = it->second.count;
+    return CUIBM_OK;
+}
+
+int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
+{
+    if (!h || !key) return CUIBM_ERR_BAD_INPUT;
+    Context &c = h->c;
+    std::string k(key);
+    if (k == "profile_phases") c.profile_phases = value != 0;
+    else if (k == "use_graph") {
+        bool want = value != 0;
+        if (want != c.use_graph && c.initialised) {
+            CUIBM_GUARD(h, {
+                c.use_graph = want;
+                if (want) build_step_graph(c);
+            });
+        }
+        c.use_graph = want;
+    } else if (k == "write_output") c.P.writeOutput = value != 0;
+    else return fail(h, CUIBM_ERR_BAD_INPUT, "unknown option " + k);
+    return CUIBM_OK;
+}
+
+int cuibm_write_data(cuibm_ctx *h)
+{
+    if (!h || !h->c.initialised) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, { write_step_output(c); });
+    return CUIBM_OK;
+}
+
+int cuibm_shutdown(cuibm_ctx *h)
+{
+    if (!h) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    if (c.iterationsFile) fclose(c.iterationsFile);
+    if (c.forceFile) fclose(c.forceFile);
+    if (c.midPositionFile) fclose(c.midPositionFile);
+    c.iterationsFile = c.forceFile = c.midPositionFile = nullptr;
+    return CUIBM_OK;
+}
+
+void cuibm_destroy(cuibm_ctx *h)
+{
+    if (!h) return;
+    Context &c = h->c;
+    cuibm_shutdown(h);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    if (c.step_exec) cudaGraphExecDestroy(c.step_exec);
+    if (c.step_graph) cudaGraphDestroy(c.step_graph);
+    free_sa_hierarchy(c.sys1);
+    free_sa_hierarchy(c.sys2);
+    if (c.arena) cudaFree(c.arena);
+    if (c.h_scalars) cudaFreeHost(c.h_scalars);
+    if (c.ev0) cudaEventDestroy(c.ev0);
+    if (c.ev1) cudaEventDestroy(c.ev1);
+    if (c.side_stream) cudaStreamDestroy(c.side_stream);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete h;
+}
+
+}  // extern "C"

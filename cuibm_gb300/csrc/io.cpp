@@ -1,0 +1,95 @@
+// Output files in the reference's formats, so its post-processing scripts read
+// this build's output unchanged:
+//   grid             src/io/io.cu:428-444 (int nx, nx+1 doubles, int ny, ny+1 doubles; the
+//                    reference writes one double past the cell centres - here the domain
+//                    end coordinate)
+//   NNNNNNN/q        src/io/io.cu:459-488 (int N, N doubles of uhat), every nsave steps
+//   NNNNNNN/lambda   same, pressure
+//   NNNNNNN/bodies   src/bodies.cu:459-471 (body point coordinates)
+//   iterations       NavierStokesSolver.cu:350 (timeStep, velocity and Poisson iterations)
+//   forces           luoIBM.cu:76-78 (time, Fx, Fy)
+//   midPosition      luo_base.cu:193-205 (timeStep, X, Y, U, V)
+#include <sys/stat.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "solver.h"
+
+namespace cuibm {
+
+void write_grid_file(Context &c)
+{
+    std::string f = c.P.caseFolder + "/grid";
+    FILE *fp = fopen(f.c_str(), "wb");
+    if (!fp) throw InputError("cannot write " + f);
+    auto axis = [&](const Axis &a, double end) {
+        int n = a.n;
+        std::vector<double> v(a.centre);
+        v.push_back(end);
+        fwrite(&n, sizeof(int), 1, fp);
+        fwrite(v.data(), sizeof(double), v.size(), fp);
+    };
+    axis(c.gx, c.P.axis[0].ends.back());
+    axis(c.gy, c.P.axis[1].ends.back());
+    fclose(fp);
+}
+
+static void write_array(const std::string &path, const std::vector<double> &v)
+{
+    FILE *fp = fopen(path.c_str(), "wb");
+    if (!fp) throw InputError("cannot write " + path);
+    int n = (int)v.size();
+    fwrite(&n, sizeof(int), 1, fp);
+    fwrite(v.data(), sizeof(double), v.size(), fp);
+    fclose(fp);
+}
+
+void write_step_output(Context &c)
+{
+    if (!c.P.writeOutput) return;
+    int it1 = 0, it2 = 0;
+    read_solve_status(c, c.sys1, &it1);
+    read_solve_status(c, c.sys2, &it2);
+    if (c.iterationsFile) fprintf(c.iterationsFile, "%d\t%d\t%d\n", c.timeStep, it1, it2);
+    if (c.timeStep % c.P.nsave == 0) {
+        char dir[4096];
+        snprintf(dir, sizeof dir, "%s/%07d", c.P.caseFolder.c_str(), c.timeStep);
+        mkdir(dir, 0755);
+        std::vector<double> q(c.g.nUV), lam(c.g.nP);
+        CUIBM_TRY(cudaMemcpyAsync(q.data(), c.uhat, q.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaMemcpyAsync(lam.data(), c.p, lam.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        write_array(std::string(dir) + "/q", q);
+        write_array(std::string(dir) + "/lambda", lam);
+        if (c.has_body) {
+            std::vector<double> bx(c.body.total), by(c.body.total);
+            CUIBM_TRY(cudaMemcpyAsync(bx.data(), c.ib.bx, bx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            CUIBM_TRY(cudaMemcpyAsync(by.data(), c.ib.by, by.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            FILE *fp = fopen((std::string(dir) + "/bodies").c_str(), "w");
+            if (fp) {
+                fprintf(fp, "#%19s%20s\n", "x-coordinate", "y-coordinate");
+                for (int l = 0; l < c.body.total; ++l) fprintf(fp, "%g\t%g\n", bx[l], by[l]);
+                fclose(fp);
+            }
+        }
+    }
+    if (c.has_body) {
+        double f[2] = {0, 0}, m[4] = {0, 0, 0, 0};
+        CUIBM_TRY(cudaMemcpyAsync(f, c.ib.forceOut, sizeof f, cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaMemcpyAsync(m, c.ib.motion, sizeof m, cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        if (c.forceFile) {
+            if (c.timeStep == 1) fprintf(c.forceFile, "timestep\tFx\tFy\n");
+            fprintf(c.forceFile, "%g\t%g\t%g\n", c.timeStep * c.P.dt, f[0], f[1]);
+        }
+        if (c.midPositionFile) {
+            if (c.timeStep == 1) fprintf(c.midPositionFile, "ts\tX\tY\tU\tV\n");
+            fprintf(c.midPositionFile, "%d\t%g\t%g\t%g\t%g\n", c.timeStep, m[0], m[1], m[2], m[3]);
+        }
+    }
+    if (c.iterationsFile) fflush(c.iterationsFile);
+}
+
+}  // namespace cuibm

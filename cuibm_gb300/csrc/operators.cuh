@@ -1,0 +1,86 @@
+// Matrix-free rows of the reference's LHS1 (I - dt/2 nu L) and LHS2 (dt D G)
+// COO matrices (NavierStokes/kernels/LHS1.cu, LHS2.cu), shared by the operator
+// kernels and the Krylov solvers.  Diagonals are summed in the reference's
+// order (1 + E + W + N + S; 0 + E + W + N + S), so diagonal values are bit-
+// identical to the reference's matrix entries.
+#pragma once
+#include "solver.h"
+
+namespace cuibm {
+
+// ---------------------------------------------------------------------------
+// operator rows (device)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double lhs1_diag(const Lhs1Coef &c, const Grid &g, int i)
+{
+    if (i < g.nU) {
+        int I = i % (g.nx - 1), J = i / (g.nx - 1);
+        return (((1 + c.uE[I]) + c.uW[I]) + c.uN[J]) + c.uS[J];
+    }
+    int k = i - g.nU, I = k % g.nx, J = k / g.nx;
+    return (((1 + c.vE[I]) + c.vW[I]) + c.vN[J]) + c.vS[J];
+}
+
+template <class X>
+__device__ __forceinline__ double lhs1_row_f(const Lhs1Coef &c, const Grid &g, int i, const X &x)
+{
+    const int w = g.nx - 1;
+    if (i < g.nU) {
+        int I = i % w, J = i / w;
+        double d = (((1 + c.uE[I]) + c.uW[I]) + c.uN[J]) + c.uS[J];
+        double y = d * x(i);
+        if (I != g.nx - 2) y -= c.uE[I] * x(i + 1);
+        if (I != 0) y -= c.uW[I] * x(i - 1);
+        if (J != g.ny - 1) y -= c.uN[J] * x(i + w);
+        if (J != 0) y -= c.uS[J] * x(i - w);
+        return y;
+    }
+    int k = i - g.nU, I = k % g.nx, J = k / g.nx;
+    double d = (((1 + c.vE[I]) + c.vW[I]) + c.vN[J]) + c.vS[J];
+    double y = d * x(i);
+    if (I != g.nx - 1) y -= c.vE[I] * x(i + 1);
+    if (I != 0) y -= c.vW[I] * x(i - 1);
+    if (J != g.ny - 2) y -= c.vN[J] * x(i + g.nx);
+    if (J != 0) y -= c.vS[J] * x(i - g.nx);
+    return y;
+}
+
+__device__ __forceinline__ double lhs2_diag(const Lhs2Coef &c, const Grid &g, int i)
+{
+    int I = i % g.nx, J = i / g.nx;
+    double d = (((0 + c.E[I]) + c.W[I]) + c.N[J]) + c.S[J];
+    if (i == c.pin0 || i == c.pinc) d += d;
+    return d;
+}
+
+template <class X>
+__device__ __forceinline__ double lhs2_row_f(const Lhs2Coef &c, const Grid &g, int i, const X &x)
+{
+    int I = i % g.nx, J = i / g.nx;
+    double d = (((0 + c.E[I]) + c.W[I]) + c.N[J]) + c.S[J];
+    if (i == c.pin0 || i == c.pinc) d += d;
+    double y = d * x(i);
+    if (I != g.nx - 1) y -= c.E[I] * x(i + 1);
+    if (I != 0) y -= c.W[I] * x(i - 1);
+    if (J != g.ny - 1) y -= c.N[J] * x(i + g.nx);
+    if (J != 0) y -= c.S[J] * x(i - g.nx);
+    return y;
+}
+
+
+struct PtrAccess {
+    const double *__restrict__ p;
+    __device__ __forceinline__ double operator()(int j) const { return p[j]; }
+};
+
+__device__ __forceinline__ double lhs1_row(const Lhs1Coef &c, const Grid &g, int i, const double *__restrict__ x)
+{
+    return lhs1_row_f(c, g, i, PtrAccess{x});
+}
+
+__device__ __forceinline__ double lhs2_row(const Lhs2Coef &c, const Grid &g, int i, const double *__restrict__ x)
+{
+    return lhs2_row_f(c, g, i, PtrAccess{x});
+}
+
+}  // namespace cuibm

@@ -1,0 +1,230 @@
+// Device context of one simulation and the declarations shared by the
+// translation units of libcuibm_gb300.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "config.h"
+#include "geometry.h"
+
+namespace cuibm {
+
+#define CUIBM_TRY(expr)                                                                         \
+    do {                                                                                        \
+        cudaError_t e_ = (expr);                                                                \
+        if (e_ != cudaSuccess) throw CudaError(std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct CudaError {
+    std::string msg;
+    explicit CudaError(const std::string &m) : msg(m) {}
+};
+struct InputError {
+    std::string msg;
+    explicit InputError(const std::string &m) : msg(m) {}
+};
+
+constexpr int kBlock = 256;
+inline int blocks_for(long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
+
+// ---- structured operators --------------------------------------------------
+// 1-D coefficient tables of the separable 5-point operators.  Index ranges are
+// noted per array; every value is computed on the host with the reference's
+// formula and operation order.
+struct Lhs1Coef {
+    // u rows: E/W depend on I (0..nx-2), N/S on J (0..ny-1, boundary spacing folded in)
+    const double *uE, *uW, *uN, *uS;
+    // v rows: E/W on I (0..nx-1), N/S on J (0..ny-2)
+    const double *vE, *vW, *vN, *vS;
+};
+struct Lhs2Coef {
+    const double *E, *W;  // on I (0..nx-1), zero where the neighbour is missing
+    const double *N, *S;  // on J (0..ny-1)
+    int pin0, pinc;       // doubled diagonals: cell 0 and (if >= 0) the centre cell
+};
+struct Grid {
+    int nx, ny, nU, nV, nUV, nP;
+};
+
+// explicit-term metric tables for the fused RHS kernel (convection/diffusion)
+struct RhsCoef {
+    // u nodes, per I (0..nx-2)
+    const double *uxE, *uxW, *uxC, *uxA;   // convection x-part, v-bar weight a/(a+b)
+    const double *ulE, *ulW;               // diffusion 1/(dx[I+1](dx[I+1]+dx[I])/2), 1/(dx[I](..)/2)
+    // u nodes, per J (0..ny-1), boundary spacing folded in
+    const double *uyN, *uyS, *uyC;
+    const double *ulN, *ulS;               // diffusion (2/dy^2 at the top/bottom walls)
+    // v nodes, per I (0..nx-1)
+    const double *vxE, *vxW, *vxC;
+    const double *vlE, *vlW;
+    // v nodes, per J (0..ny-2)
+    const double *vyN, *vyS, *vyC, *vyA;   // v-bar weight c/(c+d) for u at v nodes
+    const double *vlN, *vlS;
+    const double *dx, *dy;
+};
+
+// ---- Krylov state living in device memory -------------------------------------
+enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3 };
+struct KrylovScalars {
+    double rho, alpha, omega, beta;
+    double bnorm, tol, rnorm, snorm;
+    double rtol, pad0;
+    int it, maxit, status, s_done;
+    unsigned int arrive;  // last-block-done counter of the fused reductions
+    int pad;
+};
+
+struct SaLevel;  // amg.cu
+
+struct LinearSystem {
+    int which = 1;  // 1 = LHS1 (velocity), 2 = LHS2 (Poisson)
+    int n = 0;
+    int krylov = 0, precond = 0;
+    double rtol = 1e-5;
+    int maxit = 1000;
+    // workspaces
+    double *r = nullptr, *rs = nullptr, *p = nullptr, *Mp = nullptr, *AMp = nullptr, *s = nullptr, *Ms = nullptr,
+           *AMs = nullptr, *z = nullptr, *q = nullptr;
+    double *dinv = nullptr;      // Jacobi of the (possibly symmetrised) operator
+    double *w = nullptr;         // CG symmetrisation weights (row scaling), n
+    double *partials = nullptr;  // per-block partial sums, 4 per block
+    KrylovScalars *ks = nullptr; // device
+    std::vector<SaLevel *> amg;  // SA hierarchy (Poisson)
+    int last_iterations = 0;
+};
+
+struct Timer {
+    double ms = 0;
+    int count = 0;
+};
+
+struct IbArrays {
+    int *ghostUV, *hybridUV, *hybrid2UV, *ghostP, *hybridP;
+    double *biX, *biY, *ipX, *ipY;        // numUV
+    double *bipX, *bipY, *ippX, *ippY;    // numP
+    double *distNode, *distBetween, *distU, *distV, *uvBody;  // Fadlun distances (numUV / numP)
+    double *ustar, *pstar, *dpdn, *biP, *imageValue;
+    int *gIdx, *hIdx, *gpIdx, *hpIdx;     // 4 per node
+    double *gCoef, *hCoef, *gpCoef, *hpCoef;
+    double *gnValue;                      // staging of ghost values (snapshot semantics)
+    // tagging work records
+    void *tagRec;
+    // body (device)
+    double *bx, *by, *uB, *vB, *uBk, *vBk, *bdx, *bdy;
+    // force partial sums
+    double *forcePart;
+    double *forceOut;  // [fx, fy]
+    double *motion;    // [midX, midY, centerVelocityU, centerVelocityV, midX0, midY0, U0, V0]
+};
+
+struct Context {
+    Params P;
+    Axis gx, gy;
+    BodyState body;
+    BoundingBox bb;
+    Grid g{};
+    int device = 0;
+    cudaStream_t stream = nullptr, side_stream = nullptr;
+    int *err_word = nullptr;          // device: first failing solve, system*16 + status
+    int *step_counter_dev = nullptr;  // device copy of timeStep (read by the body motion)
+    std::vector<double> htab;         // host copy of the metric tables (see upload_ns_tables)
+    std::map<std::string, size_t> hoff;
+    std::string err;
+    bool created = false, initialised = false;
+    int timeStep = 0;
+
+    // device memory: one arena carved into 256-byte aligned slices
+    char *arena = nullptr;
+    size_t arena_bytes = 0, arena_used = 0;
+
+    double *u, *uhat, *uold, *N, *Nold, *L, *bc1, *rhs1;
+    double *p, *p_old, *rhs2, *cfl, *work_x, *work_y;
+    double *bc[4];
+    double *x, *dx, *xu, *xv, *y, *dy, *yu, *yv;
+    RhsCoef rc{};
+    Lhs1Coef l1{};
+    Lhs2Coef l2{};
+    double *gradU, *gradV;  // projection: dt / (0.5 dx[I+1] + 0.5 dx[I]), dt / (0.5 dy[J+1] + 0.5 dy[J])
+    LinearSystem sys1, sys2;
+    IbArrays ib{};
+    bool has_body = false;
+    bool ib_dirty = false;
+    double cfl_max = 0;
+    double forceX = 0, forceY = 0;
+
+    // host mirrors read back once per step
+    double *h_scalars = nullptr;  // pinned: [it1, it2, fx, fy, status1, status2]
+    std::map<std::string, Timer> timers;
+    bool profile_phases = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // CUDA graph of one step
+    bool use_graph = true;
+    cudaGraphExec_t step_exec = nullptr;
+    cudaGraph_t step_graph = nullptr;
+
+    // output files
+    FILE *iterationsFile = nullptr, *forceFile = nullptr, *midPositionFile = nullptr;
+
+    template <class T>
+    T *carve(size_t count)
+    {
+        size_t bytes = ((count * sizeof(T)) + 255) & ~size_t(255);
+        if (arena_used + bytes > arena_bytes) throw CudaError("device arena exhausted");
+        T *p_ = reinterpret_cast<T *>(arena + arena_used);
+        arena_used += bytes;
+        return p_;
+    }
+};
+
+// ---- entry points between translation units ----------------------------------
+// ns_kernels.cu
+void upload_ns_tables(Context &c);
+void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val);
+void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
+                       std::vector<double> &val);
+void launch_rhs1(Context &c, bool debug_terms);
+void launch_rhs2(Context &c, const double *uh);
+void launch_project(Context &c);
+void launch_initial_velocity(Context &c);
+void launch_apply(Context &c, int which, const double *xin, double *yout);
+void launch_cfl(Context &c);
+void launch_copy(Context &c, double *dst, const double *src, int n);
+
+// krylov.cu
+void setup_system(Context &c, LinearSystem &S);
+void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool in_graph);
+int read_solve_status(Context &c, LinearSystem &S, int *iterations);
+
+// amg.cu
+void build_sa_hierarchy(Context &c, LinearSystem &S);
+void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z);
+void free_sa_hierarchy(LinearSystem &S);
+
+// ib_kernels.cu
+void setup_ib(Context &c);
+void launch_tag_points(Context &c);
+void launch_ghost_velocity(Context &c, double *field, bool set);
+void launch_hybrid_velocity(Context &c, const double *field);
+void launch_set_inside(Context &c, double *field);
+void launch_weight_uhat(Context &c);
+void launch_hybrid_pressure(Context &c);
+void launch_ghost_pressure(Context &c, bool set);
+void launch_weight_pressure(Context &c);
+void launch_robin(Context &c);
+void launch_force(Context &c);
+void launch_body_motion(Context &c, double t);
+void launch_body_pre_step(Context &c);
+void launch_step_counter(Context &c);
+void initialise_body(Context &c);
+
+// io.cpp / fields.cu
+void write_grid_file(Context &c);
+void write_step_output(Context &c);
+void *field_pointer(Context &c, int field, size_t *bytes);
+void field_changed(Context &c, int field);
+
+}  // namespace cuibm

@@ -1,0 +1,172 @@
+/*
+ * cuibm.h - C ABI of the GB300-native fractional-step solver (libcuibm_gb300.so).
+ *
+ * This is the drop-in boundary for cuIBM's solver classes.  A case folder holds
+ * the same four files the reference reads (simParams.yaml, flow.yaml,
+ * domain.yaml, bodies.yaml) and the same command-line overrides apply.  One
+ * context = one simulation on one GPU and one CUDA stream; a context is not
+ * thread-safe, several contexts may coexist.  No entry point exits or aborts:
+ * each returns a cuibm_status and cuibm_last_error() gives the message.
+ *
+ * Reference interfaces replaced (paths inside the cuIBM source tree):
+ *   cuibm_create      src/io/io.cu:108-138 readInputs (+ defaults io.cu:145-197,
+ *                     command line io.cu:207-299) and the solver switch src/cuIBM.cu:42-60
+ *   cuibm_initialise  NavierStokesSolver::initialise (NavierStokesSolver.cu:34-40),
+ *                     luo_base::initialise (luo_base.cu:28-107), luoIBM::initialise (luoIBM.cu:27-52)
+ *   cuibm_step        NavierStokesSolver::stepTime (NavierStokesSolver.cu:163-188),
+ *                     luo_base::stepTime (luo_base.cu:208-233)
+ *   cuibm_finished    NavierStokesSolver::finished (NavierStokesSolver.cu:195-199)
+ *   cuibm_write_data  NavierStokesSolver::writeData/writeCommon (NavierStokesSolver.cu:339-363),
+ *                     luoIBM::writeData (luoIBM.cu:69-80), luo_base::writeCommon (luo_base.cu:180-206)
+ *   cuibm_shutdown    NavierStokesSolver::shutDown (NavierStokesSolver.cu:368-372)
+ *   cuibm_get_field   the protected members u, uhat, pressure, ... (NavierStokesSolver.h:28-123,
+ *                     luo_base.h tag and interpolation arrays)
+ *   cuibm_get_forces  bodies::forceX/forceY after luo_base::calculateForce (calculateForce.cu:21-74)
+ *   cuibm_run         one phase or kernel group of the step (the reference's
+ *                     generateRHS1/solveIntermediateVelocity/generateRHS2/... methods)
+ */
+#ifndef CUIBM_H
+#define CUIBM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cuibm_ctx cuibm_ctx;
+
+typedef enum {
+    CUIBM_OK = 0,
+    CUIBM_ERR_BAD_INPUT = 1,     /* malformed case file, bad argument or size */
+    CUIBM_ERR_IO = 2,            /* a case or output file could not be opened */
+    CUIBM_ERR_CUDA = 3,          /* a CUDA runtime call failed */
+    CUIBM_ERR_NOT_CONVERGED = 4, /* a linear solve hit maxIterations (reference: std::exit(-1)) */
+    CUIBM_ERR_NAN = 5,           /* a non-finite residual appeared in a solve */
+    CUIBM_ERR_STATE = 6,         /* call out of order (e.g. step before initialise) */
+    CUIBM_ERR_UNSUPPORTED = 7    /* a configuration this build does not implement */
+} cuibm_status;
+
+/* solver types, same order and names as the reference's src/types.h */
+enum { CUIBM_NAVIER_STOKES = 0, CUIBM_FADLUN = 1, CUIBM_OSC_CYLINDER = 2, CUIBM_FSI = 3, CUIBM_LUO = 4 };
+
+typedef struct {
+    int nx, ny, numU, numV, numUV, numP;
+    int solver_type;
+    int time_step, nt, nsave;
+    double dt, nu;
+    int total_points;                 /* body points (0 without a body) */
+    int bb_start_i, bb_start_j, bb_ncx, bb_ncy; /* scaled bounding box of body 0 */
+    int nnz_lhs1, nnz_lhs2;           /* entries of the reference's COO matrices */
+    int velocity_precond, poisson_precond;   /* 0 NONE 1 DIAGONAL 2 SMOOTHED_AGGREGATION 3 AINV */
+    int velocity_krylov, poisson_krylov;     /* 0 BiCGSTAB, 1 CG */
+    int amg_levels;                   /* levels of the Poisson SA hierarchy (0 if none) */
+} cuibm_info;
+
+/* Fields readable/writable through cuibm_get_field / cuibm_set_field.
+ * D = double, I = int32.  Sizes: UV = numUV, P = numP. */
+enum {
+    CUIBM_F_U = 0,        /* D UV  velocity u^{n+1} (u block then v block) */
+    CUIBM_F_UHAT,         /* D UV  intermediate velocity */
+    CUIBM_F_UOLD,         /* D UV  previous velocity */
+    CUIBM_F_P,            /* D P   pressure */
+    CUIBM_F_P_OLD,        /* D P   previous pressure */
+    CUIBM_F_N,            /* D UV  convection term of the current step */
+    CUIBM_F_NOLD,         /* D UV  convection term of the previous step */
+    CUIBM_F_L,            /* D UV  explicit diffusion term (written by CUIBM_OP_RHS1_TERMS) */
+    CUIBM_F_BC1,          /* D UV  implicit-diffusion boundary term (CUIBM_OP_RHS1_TERMS) */
+    CUIBM_F_RHS1,         /* D UV  */
+    CUIBM_F_RHS2,         /* D P   */
+    CUIBM_F_BC_XMINUS,    /* D 2ny-1 */
+    CUIBM_F_BC_XPLUS,     /* D 2ny-1 */
+    CUIBM_F_BC_YMINUS,    /* D 2nx-1 */
+    CUIBM_F_BC_YPLUS,     /* D 2nx-1 */
+    CUIBM_F_X, CUIBM_F_DX, CUIBM_F_XU, CUIBM_F_XV,   /* D nx, nx, nx-1, nx */
+    CUIBM_F_Y, CUIBM_F_DY, CUIBM_F_YU, CUIBM_F_YV,   /* D ny, ny, ny, ny-1 */
+    CUIBM_F_BODY_X, CUIBM_F_BODY_Y,                  /* D total_points */
+    CUIBM_F_BODY_UB, CUIBM_F_BODY_VB,                /* D total_points */
+    CUIBM_F_GHOST_TAGS_UV,  /* I UV */
+    CUIBM_F_HYBRID_TAGS_UV, /* I UV */
+    CUIBM_F_HYBRID_TAGS_UV2,/* I UV */
+    CUIBM_F_GHOST_TAGS_P,   /* I P  */
+    CUIBM_F_HYBRID_TAGS_P,  /* I P  */
+    CUIBM_F_BI_X, CUIBM_F_BI_Y, CUIBM_F_IP_X, CUIBM_F_IP_Y,      /* D UV body intercept / image point */
+    CUIBM_F_BIP_X, CUIBM_F_BIP_Y, CUIBM_F_IPP_X, CUIBM_F_IPP_Y,  /* D P  same for pressure nodes */
+    CUIBM_F_DIST_NODE, CUIBM_F_DIST_BETWEEN, CUIBM_F_UV_BODY,    /* D UV Fadlun distances, body velocity */
+    CUIBM_F_USTAR,          /* D UV hybrid-node interpolated velocity */
+    CUIBM_F_PSTAR,          /* D P  hybrid-node interpolated pressure */
+    CUIBM_F_DPDN,           /* D P  ghost-node pressure normal-derivative term */
+    CUIBM_F_BI_P,           /* D P  pressure at the body intercept (ghost nodes) */
+    /* interpolation stencils: 4 corner indices (I, 4 per node) and 4 weights (D, 4 per node),
+     * stored per node class; index = node index, entries [4*node .. 4*node+3] */
+    CUIBM_F_GHOST_UV_INDEX,  CUIBM_F_GHOST_UV_COEF,   /* size 4*UV */
+    CUIBM_F_HYBRID_UV_INDEX, CUIBM_F_HYBRID_UV_COEF,  /* size 4*UV */
+    CUIBM_F_GHOST_P_INDEX,   CUIBM_F_GHOST_P_COEF,    /* size 4*P  */
+    CUIBM_F_HYBRID_P_INDEX,  CUIBM_F_HYBRID_P_COEF,   /* size 4*P  */
+    CUIBM_F_IMAGE_VALUE_UV,  /* D UV value interpolated at the image point */
+    CUIBM_F_CFL,             /* D P  */
+    CUIBM_F_WORK_X,          /* D max(UV,P) operator test input  */
+    CUIBM_F_WORK_Y,          /* D max(UV,P) operator test output */
+    CUIBM_F_COUNT
+};
+
+/* Phases and kernel groups for cuibm_run (state in, state out). */
+enum {
+    CUIBM_OP_RHS1_TERMS = 0,   /* N, L, bc1, rhs1 from u and Nold (writes all four) */
+    CUIBM_OP_GENERATE_RHS1,    /* the method's full generateRHS1 (IB interpolation included) */
+    CUIBM_OP_SOLVE_VELOCITY,   /* LHS1 uhat = rhs1 */
+    CUIBM_OP_WEIGHT_UHAT,      /* external method: blend uhat with ustar at hybrid nodes */
+    CUIBM_OP_GENERATE_RHS2,    /* the method's full generateRHS2 */
+    CUIBM_OP_RHS2,             /* rhs2 = -D uhat only */
+    CUIBM_OP_SOLVE_POISSON,    /* LHS2 p = rhs2 */
+    CUIBM_OP_WEIGHT_PRESSURE,  /* external method: hybrid/ghost pressure interpolation and blend */
+    CUIBM_OP_PROJECT,          /* u = uhat - dt G p, uold = u (plain projection only) */
+    CUIBM_OP_PROJECT_VELOCITY, /* the method's full projection phase */
+    CUIBM_OP_UPDATE_BODY,      /* force, motion, bounding box, tagging, CFL */
+    CUIBM_OP_APPLY_LHS1,       /* WORK_Y = LHS1 WORK_X */
+    CUIBM_OP_APPLY_LHS2,       /* WORK_Y = LHS2 WORK_X */
+    CUIBM_OP_TAG_POINTS,       /* tagging of u, v, p nodes */
+    CUIBM_OP_GHOST_VELOCITY_U, /* interpolate u to ghost nodes and set them (set=true) */
+    CUIBM_OP_GHOST_VELOCITY_UHAT, /* same on uhat */
+    CUIBM_OP_HYBRID_VELOCITY,  /* ustar at hybrid nodes from u */
+    CUIBM_OP_HYBRID_PRESSURE,  /* pstar at hybrid pressure nodes */
+    CUIBM_OP_GHOST_PRESSURE,   /* ghost pressure values (set=true) */
+    CUIBM_OP_SET_INSIDE,       /* u inside the body := body velocity */
+    CUIBM_OP_ROBIN_BOUNDARY,   /* convective outflow update of the x+ boundary */
+    CUIBM_OP_FORCE,            /* control-volume force on body 0 */
+    CUIBM_OP_CFL,              /* CFL field */
+    CUIBM_OP_COUNT
+};
+
+int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx **out);
+int cuibm_initialise(cuibm_ctx *ctx);
+int cuibm_step(cuibm_ctx *ctx, int nsteps);
+int cuibm_finished(const cuibm_ctx *ctx);
+int cuibm_write_data(cuibm_ctx *ctx);
+int cuibm_shutdown(cuibm_ctx *ctx);
+void cuibm_destroy(cuibm_ctx *ctx);
+const char *cuibm_last_error(const cuibm_ctx *ctx);
+
+int cuibm_get_info(const cuibm_ctx *ctx, cuibm_info *info);
+/* copy a field; bytes must equal the field size; *_on_device != 0 means the
+ * caller's pointer is device memory of the context's GPU */
+int cuibm_get_field(cuibm_ctx *ctx, int field, void *dst, size_t bytes, int dst_on_device);
+int cuibm_set_field(cuibm_ctx *ctx, int field, const void *src, size_t bytes, int src_on_device);
+int cuibm_get_forces(cuibm_ctx *ctx, double *fx, double *fy);
+int cuibm_get_iterations(cuibm_ctx *ctx, int *velocity_iterations, int *poisson_iterations);
+/* The reference's COO matrix for system 1 (LHS1) or 2 (LHS2), entries in the
+ * reference's order; arrays of length info.nnz_lhs1 / nnz_lhs2. */
+int cuibm_get_matrix(cuibm_ctx *ctx, int system, int *row, int *col, double *val, size_t nnz);
+int cuibm_run(cuibm_ctx *ctx, int op);
+/* the context's cudaStream_t, for callers that order their own work after it */
+int cuibm_get_stream(cuibm_ctx *ctx, void **stream);
+/* accumulated device time (ms) and count of a named phase; names as the
+ * reference Logger: "Intermediate Velocity Setup", "Intermediate Velocity Solve",
+ * "Poisson Setup", "Poisson Solve", "Velocity Projection", "Update Solver", ... */
+int cuibm_get_timer(cuibm_ctx *ctx, const char *name, double *ms, int *count);
+int cuibm_set_option(cuibm_ctx *ctx, const char *key, double value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUIBM_H */

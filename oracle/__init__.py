@@ -1,0 +1,315 @@
+"""CPU oracle of the fractional-step path (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+legs use this package, as the checker or the CPU baseline.  The product
+(cuibm_gb300) never imports it.
+
+liboracle.so (oracle/*.c) is a plain-C restatement of the reference's kernels
+and of the CUSP Krylov solvers it calls; this module wraps it with numpy and
+restates the host orchestration of a time step (NavierStokesSolver::stepTime,
+NavierStokesSolver.cu:163-188).  The restatement is pinned bit-for-bit against
+the reference's own kernel code by the golden fixtures in tests/golden.
+"""
+import ctypes
+import json
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_KERNELS = os.path.join(HERE, "_ref", "libcuibm_refkernels.so")
+REF_IO = os.path.join(HERE, "_ref", "libcuibm_refio.so")
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def build(ref=False):
+    """Compile liboracle.so (and, with ref=True, the reference-derived _ref libraries)."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["all", "ref"] if ref else ["all"]), check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = ctypes.CDLL(LIB)
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+# case files (the JSON twins that cuibm_gb300.cases writes next to the YAML)
+# ---------------------------------------------------------------------------
+def load_case(folder):
+    def rd(n):
+        with open(os.path.join(folder, n + ".json")) as f:
+            return json.load(f)
+    return rd("simParams"), rd("flow"), rd("domain"), rd("bodies")
+
+
+def axis_arrays(ax):
+    """(centres, widths, faces) of one domain axis (io/parseDomainFile.cu)."""
+    L = lib()
+    ends = f64([s["end"] for s in ax["subDomains"]])
+    ratios = f64([s["stretchRatio"] for s in ax["subDomains"]])
+    L.or_axis_count.restype = ctypes.c_int
+    L.or_axis_count.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp]
+    n = L.or_axis_count(float(ax["start"]), float(ax["mid_h"]), len(ends), _d(ends), _d(ratios))
+    c, w, face = np.zeros(n), np.zeros(n), np.zeros(n - 1)
+    L.or_axis_fill.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
+    L.or_axis_fill(float(ax["start"]), float(ax["mid_h"]), len(ends), _d(ends), _d(ratios), _d(c), _d(w), _d(face))
+    return c, w, face
+
+
+class Grid:
+    def __init__(self, domain):
+        xs = [a for a in domain if a["direction"] == "x"][0]
+        ys = [a for a in domain if a["direction"] == "y"][0]
+        self.x, self.dx, self.xu = axis_arrays(xs)
+        self.y, self.dy, self.yv = axis_arrays(ys)
+        self.xv, self.yu = self.x.copy(), self.y.copy()
+        self.nx, self.ny = len(self.x), len(self.y)
+        self.nU = (self.nx - 1) * self.ny
+        self.nV = self.nx * (self.ny - 1)
+        self.nUV = self.nU + self.nV
+        self.nP = self.nx * self.ny
+
+    @classmethod
+    def from_arrays(cls, x, dx, xu, y, dy, yv):
+        g = cls.__new__(cls)
+        g.x, g.dx, g.xu, g.y, g.dy, g.yv = map(f64, (x, dx, xu, y, dy, yv))
+        g.xv, g.yu = g.x.copy(), g.y.copy()
+        g.nx, g.ny = len(g.x), len(g.y)
+        g.nU = (g.nx - 1) * g.ny
+        g.nV = g.nx * (g.ny - 1)
+        g.nUV = g.nU + g.nV
+        g.nP = g.nx * g.ny
+        return g
+
+
+def boundary_arrays(flow, nx, ny):
+    """bc[XMINUS..YPLUS] (NavierStokesSolver.cu:104-128)."""
+    val = {}
+    for b in flow[0]["boundaryConditions"]:
+        val[b["location"]] = (float(b["u"][1]), float(b["v"][1]))
+    xm, xp = np.zeros(2 * ny - 1), np.zeros(2 * ny - 1)
+    ym, yp = np.zeros(2 * nx - 1), np.zeros(2 * nx - 1)
+    ym[:nx - 1], yp[:nx - 1] = val["yMinus"][0], val["yPlus"][0]
+    ym[nx - 1:], yp[nx - 1:] = val["yMinus"][1], val["yPlus"][1]
+    xm[:ny], xp[:ny] = val["xMinus"][0], val["xPlus"][0]
+    xm[ny:], xp[ny:] = val["xMinus"][1], val["xPlus"][1]
+    return xm, xp, ym, yp
+
+
+# ---------------------------------------------------------------------------
+# kernels
+# ---------------------------------------------------------------------------
+def _sig(name, *args, restype=None):
+    fn = getattr(lib(), name)
+    fn.argtypes = list(args)
+    fn.restype = restype
+    return fn
+
+
+D, I_, INT = ctypes.c_double, ctypes.c_int, ctypes.c_int
+
+
+def generate_N(u, g, bc):
+    N = np.zeros(g.nUV)
+    xm, xp, ym, yp = bc
+    _sig("or_generateN", _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT)(
+        _d(N), _d(u), _d(g.dx), _d(g.dy), _d(ym), _d(yp), _d(xm), _d(xp), g.nx, g.ny)
+    return N
+
+
+def generate_L(u, g, bc, nu):
+    L = np.zeros(g.nUV)
+    xm, xp, ym, yp = bc
+    _sig("or_generateL", _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, D)(
+        _d(L), _d(u), _d(g.dx), _d(g.dy), _d(ym), _d(yp), _d(xm), _d(xp), g.nx, g.ny, nu)
+    return L
+
+
+def generate_bc1(u, g, bc, nu, dt):
+    b1 = np.zeros(g.nUV)
+    xm, xp, ym, yp = bc
+    _sig("or_generateBC1", _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, D, D, INT, INT)(
+        _d(u), _d(b1), _d(ym), _d(yp), _d(xm), _d(xp), _d(g.dx), _d(g.dy), nu, dt, g.nx, g.ny)
+    return b1
+
+
+def generate_rhs(L, Nold, N, u, bc1, dt):
+    r = np.zeros(len(u))
+    _sig("or_generateRHS", _dp, _dp, _dp, _dp, _dp, _dp, D, INT)(
+        _d(r), _d(L), _d(Nold), _d(N), _d(u), _d(bc1), dt, len(u))
+    return r
+
+
+def lhs1_coo(g, dt, nu):
+    nnz = (g.nx - 1) * g.ny * 5 - 2 * g.ny - 2 * (g.nx - 1) + (g.ny - 1) * g.nx * 5 - 2 * (g.ny - 1) - 2 * g.nx
+    row, col, val = np.zeros(nnz, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+    _sig("or_lhs1_coo", _ip, _ip, _dp, _dp, _dp, D, D, INT, INT)(
+        _i(row), _i(col), _d(val), _d(g.dx), _d(g.dy), dt, nu, g.nx, g.ny)
+    return row, col, val
+
+
+def lhs2_coo(g, dt, centre_pin=True):
+    nnz = 5 * g.nx * g.ny - 2 * g.ny - 2 * g.nx
+    row, col, val = np.zeros(nnz, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+    _sig("or_lhs2_coo", INT, _ip, _ip, _dp, _dp, _dp, INT, INT, D)(
+        int(centre_pin), _i(row), _i(col), _d(val), _d(g.dx), _d(g.dy), g.nx, g.ny, dt)
+    return row, col, val
+
+
+def generate_rhs2(uhat, g, bc):
+    r = np.zeros(g.nP)
+    xm, xp, ym, yp = bc
+    _sig("or_generateRHS2", _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT)(
+        _d(r), _d(uhat), _d(ym), _d(yp), _d(xm), _d(xp), _d(g.dx), _d(g.dy), g.nx, g.ny)
+    return r
+
+
+def project(u, uhat, p, g, dt):
+    u = u.copy()
+    uold = np.zeros(g.nUV)
+    _sig("or_project", _dp, _dp, _dp, _dp, _dp, _dp, D, INT, INT)(
+        _d(u), _d(uhat), _d(uold), _d(p), _d(g.dx), _d(g.dy), dt, g.nx, g.ny)
+    return u, uold
+
+
+def initial_velocity(g, uI, vI, uP=0.0, vP=0.0):
+    u = np.zeros(g.nUV)
+    _sig("or_initialiseVelocity", _dp, _dp, _dp, _dp, _dp, D, D, D, D, D, D, D, D, INT, INT)(
+        _d(u), _d(g.xu), _d(g.yu), _d(g.xv), _d(g.yv), uI, vI, uP, vP, g.x[-1], g.x[0], g.y[-1], g.y[0], g.nx, g.ny)
+    return u
+
+
+def cfl(u, g, dt):
+    c = np.zeros(g.nP)
+    _sig("or_calculateCFL", _dp, _dp, _dp, _dp, INT, INT, D)(_d(c), _d(u), _d(g.dx), _d(g.dy), g.nx, g.ny, dt)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# sparse solves
+# ---------------------------------------------------------------------------
+class Csr:
+    def __init__(self, n, row, col, val):
+        self.n = n
+        self.ptr = np.zeros(n + 1, np.int32)
+        self.col = np.zeros(len(row), np.int32)
+        self.val = np.zeros(len(row))
+        _sig("or_coo_to_csr", INT, INT, _ip, _ip, _dp, _ip, _ip, _dp)(
+            n, len(row), _i(np.ascontiguousarray(row, np.int32)), _i(np.ascontiguousarray(col, np.int32)),
+            _d(f64(val)), _i(self.ptr), _i(self.col), _d(self.val))
+
+    def scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.ptr), shape=(self.n, self.n))
+
+    def matvec(self, x):
+        y = np.zeros(self.n)
+        _sig("or_csr_spmv", INT, _ip, _ip, _dp, _dp, _dp)(self.n, _i(self.ptr), _i(self.col), _d(self.val),
+                                                          _d(f64(x)), _d(y))
+        return y
+
+
+def bicgstab(A, b, x, rtol, maxit, precond=1):
+    """Right-preconditioned BiCGSTAB under cusp::monitor semantics; returns (x, iters, converged)."""
+    x = f64(x).copy()
+    res = ctypes.c_double()
+    it = _sig("or_bicgstab", INT, _ip, _ip, _dp, _dp, _dp, D, INT, INT, ctypes.c_void_p, _dp, restype=INT)(
+        A.n, _i(A.ptr), _i(A.col), _d(A.val), _d(f64(b)), _d(x), rtol, maxit, precond, None, ctypes.byref(res))
+    return x, abs(it) - (1 if it < 0 else 0), it >= 0
+
+
+def direct_solve(A, b):
+    import scipy.sparse.linalg as spla
+    return spla.spsolve(A.scipy().tocsc(), f64(b))
+
+
+# ---------------------------------------------------------------------------
+# step orchestration of the plain solver (NavierStokesSolver::stepTime)
+# ---------------------------------------------------------------------------
+class PlainSolver:
+    """NAVIER_STOKES_SOLVER on the CPU.  solve='direct' solves both systems
+    exactly (sparse LU) so that fields can be compared with any converged
+    solver; solve='krylov' uses the case's BiCGSTAB tolerances."""
+
+    def __init__(self, folder=None, grid=None, flow=None, nu=None, dt=None, sim=None, solve="direct"):
+        if folder is not None:
+            sim_, flow_, dom, _ = load_case(folder)
+            sim = sim or sim_[0]
+            flow = flow or flow_
+            grid = grid or Grid(dom)
+            nu = nu if nu is not None else float(flow_[0]["nu"])
+            dt = dt if dt is not None else float(sim_[0]["dt"])
+        self.g, self.nu, self.dt, self.sim = grid, nu, dt, sim
+        self.bc = boundary_arrays(flow, grid.nx, grid.ny)
+        f0 = flow[0]
+        ip = f0.get("initialPerturbation", [0.0, 0.0])
+        self.u = initial_velocity(grid, float(f0["initialVelocity"][0]), float(f0["initialVelocity"][1]),
+                                  float(ip[0]), float(ip[1]))
+        self.uhat = self.u.copy()
+        self.uold = np.zeros(grid.nUV)
+        self.N = np.zeros(grid.nUV)
+        self.Nold = np.zeros(grid.nUV)
+        self.p = np.zeros(grid.nP)
+        self.A1 = Csr(grid.nUV, *lhs1_coo(grid, dt, nu))
+        self.A2 = Csr(grid.nP, *lhs2_coo(grid, dt, centre_pin=True))
+        self.solve = solve
+        self.timeStep = 0
+        self.iters = (0, 0)
+        if solve == "direct":
+            import scipy.sparse.linalg as spla
+            self._lu1 = spla.splu(self.A1.scipy().tocsc())
+            self._lu2 = spla.splu(self.A2.scipy().tocsc())
+
+    def _tol(self, system):
+        for s in self.sim.get("linearSolvers", []):
+            if s["system"] == system:
+                return float(s.get("tolerance", 1e-5)), int(s.get("maxIterations", 10000))
+        return 1e-5, 10000
+
+    def step(self):
+        g, bc = self.g, self.bc
+        self.Nold = self.N
+        self.N = generate_N(self.u, g, bc)
+        L = generate_L(self.u, g, bc, self.nu)
+        b1 = generate_bc1(self.u, g, bc, self.nu, self.dt)
+        rhs1 = generate_rhs(L, self.Nold, self.N, self.u, b1, self.dt)
+        if self.solve == "direct":
+            self.uhat = self._lu1.solve(rhs1)
+        else:
+            tol, mx = self._tol("velocity")
+            self.uhat, it1, ok = bicgstab(self.A1, rhs1, self.uhat, tol, mx, 1)
+        rhs2 = generate_rhs2(self.uhat, g, bc)
+        if self.solve == "direct":
+            self.p = self._lu2.solve(rhs2)
+        else:
+            tol, mx = self._tol("Poisson")
+            self.p, it2, ok = bicgstab(self.A2, rhs2, self.p, tol, mx, 1)
+        self.u, self.uold = project(self.u, self.uhat, self.p, g, self.dt)
+        self.timeStep += 1
+
+
+def circle_points(cx, cy, R, n):
+    X, Y = np.zeros(n), np.zeros(n)
+    _sig("or_circle_points", D, D, D, INT, _dp, _dp)(cx, cy, R, n, _d(X), _d(Y))
+    return X, Y
