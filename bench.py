@@ -1,0 +1,297 @@
+"""Benchmark: Mcell-steps/s of the fractional-step time step on one GB300.
+
+A "step" is one full time step of the solver (NavierStokesSolver::stepTime /
+luo_base::stepTime): explicit RHS, velocity solve, Poisson solve, projection
+and, for immersed-boundary cases, the ghost-node interpolation, blending,
+force, motion and tagging.  Mcell-steps/s = pressure cells x steps / seconds.
+
+Workloads (synthetic inputs generated from the project's case presets):
+  cylinder_re40  impulsively started cylinder, Re 40, external (Luo) method,
+                 [-15,15]^2, h = 0.02 core stretched by 1.03 (270 x 270), 157 points,
+                 dt 0.01, plain FP64 (the default: the headline configuration)
+  cavity64       lid-driven cavity 64 x 64, Re 100, dt 0.01, plain FP64
+
+Timing: W warm-up steps, then K steps, each timed with CUDA events on the
+solver's stream; before every timed step a 256 MB buffer is written on that
+stream (outside the events) to flush the 129 MB L2, because the whole working
+set of these grids fits in L2.  --gpus N runs N independent replicas (one per
+GPU, one process each under torchrun); value = total cell-steps / max time.
+
+--impl reference times the reference's algorithm on the host CPU cores: the
+oracle port (oracle/, a C restatement of the reference's kernels and of its
+BiCGSTAB / smoothed-aggregation solvers - the reference itself needs CUSP,
+which is not available, and a GPU build of it cannot be made here).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s"
+
+
+def make_case(workload, folder, tight=False):
+    from cuibm_gb300 import cases
+    if workload == "cavity64":
+        return cases.cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000000, vel_tol=1e-8, pois_tol=1e-8,
+                            pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG"), 64 * 64
+    if workload == "cylinder_re40":
+        f = cases.cylinder(folder, h=0.02, ratio=1.03, points=157, nu=1.0 / 40, dt=0.01, nt=1000000,
+                           vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION")
+        return f, 270 * 270
+    raise SystemExit("unknown workload " + workload)
+
+
+def workload_config(workload):
+    if workload == "cavity64":
+        return {"workload": "lid-driven cavity 64x64, Re 100, plain method", "nx": 64, "ny": 64, "dt": 0.01,
+                "velocity": "BiCGSTAB + diagonal, rtol 1e-8", "poisson": "CG + smoothed aggregation, rtol 1e-8"}
+    return {"workload": "impulsively started cylinder Re 40, external (Luo) ghost-node method, plain FP64",
+            "nx": 270, "ny": 270, "body_points": 157, "dt": 0.01,
+            "velocity": "BiCGSTAB + diagonal, rtol 1e-5", "poisson": "BiCGSTAB + smoothed aggregation, rtol 1e-5"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 8 and p[0].replace(".", "").isdigit():
+                    rows.append(p)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(r[0]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[4 + k] and "Not" not in r[4 + k]})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": float(rows[0][1]), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d.get("hbm_gbs") or d.get("hbm_GBs")), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def reduce_max(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def run_ours(a, rank, world, local, pg):
+    import numpy as np
+    import torch
+
+    import cuibm_gb300 as cb
+
+    torch.cuda.set_device(local)
+    tmp = tempfile.mkdtemp(prefix="cuibm_bench_")
+    folder, cells = make_case(a.workload, os.path.join(tmp, "case"))
+    s = cb.NavierStokesSolver(folder, ["-deviceNumber", str(local)])
+    s.set_option("write_output", 0)
+    s.initialise()
+    stream = torch.cuda.ExternalStream(s.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    s.stepTime(a.warmup)
+    torch.cuda.synchronize()
+    barrier(pg)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for k in range(a.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                evs[k][0].record(stream)
+            s.stepTime(1)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(pg)
+    dev_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    dev_ms = reduce_max(pg, dev_ms)
+    ms_per_step = dev_ms / a.steps
+    value = world * cells * a.steps / (dev_ms * 1e-3) / 1e6
+    it1, it2 = s.iterations()
+
+    # roofline: the dominant kernel, timed with CUDA events on the solver's stream
+    peak, peak_kind = measured_peaks()
+    roof = {}
+    cand = ["rhs1", "apply_lhs2", "apply_lhs1", "rhs2", "project"]
+    if s.info.amg_levels > 0:
+        cand.append("poisson_vcycle")
+    prof = {}
+    for k in cand:
+        ms, b = s.profile_kernel(k, reps=50)
+        prof[k] = (ms, b)
+    dom = a.roofline_kernel if a.roofline_kernel in prof else "rhs1"
+    ms, b = prof[dom]
+    achieved = b / (ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+            "bytes_per_launch": b, "ms_per_launch": ms,
+            "other_kernels": {k: {"ms": round(v[0], 5), "GB/s": round(v[1] / (v[0] * 1e-3) / 1e9, 1)}
+                              for k, v in prof.items()}}
+
+    # end to end through the public API with host buffers: every step uploads the
+    # step's boundary inputs from pinned memory and reads back the fields and forces
+    bnames = ["bc_xminus", "bc_xplus", "bc_yminus", "bc_yplus"]
+    pinned_in = {n: torch.from_numpy(s.get(n)).pin_memory() for n in bnames}
+    out_u = torch.empty(s.info.numUV, dtype=torch.float64).pin_memory()
+    out_p = torch.empty(s.info.numP, dtype=torch.float64).pin_memory()
+    h2d = sum(t.numel() * 8 for t in pinned_in.values())
+    d2h = (out_u.numel() + out_p.numel()) * 8 + 16
+    e2e_steps = max(3, a.steps)
+    torch.cuda.synchronize()
+    barrier(pg)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        for n, t in pinned_in.items():
+            s._check(s._L.cuibm_set_field(s._h, cb.FIELDS[n], t.data_ptr(), t.numel() * 8, 0))
+        s.stepTime(1)
+        s.get_into("u", out_u.data_ptr(), out_u.numel() * 8)
+        s.get_into("p", out_p.data_ptr(), out_p.numel() * 8)
+        s.forces()
+    torch.cuda.synchronize()
+    e2e_s = reduce_max(pg, time.perf_counter() - t0)
+    e2e = {"value": round(world * cells * e2e_steps / e2e_s / 1e6, 3), "unit": METRIC,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    launches = s.launch_count()
+    s.close()
+    return {"value": value, "ms_per_step": ms_per_step, "wall_s": wall, "roofline": roof, "e2e": e2e,
+            "clocks": clk.summary(), "iterations_last_step": [it1, it2], "gpu_launches": launches * a.steps}
+
+
+def cpu_baseline(workload, budget_s=15.0):
+    """The oracle port on the host cores, for a bounded number of steps."""
+    import oracle
+    tmp = tempfile.mkdtemp(prefix="cuibm_cpu_")
+    folder, cells = make_case(workload, os.path.join(tmp, "case"))
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    if workload == "cavity64":
+        solver = oracle.PlainSolver(folder, solve="krylov")
+    else:
+        solver = oracle.LuoSolver(folder)
+    solver.step()  # warm-up (setup)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        solver.step()
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or steps >= 200:
+            break
+    value = cells * steps / el / 1e6
+    return {"value": round(value, 4), "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "%d steps of the same workload after one warm-up step (%.1f s)" % (steps, el)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("CUIBM_BENCH_WORKLOAD", "cylinder_re40"))
+    ap.add_argument("--roofline-kernel", default="rhs1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    rank, world, local, pg = dist_setup(a.gpus)
+    cfg = workload_config(a.workload)
+    cfg.update({"l2": "flushed before every timed step (256 MB write)", "parallelism": "replicas" if world > 1
+                else "single GPU"})
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(a.workload, budget_s=max(10.0, 2.0 * a.steps))
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": a.gpus,
+                "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "dtype": "f64",
+                "data": "synthetic", "config": cfg, "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    r = run_ours(a, rank, world, local, pg)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": round(r["value"], 3), "unit": METRIC, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(r["ms_per_step"], 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "roofline": r["roofline"], "e2e": r["e2e"], "clocks": r["clocks"],
+            "gpu_launches": r["gpu_launches"], "iterations_last_step": r["iterations_last_step"]}
+    if not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(a.workload)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -98,6 +98,11 @@ def library():
         L.cuibm_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
         L.cuibm_get_timer.argtypes = [vp, cp, dp, ctypes.POINTER(ip)]
         L.cuibm_set_option.argtypes = [vp, cp, ctypes.c_double]
+        L.cuibm_case_info.argtypes = [cp, ip, ctypes.POINTER(cp), ctypes.POINTER(Info)]
+        L.cuibm_case_array.argtypes = [cp, ip, ctypes.POINTER(cp), ip, dp, ctypes.c_size_t]
+        L.cuibm_case_error.restype = cp
+        L.cuibm_profile_kernel.argtypes = [vp, cp, ip, dp, dp]
+        L.cuibm_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         _lib = L
     return _lib
 
@@ -235,6 +240,50 @@ class NavierStokesSolver:
     def set_option(self, key, value):
         self._check(self._L.cuibm_set_option(self._h, key.encode(), float(value)))
 
+    def profile_kernel(self, name, reps=20):
+        """(mean ms per launch, algorithmic bytes per launch) of one kernel, CUDA-event timed."""
+        ms, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.cuibm_profile_kernel(self._h, name.encode(), int(reps), ctypes.byref(ms),
+                                                 ctypes.byref(b)))
+        return ms.value, b.value
+
+    def launch_count(self):
+        """Kernels of this library launched by the last step (graph nodes x loop trips)."""
+        n = ctypes.c_longlong()
+        self._check(self._L.cuibm_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
     @property
     def timeStep(self):
         return self.get_info().time_step
+
+
+def _argv(args):
+    argv = [a.encode() if isinstance(a, str) else a for a in args]
+    return len(argv), (ctypes.c_char_p * max(1, len(argv)))(*argv)
+
+
+def case_info(case_folder, args=()):
+    """Parse a case folder on the host only (no GPU): the same Info a solver would report."""
+    L = library()
+    n, arr = _argv(args)
+    info = Info()
+    st = L.cuibm_case_info(str(case_folder).encode(), n, arr, ctypes.byref(info))
+    if st != OK:
+        raise CuibmError(st, L.cuibm_case_error().decode())
+    return info
+
+
+def case_array(case_folder, name, args=()):
+    """Grid or body array of a case, built on the host exactly as the solver builds it."""
+    L = library()
+    info = case_info(case_folder, args)
+    size = {"x": info.nx, "dx": info.nx, "xu": info.nx - 1, "xv": info.nx, "y": info.ny, "dy": info.ny,
+            "yu": info.ny, "yv": info.ny - 1, "body_x": info.total_points, "body_y": info.total_points}[name]
+    out = np.empty(size)
+    n, arr = _argv(args)
+    st = L.cuibm_case_array(str(case_folder).encode(), n, arr, FIELDS[name],
+                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), size)
+    if st != OK:
+        raise CuibmError(st, L.cuibm_case_error().decode())
+    return out

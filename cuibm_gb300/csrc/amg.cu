@@ -326,6 +326,28 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
 }
 
+// Algorithmic bytes of one V-cycle: per level with a coarser one, the smoother
+// and residual read b and write x and r; restriction reads r and the R matrix;
+// prolongation reads the coarse x and P and updates x; the post-smoother reads
+// b and x and writes the result.  Matrices count 12 bytes per entry.
+double sa_vcycle_bytes(const LinearSystem &S)
+{
+    double b = 0;
+    for (size_t l = 0; l < S.amg.size(); ++l) {
+        const SaLevel *L = S.amg[l];
+        if (l + 1 == S.amg.size()) {
+            b += (double)L->n * L->n * 8 + 2.0 * L->n * 8;
+            break;
+        }
+        double nnzP = 0, nnzR = 0;
+        (void)nnzP;
+        (void)nnzR;
+        b += 8.0 * L->n * 8;  // b, x, r (down); x rmw, b, out (up)
+        b += 12.0 * L->P.n * 2.5 + 12.0 * L->R.n * 20;  // approximate matrix traffic
+    }
+    return b;
+}
+
 void free_sa_hierarchy(LinearSystem &S)
 {
     for (SaLevel *L : S.amg) delete L;  // device memory belongs to the context arena

@@ -11,6 +11,7 @@
 // step.  cuibm_step checks the solver status once at the end of the call.
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <sys/stat.h>
 
 #include "../../include/cuibm.h"
@@ -24,7 +25,7 @@ static void alloc_fields(Context &c)
 {
     const Grid &g = c.g;
     const size_t nUV = g.nUV, nP = g.nP, nx = g.nx, ny = g.ny;
-    size_t est = (nUV + nP) * 1800 + (size_t)96 << 20;
+    size_t est = (nUV + nP) * 1800 + ((size_t)96 << 20);
     if (c.has_body) est += (nUV + nP) * 400;
     CUIBM_TRY(cudaMalloc(&c.arena, est));
     c.arena_bytes = est;
@@ -233,6 +234,7 @@ static void build_step_graph(Context &c)
     }
     CUIBM_TRY(cudaStreamEndCapture(c.stream, &c.step_graph));
     CUIBM_TRY(cudaGraphInstantiate(&c.step_exec, c.step_graph, 0));
+    c.static_kernels = count_kernel_nodes(c.step_graph);
 }
 
 }  // namespace cuibm
@@ -619,6 +621,64 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
     return CUIBM_OK;
 }
 
+int cuibm_profile_kernel(cuibm_ctx *h, const char *kernel, int reps, double *avg_ms, double *bytes)
+{
+    if (!h || !h->c.initialised || !kernel || reps <= 0) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        std::string k(kernel);
+        const double UV = c.g.nUV, P = c.g.nP, D = sizeof(double);
+        std::function<void()> launch;
+        double b = 0;
+        if (k == "rhs1") {
+            // production form: u, N in; N, Nold, rhs1 out.  Algorithmic: u, Nold in; N, rhs1 out
+            launch = [&] { launch_rhs1(c, false); };
+            b = 4 * UV * D;
+        } else if (k == "rhs2") {
+            launch = [&] { launch_rhs2(c, c.uhat); };
+            b = UV * D + P * D;
+        } else if (k == "project") {
+            launch = [&] { launch_project(c); };
+            b = 3 * UV * D + P * D;  // uhat, u, p in; u, uold out (u read+write counted once each)
+            b += UV * D;
+        } else if (k == "apply_lhs1") {
+            launch = [&] { launch_apply(c, 1, c.work_x, c.work_y); };
+            b = 2 * UV * D;
+        } else if (k == "apply_lhs2") {
+            launch = [&] { launch_apply(c, 2, c.work_x, c.work_y); };
+            b = 2 * P * D;
+        } else if (k == "poisson_vcycle") {
+            if (c.sys2.amg.empty()) return fail(h, CUIBM_ERR_BAD_INPUT, "the Poisson system has no SA hierarchy");
+            launch = [&] { launch_vcycle(c, c.sys2, c.work_x, c.work_y); };
+            b = sa_vcycle_bytes(c.sys2);
+        } else {
+            return fail(h, CUIBM_ERR_BAD_INPUT, "unknown kernel " + k);
+        }
+        launch();  // warm
+        CUIBM_TRY(cudaEventRecord(c.ev0, c.stream));
+        for (int r = 0; r < reps; ++r) launch();
+        CUIBM_TRY(cudaEventRecord(c.ev1, c.stream));
+        CUIBM_TRY(cudaEventSynchronize(c.ev1));
+        float ms = 0;
+        CUIBM_TRY(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+        if (avg_ms) *avg_ms = ms / reps;
+        if (bytes) *bytes = b;
+    });
+    return CUIBM_OK;
+}
+
+int cuibm_launch_count(cuibm_ctx *h, long long *per_step)
+{
+    if (!h || !h->c.initialised || !per_step) return CUIBM_ERR_STATE;
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        if (!c.step_exec) return fail(h, CUIBM_ERR_STATE, "launch counts need the step graph");
+        *per_step = c.static_kernels + (long long)c.sys1.body_kernels * read_body_runs(c, c.sys1) +
+                    (long long)c.sys2.body_kernels * read_body_runs(c, c.sys2);
+    });
+    return CUIBM_OK;
+}
+
 int cuibm_write_data(cuibm_ctx *h)
 {
     if (!h || !h->c.initialised) return CUIBM_ERR_STATE;
@@ -637,6 +697,89 @@ int cuibm_shutdown(cuibm_ctx *h)
     c.iterationsFile = c.forceFile = c.midPositionFile = nullptr;
     return CUIBM_OK;
 }
+
+struct HostCase {
+    Params P;
+    Axis gx, gy;
+    BodyState body;
+    BoundingBox bb;
+};
+
+static int host_case(const char *folder, int argc, const char **argv, HostCase &hc)
+{
+    std::string err = load_case(folder ? folder : ".", argc, argv, hc.P);
+    if (err.empty()) err = build_axis(hc.P.axis[0], hc.gx);
+    if (err.empty()) err = build_axis(hc.P.axis[1], hc.gy);
+    if (err.empty()) err = build_bodies(hc.P.bodies, hc.body);
+    if (!err.empty()) {
+        g_create_error = err;
+        return err.rfind("cannot open", 0) == 0 ? CUIBM_ERR_IO : CUIBM_ERR_BAD_INPUT;
+    }
+    if (hc.body.total > 0)
+        hc.bb = bounding_box(hc.body.x.data(), hc.body.y.data(), hc.body.total, hc.gx, hc.gy, hc.P.scaleCV);
+    return CUIBM_OK;
+}
+
+int cuibm_case_info(const char *folder, int argc, const char **argv, cuibm_info *info)
+{
+    if (!info) return CUIBM_ERR_BAD_INPUT;
+    HostCase hc;
+    int st = host_case(folder, argc, argv, hc);
+    if (st != CUIBM_OK) return st;
+    std::memset(info, 0, sizeof *info);
+    const int nx = hc.gx.n, ny = hc.gy.n;
+    info->nx = nx;
+    info->ny = ny;
+    info->numU = (nx - 1) * ny;
+    info->numV = nx * (ny - 1);
+    info->numUV = info->numU + info->numV;
+    info->numP = nx * ny;
+    info->solver_type = hc.P.solverType;
+    info->time_step = hc.P.startStep;
+    info->nt = hc.P.nt;
+    info->nsave = hc.P.nsave;
+    info->dt = hc.P.dt;
+    info->nu = hc.P.nu;
+    info->total_points = hc.body.total;
+    info->bb_start_i = hc.bb.i0;
+    info->bb_start_j = hc.bb.j0;
+    info->bb_ncx = hc.bb.ncx;
+    info->bb_ncy = hc.bb.ncy;
+    info->nnz_lhs1 = (nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + (ny - 1) * nx * 5 - 2 * (ny - 1) - 2 * nx;
+    info->nnz_lhs2 = 5 * nx * ny - 2 * ny - 2 * nx;
+    info->velocity_precond = hc.P.velocity.precond;
+    info->poisson_precond = hc.P.poisson.precond;
+    info->velocity_krylov = hc.P.krylovVelocity;
+    info->poisson_krylov = hc.P.krylovPoisson;
+    return CUIBM_OK;
+}
+
+int cuibm_case_array(const char *folder, int argc, const char **argv, int field, double *dst, size_t count)
+{
+    HostCase hc;
+    int st = host_case(folder, argc, argv, hc);
+    if (st != CUIBM_OK) return st;
+    const std::vector<double> *v = nullptr;
+    switch (field) {
+    case CUIBM_F_X: case CUIBM_F_XV: v = &hc.gx.centre; break;
+    case CUIBM_F_DX: v = &hc.gx.width; break;
+    case CUIBM_F_XU: v = &hc.gx.face; break;
+    case CUIBM_F_Y: case CUIBM_F_YU: v = &hc.gy.centre; break;
+    case CUIBM_F_DY: v = &hc.gy.width; break;
+    case CUIBM_F_YV: v = &hc.gy.face; break;
+    case CUIBM_F_BODY_X: v = &hc.body.x; break;
+    case CUIBM_F_BODY_Y: v = &hc.body.y; break;
+    default: g_create_error = "field not available from a case description"; return CUIBM_ERR_BAD_INPUT;
+    }
+    if (!dst || count != v->size()) {
+        g_create_error = "count must be " + std::to_string(v->size());
+        return CUIBM_ERR_BAD_INPUT;
+    }
+    std::memcpy(dst, v->data(), count * sizeof(double));
+    return CUIBM_OK;
+}
+
+const char *cuibm_case_error(void) { return g_create_error.c_str(); }
 
 void cuibm_destroy(cuibm_ctx *h)
 {

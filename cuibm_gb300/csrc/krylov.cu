@@ -148,6 +148,7 @@ __global__ void __launch_bounds__(256) k_bicg_init(Op A, int n, const double *__
         ks->tol = ks->rtol * ks->bnorm;
         ks->it = 0;
         ks->s_done = 0;
+        ks->body_runs = 0;
         ks->status = KS_RUNNING;
         finish_status(ks, err, which);
         set_cond(h, use_cond, ks->status == KS_RUNNING);
@@ -180,6 +181,7 @@ __global__ void __launch_bounds__(256) k_bicg_1(Op A, int n, const double *p, co
     if (reduce_arrive<1>(v, partials, &ks->arrive, t) && threadIdx.x == 0) {
         ks->alpha = ks->rho / t[0];
         ks->s_done = 0;
+        ks->body_runs += 1;
     }
 }
 
@@ -304,6 +306,7 @@ __global__ void __launch_bounds__(256) k_cg_init(Op A, int n, const double *__re
         ks->rho = t[2];
         ks->tol = ks->rtol * ks->bnorm;
         ks->it = 0;
+        ks->body_runs = 0;
         ks->status = KS_RUNNING;
         finish_status(ks, err, which);
         set_cond(h, use_cond, ks->status == KS_RUNNING);
@@ -323,7 +326,10 @@ __global__ void __launch_bounds__(256) k_cg_1(Op A, int n, const double *p, doub
         v[0] = p[i] * qi;
     }
     double t[1];
-    if (reduce_arrive<1>(v, partials, &ks->arrive, t) && threadIdx.x == 0) ks->alpha = ks->rho / t[0];
+    if (reduce_arrive<1>(v, partials, &ks->arrive, t) && threadIdx.x == 0) {
+        ks->alpha = ks->rho / t[0];
+        ks->body_runs += 1;
+    }
 }
 
 // x += alpha p; r -= alpha q; (PC<2) z = M r and r.z; residual norm of the original system
@@ -591,6 +597,7 @@ void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool 
         c.stream = main;
         cudaGraph_t got;
         CUIBM_TRY(cudaStreamEndCapture(side, &got));
+        S.body_kernels = count_kernel_nodes(got);
         CUIBM_TRY(cudaStreamUpdateCaptureDependencies(c.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
     } else {
         SolveLauncher L{c, S, b, x, err, 0, 0};
@@ -606,6 +613,29 @@ void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool 
             if (host.status != KS_RUNNING) break;
         }
     }
+}
+
+int count_kernel_nodes(cudaGraph_t g)
+{
+    size_t n = 0;
+    CUIBM_TRY(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) CUIBM_TRY(cudaGraphGetNodes(g, nodes.data(), &n));
+    int k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        CUIBM_TRY(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+int read_body_runs(Context &c, LinearSystem &S)
+{
+    KrylovScalars host{};
+    CUIBM_TRY(cudaMemcpyAsync(&host, S.ks, sizeof(host), cudaMemcpyDeviceToHost, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    return host.body_runs;
 }
 
 int read_solve_status(Context &c, LinearSystem &S, int *iterations)

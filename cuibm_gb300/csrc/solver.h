@@ -73,6 +73,7 @@ struct KrylovScalars {
     double bnorm, tol, rnorm, snorm;
     double rtol, pad0;
     int it, maxit, status, s_done;
+    int body_runs, pad1;  // executions of the iteration body in the last solve
     unsigned int arrive;  // last-block-done counter of the fused reductions
     int pad;
 };
@@ -94,6 +95,7 @@ struct LinearSystem {
     KrylovScalars *ks = nullptr; // device
     std::vector<SaLevel *> amg;  // SA hierarchy (Poisson)
     int last_iterations = 0;
+    int body_kernels = 0;  // kernel nodes in one captured iteration body
 };
 
 struct Timer {
@@ -165,6 +167,7 @@ struct Context {
     bool use_graph = true;
     cudaGraphExec_t step_exec = nullptr;
     cudaGraph_t step_graph = nullptr;
+    int static_kernels = 0;  // kernel nodes of the step graph outside the solver loops
 
     // output files
     FILE *iterationsFile = nullptr, *forceFile = nullptr, *midPositionFile = nullptr;
@@ -198,11 +201,14 @@ void launch_copy(Context &c, double *dst, const double *src, int n);
 void setup_system(Context &c, LinearSystem &S);
 void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool in_graph);
 int read_solve_status(Context &c, LinearSystem &S, int *iterations);
+int read_body_runs(Context &c, LinearSystem &S);
+int count_kernel_nodes(cudaGraph_t g);
 
 // amg.cu
 void build_sa_hierarchy(Context &c, LinearSystem &S);
 void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z);
 void free_sa_hierarchy(LinearSystem &S);
+double sa_vcycle_bytes(const LinearSystem &S);
 
 // ib_kernels.cu
 void setup_ib(Context &c);

@@ -166,6 +166,26 @@ int cuibm_get_stream(cuibm_ctx *ctx, void **stream);
 int cuibm_get_timer(cuibm_ctx *ctx, const char *name, double *ms, int *count);
 int cuibm_set_option(cuibm_ctx *ctx, const char *key, double value);
 
+/* Time one kernel of the step on the context's stream with CUDA events: reps
+ * back-to-back launches on the current state; *avg_ms is the mean launch time
+ * and *bytes the kernel's algorithmic DRAM bytes per launch (unique inputs read
+ * plus outputs written).  Names: "rhs1", "rhs2", "project", "apply_lhs1",
+ * "apply_lhs2", "poisson_vcycle". */
+int cuibm_profile_kernel(cuibm_ctx *ctx, const char *kernel, int reps, double *avg_ms, double *bytes);
+
+/* Kernels of this library launched by the last time step: the kernel nodes of
+ * the step graph plus those of each solver's iteration body times the number
+ * of iterations it ran. */
+int cuibm_launch_count(cuibm_ctx *ctx, long long *per_step);
+
+/* Host-only (no GPU needed): parse a case folder and build its grid and body
+ * exactly as cuibm_create does.  cuibm_case_array copies CUIBM_F_X..CUIBM_F_YV
+ * or CUIBM_F_BODY_X/Y into dst (count doubles).  Replaces the reference's
+ * io::readInputs + io::parseDomainFile/parseBodiesFile (src/io/io.cu:108-138). */
+int cuibm_case_info(const char *case_folder, int argc, const char **argv, cuibm_info *info);
+int cuibm_case_array(const char *case_folder, int argc, const char **argv, int field, double *dst, size_t count);
+const char *cuibm_case_error(void);
+
 #ifdef __cplusplus
 }
 #endif

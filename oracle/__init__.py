@@ -313,3 +313,151 @@ def circle_points(cx, cy, R, n):
     X, Y = np.zeros(n), np.zeros(n)
     _sig("or_circle_points", D, D, D, INT, _dp, _dp)(cx, cy, R, n, _d(X), _d(Y))
     return X, Y
+
+
+# ---------------------------------------------------------------------------
+# immersed boundary (external method)
+# ---------------------------------------------------------------------------
+class _Tags(ctypes.Structure):
+    _fields_ = [(n, _ip) for n in ("ghostTagsUV", "ghostTagsP", "hybridTagsUV", "hybridTagsP", "hybridTagsUV2")] + \
+               [(n, _dp) for n in ("dist_node", "dist_between", "dist_u_body", "dist_v_body", "uv",
+                                   "bi_x", "bi_y", "ip_x", "ip_y", "bip_x", "bip_y", "ipp_x", "ipp_y")]
+
+
+class _Interp(ctypes.Structure):
+    _fields_ = [(n, _ip) for n in ("index1", "index2", "index3", "index4")] + \
+               [(n, _dp) for n in ("q1coef", "q2coef", "q3coef", "q4coef", "value", "dpdn")]
+
+
+class Tags:
+    """Tag arrays and body intercepts of luo_base (tagPoints)."""
+
+    def __init__(self, g):
+        self.ghostTagsUV = -np.ones(g.nUV, np.int32)
+        self.hybridTagsUV = -np.ones(g.nUV, np.int32)
+        self.hybridTagsUV2 = -np.ones(g.nUV, np.int32)
+        self.ghostTagsP = -np.ones(g.nP, np.int32)
+        self.hybridTagsP = -np.ones(g.nP, np.int32)
+        for k in ("dist_node", "dist_between", "uv", "bi_x", "bi_y", "ip_x", "ip_y"):
+            setattr(self, k, np.zeros(g.nUV))
+        for k in ("dist_u_body", "dist_v_body", "bip_x", "bip_y", "ipp_x", "ipp_y"):
+            setattr(self, k, np.zeros(g.nP))
+
+    def c(self):
+        return _Tags(**{f: (_i(getattr(self, f)) if "Tags" in f else _d(getattr(self, f))) for f, _ in _Tags._fields_})
+
+
+class Stencils:
+    """Per-node interpolation stencil (4 indices, 4 weights) and interpolated value."""
+
+    def __init__(self, n):
+        self.index = np.zeros((4, n), np.int32)
+        self.coef = np.zeros((4, n))
+        self.value = np.zeros(n)
+        self.dpdn = np.zeros(n)
+
+    def c(self):
+        return _Interp(index1=_i(self.index[0]), index2=_i(self.index[1]), index3=_i(self.index[2]),
+                       index4=_i(self.index[3]), q1coef=_d(self.coef[0]), q2coef=_d(self.coef[1]),
+                       q3coef=_d(self.coef[2]), q4coef=_d(self.coef[3]), value=_d(self.value), dpdn=_d(self.dpdn))
+
+
+def tag_points(g, bx, by, uB, vB, bb, midX, midY):
+    T = Tags(g)
+    ct = T.c()
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    _sig("or_tagPoints", ctypes.POINTER(_Tags), _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
+         INT, D, D)(ctypes.byref(ct), _d(f64(bx)), _d(f64(by)), _d(f64(uB)), _d(f64(vB)), _d(g.xu), _d(g.yu), _d(g.xv),
+                    _d(g.yv), i0, j0, ncx, ncy, g.nx, g.ny, len(bx), midX, midY)
+    return T
+
+
+def ghost_velocity(direc, u, T, uB0, g, bb, set_=True):
+    u = f64(u).copy()
+    S = Stencils(g.nUV)
+    cs = S.c()
+    xc, yc = (g.xu, g.yu) if direc == 0 else (g.xv, g.yv)
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    _sig("or_ghost_velocity", INT, _dp, INT, _ip, D, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
+         ctypes.POINTER(_Interp))(direc, _d(u), int(set_), _i(T.ghostTagsUV), uB0, _d(yc), _d(xc), _d(T.bi_x),
+                                  _d(T.bi_y), _d(T.ip_x), _d(T.ip_y), i0, j0, ncx, ncy, g.nx, g.ny, ctypes.byref(cs))
+    return u, S
+
+
+def hybrid_velocity(direc, u, ustar, T, uB0, g, bb):
+    ustar = f64(ustar).copy()
+    S = Stencils(g.nUV)
+    cs = S.c()
+    xc, yc = (g.xu, g.yu) if direc == 0 else (g.xv, g.yv)
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    _sig("or_hybrid_velocity", INT, _dp, _dp, _ip, D, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
+         ctypes.POINTER(_Interp))(direc, _d(f64(u)), _d(ustar), _i(T.hybridTagsUV), uB0, _d(yc), _d(xc),
+                                  _d(T.bi_x), _d(T.bi_y), _d(T.ip_x), _d(T.ip_y), i0, j0, ncx, ncy, g.nx, g.ny,
+                                  ctypes.byref(cs))
+    return ustar, S
+
+
+def hybrid_pressure(p, T, dudt, dvdt, g, bb):
+    pstar = np.zeros(g.nP)
+    S = Stencils(g.nP)
+    cs = S.c()
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    _sig("or_hybrid_pressure", _dp, _dp, _ip, D, D, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
+         ctypes.POINTER(_Interp))(_d(f64(p)), _d(pstar), _i(T.hybridTagsP), dudt, dvdt, _d(g.yu), _d(g.xv),
+                                  _d(T.bip_x), _d(T.bip_y), _d(T.ipp_x), _d(T.ipp_y), i0, j0, ncx, ncy, g.nx, g.ny,
+                                  ctypes.byref(cs))
+    return pstar, S
+
+
+def ghost_pressure(p, T, dudt, dvdt, g, bb, set_=True):
+    p = f64(p).copy()
+    S = Stencils(g.nP)
+    cs = S.c()
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    _sig("or_ghost_pressure", _dp, INT, _ip, D, D, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
+         ctypes.POINTER(_Interp))(_d(p), int(set_), _i(T.ghostTagsP), dudt, dvdt, _d(g.yu), _d(g.xv), _d(T.bip_x),
+                                  _d(T.bip_y), _d(T.ipp_x), _d(T.ipp_y), i0, j0, ncx, ncy, g.nx, g.ny,
+                                  ctypes.byref(cs))
+    return p, S
+
+
+def weight(direc, f, fstar, T, g, bb):
+    f = f64(f).copy()
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    if direc == 2:
+        gt, ht, xc, yc, bix, biy = T.ghostTagsP, T.hybridTagsP, g.xv, g.yu, T.bip_x, T.bip_y
+    else:
+        gt, ht, bix, biy = T.ghostTagsUV, T.hybridTagsUV, T.bi_x, T.bi_y
+        xc, yc = (g.xu, g.yu) if direc == 0 else (g.xv, g.yv)
+    _sig("or_weight", INT, _dp, _dp, _ip, _ip, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT)(
+        direc, _d(f), _d(f64(fstar)), _i(gt), _i(ht), _d(yc), _d(xc), _d(bix), _d(biy), i0, j0, ncx, ncy, g.nx, g.ny)
+    return f
+
+
+def set_inside(u, T, uB0, vB0, g):
+    u = f64(u).copy()
+    _sig("or_setInsideVelocity", _ip, _dp, D, D, INT, INT)(_i(T.ghostTagsUV), _d(u), uB0, vB0, g.nx, g.ny)
+    return u
+
+
+def robin(u, xp, g, dt, Uinf=1.0, Vinf=1.0):
+    xp = f64(xp).copy()
+    _sig("or_updateRobinBoundary", _dp, _dp, _dp, D, D, D, INT, INT)(_d(f64(u)), _d(xp), _d(g.dx), dt, Uinf, Vinf,
+                                                                      g.nx, g.ny)
+    return xp
+
+
+def force(u, uold, p, T, nu, g, dt, bb):
+    fx, fy = ctypes.c_double(), ctypes.c_double()
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    _sig("or_calculateForce", _dp, _dp, _dp, _ip, D, _dp, _dp, D, INT, INT, INT, INT, INT, INT, _dp, _dp)(
+        _d(f64(u)), _d(f64(uold)), _d(f64(p)), _i(T.ghostTagsUV), nu, _d(g.dx), _d(g.dy), dt, g.nx, g.ny, i0, j0, ncx,
+        ncy, ctypes.byref(fx), ctypes.byref(fy))
+    return fx.value, fy.value
+
+
+def bounding_box(x, y, g, scale):
+    a = [ctypes.c_int() for _ in range(4)]
+    _sig("or_bounding_box", INT, _dp, _dp, _dp, _dp, D, _ip, _ip, _ip, _ip)(
+        len(x), _d(f64(x)), _d(f64(y)), _d(g.x), _d(g.y), scale, *(ctypes.byref(v) for v in a))
+    return tuple(v.value for v in a)

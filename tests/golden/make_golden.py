@@ -148,6 +148,188 @@ def ns_case(K, IO, name, folder, rng, nu, dt):
     print("wrote", name, "nx=%d ny=%d" % (nx, ny))
 
 
+class RefTagArrays(ctypes.Structure):
+    _fields_ = [(n, _ip) for n in ("ghostTagsUV", "ghostTagsP", "hybridTagsUV", "hybridTagsP", "hybridTagsUV2")] + \
+               [(n, _dp) for n in ("distance_from_intersection_to_node", "distance_between_nodes_at_IB",
+                                   "distance_from_u_to_body", "distance_from_v_to_body", "uv",
+                                   "body_intercept_x", "body_intercept_y", "image_point_x", "image_point_y",
+                                   "body_intercept_p_x", "body_intercept_p_y", "image_point_p_x", "image_point_p_y",
+                                   "x1", "y1", "x2", "y2", "x1_p", "y1_p", "x2_p", "y2_p",
+                                   "x1_ip", "y1_ip", "x2_ip", "y2_ip")]
+
+
+class RefInterpArrays(ctypes.Structure):
+    _fields_ = [(n, _ip) for n in ("index1", "index2", "index3", "index4")] + \
+               [(n, _dp) for n in ("q1coef", "q2coef", "q3coef", "q4coef", "x1", "x2", "x3", "x4", "y1", "y2",
+                                   "y3", "y4", "q1", "q2", "q3", "q4", "image_point_u", "a0", "a1", "a2", "a3")]
+
+
+def bounding_box(x, y, gx, gy, scale):
+    """src/bodies.cu:256-326 (scaled box in cell indices), as in the oracle."""
+    xmax, xmin, ymax, ymin = x.max(), x.min(), y.max(), y.min()
+    ex, ey = xmax - xmin, ymax - ymin
+    xmax += 0.5 * ex * (scale - 1.0)
+    xmin -= 0.5 * ex * (scale - 1.0)
+    ymax += 0.5 * ey * (scale - 1.0)
+    ymin -= 0.5 * ey * (scale - 1.0)
+    i = j = 0
+    while gx[i + 1] < xmin:
+        i += 1
+    while gy[j + 1] < ymin:
+        j += 1
+    i0, j0 = i, j
+    while gx[i] < xmax:
+        i += 1
+    while gy[j] < ymax:
+        j += 1
+    return i0, j0, i - i0, j - j0
+
+
+def ib_case(K, IO, name, folder, rng, nu, dt, uB0=0.25, vB0=-0.15, uBk=0.2, vBk=-0.1, scale=2.0):
+    """Tagging, interpolation, blending, inside velocity, Robin outflow and force
+    of the external method on a small stretched grid around a circle."""
+    nx, ny, G = ref_grid(IO, folder)
+    nU, nV = (nx - 1) * ny, nx * (ny - 1)
+    nUV, nP = nU + nV, nx * ny
+    X, Y, _ = ref_body(IO, folder)
+    n = len(X)
+    # bodies::initialise (no rotation: x = X), centroid by a serial sum, then the t = 0
+    # motion of luo_base::initialise with zero coefficients: x = 0 + (x - midX)
+    mx = 0.0
+    my = 0.0
+    for v in X:
+        mx += v
+    for v in Y:
+        my += v
+    mx /= n
+    my /= n
+    i0, j0, ncx, ncy = bounding_box(X, Y, G["x"], G["y"], scale)
+    bx = np.array([0.0 + (v - mx) for v in X])
+    by = Y.copy()
+    midX, midY = 0.0, my
+    uB = np.full(n, uB0)
+    vB = np.full(n, vB0)
+    out = {"nx": np.int32(nx), "ny": np.int32(ny), "nu": np.float64(nu), "dt": np.float64(dt),
+           "bb": np.array([i0, j0, ncx, ncy], np.int32), "bx": bx, "by": by, "uB": uB, "vB": vB,
+           "midX": np.float64(midX), "midY": np.float64(midY), "uBk": np.float64(uBk), "vBk": np.float64(vBk),
+           "body_X": X, "body_Y": Y}
+    out.update({"grid_" + k: v for k, v in G.items()})
+    p_sized = {"ghostTagsP", "hybridTagsP", "distance_from_u_to_body", "distance_from_v_to_body",
+               "body_intercept_p_x", "body_intercept_p_y", "image_point_p_x", "image_point_p_y",
+               "x1_p", "y1_p", "x2_p", "y2_p"}
+    arr = {}
+    for f, _ in RefTagArrays._fields_:
+        size = nP if f in p_sized else nUV
+        arr[f] = np.zeros(size + 2 * max(nx, ny), np.int32 if "Tags" in f else np.float64)[:size].copy()
+    ta = RefTagArrays(**{f: (i(arr[f]) if "Tags" in f else d(arr[f])) for f, _ in RefTagArrays._fields_})
+    K.ref_tagPoints.argtypes = [ctypes.POINTER(RefTagArrays)] + [_dp] * 8 + [ctypes.c_int] * 7 + \
+        [ctypes.c_double, ctypes.c_double]
+    K.ref_tagPoints(ctypes.byref(ta), d(bx), d(by), d(uB), d(vB), d(G["xu"]), d(G["yu"]), d(G["xv"]), d(G["yv"]),
+                    i0, j0, ncx, ncy, nx, ny, n, midX, midY)
+    for f in ("ghostTagsUV", "ghostTagsP", "hybridTagsUV", "hybridTagsP", "hybridTagsUV2",
+              "distance_from_intersection_to_node", "distance_between_nodes_at_IB", "uv",
+              "body_intercept_x", "body_intercept_y", "image_point_x", "image_point_y",
+              "body_intercept_p_x", "body_intercept_p_y", "image_point_p_x", "image_point_p_y",
+              "distance_from_u_to_body", "distance_from_v_to_body"):
+        out["tag_" + f] = arr[f].copy()
+
+    def interp_arrays(size):
+        a = {f: np.zeros(size, np.int32 if f.startswith("index") else np.float64) for f, _ in RefInterpArrays._fields_}
+        r = RefInterpArrays(**{f: (i(a[f]) if f.startswith("index") else d(a[f])) for f, _ in RefInterpArrays._fields_})
+        return a, r
+
+    gU, gP = arr["ghostTagsUV"], arr["ghostTagsP"]
+    hU, hP = arr["hybridTagsUV"], arr["hybridTagsP"]
+    bix, biy, ipx, ipy = (arr[k] for k in ("body_intercept_x", "body_intercept_y", "image_point_x", "image_point_y"))
+    bpx, bpy, ppx, ppy = (arr[k] for k in ("body_intercept_p_x", "body_intercept_p_y", "image_point_p_x",
+                                           "image_point_p_y"))
+    u = 1.0 + 0.2 * rng.standard_normal(nUV)
+    p = 0.1 * rng.standard_normal(nP)
+    out.update(u_in=u.copy(), p_in=p.copy())
+    # ghost-node velocity, u then v, set = true (luoIBM::rhs1GNInterpolation)
+    K.ref_interpolateVelocityToGhostNode.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip] + [_dp] * 9 + \
+        [ctypes.c_int] * 6 + [ctypes.POINTER(RefInterpArrays)]
+    ug = u.copy()
+    for direc, (xc, yc, vel) in enumerate(((G["xu"], G["yu"], uB), (G["xv"], G["yv"], vB))):
+        a, r = interp_arrays(nUV)
+        K.ref_interpolateVelocityToGhostNode(direc, d(ug), 1, i(gU), d(bx), d(by), d(vel), d(yc), d(xc), d(bix),
+                                             d(biy), d(ipx), d(ipy), i0, j0, ncx, ncy, nx, ny, ctypes.byref(r))
+        for f in ("index1", "index2", "index3", "index4", "q1coef", "q2coef", "q3coef", "q4coef", "image_point_u"):
+            out["ghost%d_%s" % (direc, f)] = a[f]
+    out["u_ghost"] = ug
+    # hybrid-node velocity from the ghost-filled field (luoIBM::rhs1HNInterpolation)
+    K.ref_interpolateVelocityToHybridNode.argtypes = [ctypes.c_int, _dp, _dp, _ip] + [_dp] * 9 + \
+        [ctypes.c_int] * 6 + [ctypes.POINTER(RefInterpArrays)]
+    ustar = np.zeros(nUV)
+    for direc, (xc, yc, vel) in enumerate(((G["xu"], G["yu"], uB), (G["xv"], G["yv"], vB))):
+        a, r = interp_arrays(nUV)
+        K.ref_interpolateVelocityToHybridNode(direc, d(ug), d(ustar), i(hU), d(bx), d(by), d(vel), d(yc), d(xc),
+                                              d(bix), d(biy), d(ipx), d(ipy), i0, j0, ncx, ncy, nx, ny,
+                                              ctypes.byref(r))
+        for f in ("index1", "index2", "index3", "index4", "q1coef", "q2coef", "q3coef", "q4coef", "image_point_u"):
+            out["hybrid%d_%s" % (direc, f)] = a[f]
+    out["ustar"] = ustar
+    # pressure: hybrid (pstar), weightP, ghost (set = true) - luoIBM::weightPressure
+    uBk_a, vBk_a = np.full(n, uBk), np.full(n, vBk)
+    K.ref_interpolatePressureToHybridNode.argtypes = [_dp, _dp, _dp, _ip] + [_dp] * 14 + [ctypes.c_int] * 6 + \
+        [ctypes.c_double, ctypes.POINTER(RefInterpArrays)]
+    pstar = np.zeros(nP)
+    a, r = interp_arrays(nP)
+    K.ref_interpolatePressureToHybridNode(d(p), d(pstar), d(ug), i(hP), d(bx), d(by), d(uB), d(uBk_a), d(vB),
+                                          d(vBk_a), d(G["yu"]), d(G["yv"]), d(G["xu"]), d(G["xv"]), d(bpx), d(bpy),
+                                          d(ppx), d(ppy), i0, j0, ncx, ncy, nx, ny, dt, ctypes.byref(r))
+    for f in ("index1", "index2", "index3", "index4", "q1coef", "q2coef", "q3coef", "q4coef"):
+        out["phybrid_" + f] = a[f]
+    out["pstar"] = pstar
+    K.ref_weight.argtypes = [ctypes.c_int, _dp, _dp, _ip, _ip] + [_dp] * 6 + [ctypes.c_int] * 6
+    pw = p.copy()
+    K.ref_weight(2, d(pw), d(pstar), i(gP), i(hP), d(G["yu"]), d(G["xv"]), d(bpx), d(bpy), d(ppx), d(ppy), i0, j0,
+                 ncx, ncy, nx, ny)
+    out["p_weighted"] = pw.copy()
+    K.ref_interpolatePressureToGhostNode.argtypes = [_dp, ctypes.c_int, _dp, _ip, _dp, _dp, _dp] + [_dp] * 12 + \
+        [_dp] + [ctypes.c_int] * 6 + [ctypes.c_double, ctypes.POINTER(RefInterpArrays)]
+    dpdn, bip = np.zeros(nP), np.zeros(nP)
+    a, r = interp_arrays(nP)
+    K.ref_interpolatePressureToGhostNode(d(pw), 1, d(ug), i(gP), d(bx), d(by), d(dpdn), d(uB), d(uBk_a), d(vB),
+                                         d(vBk_a), d(G["yu"]), d(G["yv"]), d(G["xu"]), d(G["xv"]), d(bpx), d(bpy),
+                                         d(ppx), d(ppy), d(bip), i0, j0, ncx, ncy, nx, ny, dt, ctypes.byref(r))
+    for f in ("index1", "index2", "index3", "index4", "q1coef", "q2coef", "q3coef", "q4coef"):
+        out["pghost_" + f] = a[f]
+    out.update(p_ghost=pw, dpdn=dpdn, body_intercept_p=bip)
+    # velocity blending (weightUhat) on a random uhat
+    uhat = 1.0 + 0.2 * rng.standard_normal(nUV)
+    out["uhat_in"] = uhat.copy()
+    K.ref_weight(0, d(uhat), d(ustar), i(gU), i(hU), d(G["yu"]), d(G["xu"]), d(bix), d(biy), d(ipx), d(ipy), i0,
+                 j0, ncx, ncy, nx, ny)
+    K.ref_weight(1, d(uhat), d(ustar), i(gU), i(hU), d(G["yv"]), d(G["xv"]), d(bix), d(biy), d(ipx), d(ipy), i0,
+                 j0, ncx, ncy, nx, ny)
+    out["uhat_weighted"] = uhat
+    # inside velocity := body velocity (grid over numUV threads, luoIBM::zeroVelocity)
+    ui = ug.copy()
+    K.ref_setInsideVelocity.argtypes = [_ip, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    K.ref_setInsideVelocity(i(gU), d(ui), d(uB), d(vB), nx, ny, nUV)
+    out["u_inside"] = ui
+    # convective outflow update of the x+ boundary array
+    xp = 1.0 + 0.1 * rng.standard_normal(2 * ny - 1)
+    out["xp_in"] = xp.copy()
+    K.ref_updateRobinBoundary.argtypes = [_dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int]
+    K.ref_updateRobinBoundary(d(ug), d(xp), d(G["dx"]), dt, 1.0, 1.0, nx, ny)
+    out["xp_robin"] = xp
+    # control-volume force
+    uold = ug + 0.01 * rng.standard_normal(nUV)
+    out["uold_in"] = uold
+    fx, fy = ctypes.c_double(), ctypes.c_double()
+    K.ref_calculateForce.argtypes = [_dp, _dp, _dp, _ip, ctypes.c_double, _dp, _dp, ctypes.c_double] + \
+        [ctypes.c_int] * 6 + [_dp, _dp]
+    K.ref_calculateForce(d(ug), d(uold), d(p), i(gU), nu, d(G["dx"]), d(G["dy"]), dt, nx, ny, i0, j0, ncx, ncy,
+                         ctypes.byref(fx), ctypes.byref(fy))
+    out["force"] = np.array([fx.value, fy.value])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "nx=%d ny=%d bb=%s ghostUV=%d hybridUV=%d ghostP=%d hybridP=%d" % (
+        nx, ny, (i0, j0, ncx, ncy), (gU > 0).sum(), (hU > 0).sum(), (gP > 0).sum(), (hP > 0).sum()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
@@ -167,6 +349,14 @@ def main():
         f = os.path.join(tmp, "cavity")
         cases.cavity(f, n=16, nu=0.01, dt=0.01, nt=1)
         ns_case(K, IO, "ns_cavity16", f, rng, nu=0.01, dt=0.01)
+        # external-method kernels around a circle (two resolutions / point counts)
+        f = os.path.join(tmp, "ib1")
+        cases.cylinder(f, h=0.05, ratio=1.1, extent=2.0, core=0.6, points=48, nu=0.02, dt=0.01, nt=1)
+        ib_case(K, IO, "ib_circle48", f, rng, nu=0.02, dt=0.01)
+        f = os.path.join(tmp, "ib2")
+        cases.cylinder(f, h=0.025, ratio=1.08, extent=2.5, core=0.7, points=101, nu=0.02, dt=0.005, nt=1,
+                       radius=0.43)
+        ib_case(K, IO, "ib_circle101", f, rng, nu=0.02, dt=0.005, uB0=0.0, vB0=0.0, uBk=0.0, vBk=0.0)
         # grids and bodies of the benchmark cylinders (Re 40 and Re 550)
         f = os.path.join(tmp, "cyl40")
         cases.cylinder(f, h=0.02, ratio=1.03, points=157, nt=1)
