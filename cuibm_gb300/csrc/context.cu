@@ -180,7 +180,8 @@ static void phase_update_body(Context &c)
         PhaseTimer t(c, "Move Body");
         launch_body_motion(c, -1.0);  // time taken from the device step counter
     }
-    {
+    if (body_moves(c)) {
+        // a static body keeps its tags: re-tagging it reproduces them exactly
         PhaseTimer t(c, "Update Solver");
         launch_tag_points(c);
     }
@@ -208,8 +209,8 @@ static void record_step(Context &c, bool in_graph)
         launch_ghost_pressure(c, true);
     }
     phase_project(c);
-    launch_step_counter(c);  // timeStep++ on the device (read by motion)
-    phase_update_body(c);
+    phase_update_body(c);    // motion reads the step counter before it advances
+    launch_step_counter(c);  // _post_step: timeStep++
     {
         PhaseTimer t(c, "CFL");
         launch_cfl(c);
@@ -297,6 +298,8 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         c.has_body = c.body.total > 0 && c.P.solverType != ST_NAVIERSTOKES;
         if (c.P.solverType != ST_NAVIERSTOKES && c.P.solverType != ST_LUO)
             throw InputError("SolverType FADLUN / OSC_CYLINDER is not implemented by this build yet");
+        if (c.P.solverType == ST_LUO && c.body.total > 0 && (c.body.xCoeff != 0 || c.body.uCoeff != 0))
+            throw InputError("a moving body with the external method is not implemented by this build yet");
         if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
             throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
         if (c.has_body) {

@@ -1,23 +1,1287 @@
-// Immersed-boundary kernels (placeholder until the external method is built).
+// Immersed-boundary kernels of the external (Luo) ghost-node method.
+//
+// Replaces luo_base/kernels/tagPoints.cu (tag_u_luo, tag_v_luo, tag_p_luo, zero_*_luo),
+// luo_base/kernels/biLinearInterpolation.cu (ghost and hybrid interpolation of velocity
+// and pressure), luoIBM/kernels/weight.cu, luo_base/kernels/intermediateVelocity.cu
+// (setInsideVelocity), FadlunModified/kernels/intermediateVelocity.cu (updateBoundaryX/Y),
+// FadlunModified/kernels/calculateForce.cu (control-volume force) and
+// luo_base/kernels/structure.cu (prescribed motion).
+//
+// This translation unit is compiled with -fmad=false: every tag decision uses the
+// reference's arithmetic exactly, so tag arrays are bit-identical to the
+// reference's.  Intercepts use CUDA's acos/sin/tan, which may differ from the
+// host C library in the last bit; interpolation weights then agree to a few ulp.
+//
+// Determinism.  The reference's tagging threads write into neighbouring nodes
+// (ghost tags, body intercepts, image points), so the result depends on thread
+// order; its ghost interpolation overwrites the field it reads.  Here:
+//  * tagging runs in two passes: each node first records every write it would
+//    make (its last write per target and field, in its own segment order), then
+//    each target node resolves the records of its five possible writers in
+//    global thread order (south, west, self, east, north) - the outcome of the
+//    reference's grid run one thread after another;
+//  * ghost interpolation stages the new values and applies them in a second
+//    launch, so every node reads the field as it was before (what the
+//    reference's GPU launch does: all loads precede all stores).
+#include <cmath>
+#include <vector>
+
 #include "solver.h"
 
 namespace cuibm {
-static void nyi() { throw InputError("immersed-boundary kernels are not built yet"); }
-void setup_ib(Context &) { nyi(); }
-void launch_tag_points(Context &) { nyi(); }
-void launch_ghost_velocity(Context &, double *, bool) { nyi(); }
-void launch_hybrid_velocity(Context &, const double *) { nyi(); }
-void launch_set_inside(Context &, double *) { nyi(); }
-void launch_weight_uhat(Context &) { nyi(); }
-void launch_hybrid_pressure(Context &) { nyi(); }
-void launch_ghost_pressure(Context &, bool) { nyi(); }
-void launch_weight_pressure(Context &) { nyi(); }
-void launch_robin(Context &) { nyi(); }
-void launch_force(Context &) { nyi(); }
-void launch_body_motion(Context &, double) { nyi(); }
-void launch_body_pre_step(Context &) { nyi(); }
-void initialise_body(Context &) { nyi(); }
+
+#define IB_EPS 1.e-10
+
+// ---- tagging records ------------------------------------------------------------
+// slots: 0 self, 1 west (n-1), 2 east (n+1), 3 south (n-sv), 4 north (n+sv)
+struct TagRecords {
+    int *flags;      // bits 0-4 ghost written per slot, 8-12 intercept written per slot,
+                     // 16 final self block ran, 17 dist slot A written, 18 dist slot B written, 19 hybrid-P self
+    int *hyb, *hyb2;
+    double *dnode, *dbetween, *uv;
+    double *bi;      // [idx][5 slots][4]: bix, biy, ipx, ipy
+    double *distA, *distB;
+    int nrec;
+};
+
+struct TagGeom {
+    const double *bx, *by, *vel;
+    const double *xc, *yc;
+    int i0, j0, width, height, nthreads;
+    int nx, ny, total;
+    double midX, midY;
+};
+
+__device__ __forceinline__ void intercept_dev(const double *bx, const double *by, int k, int l, double px,
+                                              double py, double *ix, double *iy)
+{
+    double dxs = bx[l] - bx[k], dys = by[l] - by[k];
+    double dxo = bx[l] - px, dyo = by[l] - py;
+    double dxb = px - bx[k], dyb = py - by[k];
+    double p = sqrt(dxs * dxs + dys * dys);
+    double o = sqrt(dxo * dxo + dyo * dyo);
+    double b = sqrt(dxb * dxb + dyb * dyb);
+    double th = acos((p * p + b * b - o * o) / (2 * p * b));
+    double a = sin(th) * b;
+    *iy = by[k] + (by[l] - by[k]) / p * a / tan(th);
+    *ix = bx[k] + (bx[l] - bx[k]) / p * a / tan(th);
+}
+
+struct RecWriter {
+    int flags = 0;
+    double bi[5][4];
+    __device__ void ghost(int slot) { flags |= 1 << slot; }
+    __device__ void point(int slot, double bix, double biy, double ipx, double ipy)
+    {
+        flags |= 1 << (8 + slot);
+        bi[slot][0] = bix;
+        bi[slot][1] = biy;
+        bi[slot][2] = ipx;
+        bi[slot][3] = ipy;
+    }
+};
+
+// one velocity node (KIND 0 = u: tag_u_luo, 1 = v: tag_v_luo)
+template <int KIND>
+__global__ void k_tag_velocity_records(TagGeom G, TagRecords R)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G.nthreads) return;
+    const int nx = G.nx, ny = G.ny, nU = (nx - 1) * ny;
+    const int I = G.i0 + idx % G.width, J = G.j0 + idx / G.width;
+    const int sv = KIND == 0 ? nx - 1 : nx;
+    const int n = KIND == 0 ? J * (nx - 1) + I : J * nx + I + nU;
+    RecWriter w;
+    int flags_extra = 0;
+    if (KIND == 0 ? (n >= nU) : (n >= nU + nx * (ny - 1))) {
+        R.flags[idx] = 0;
+        return;
+    }
+    const double *bx = G.bx, *by = G.by, *vel = G.vel, *xc = G.xc, *yc = G.yc;
+    const double midX = G.midX, midY = G.midY;
+    int k = G.total - 1, l = 0;
+    bool outsideX = true, outsideY = true, flag = false;
+    int fX = -1, fY = -1, f2X = -1, f2Y = -1;
+    double uvX = 0.0, uvY = 0.0, Xa = 1.0, Ya = 1.0, Xb = 1.0, Yb = 1.0, x = 0.0, y = 0.0;
+    double distA = 0, distB = 0;
+    if (KIND == 0) flags_extra |= 1 << 17;  // dist_u_body[ip] = 0 at thread start
+    double ix, iy;
+    while (l < G.total && (KIND == 1 || !flag)) {
+        int bottom, top, left, right;
+        if (by[k] > by[l]) { bottom = l; top = k; } else { bottom = k; top = l; }
+        if (bx[k] > bx[l]) { left = l; right = k; } else { left = k; right = l; }
+        if (by[bottom] - IB_EPS < yc[J] && by[top] - IB_EPS > yc[J] && (KIND == 0 || !flag)) {
+            if (fabs(by[l] - by[k]) > IB_EPS) {
+                x = bx[k] + (bx[l] - bx[k]) * (yc[J] - by[k]) / (by[l] - by[k]);
+                uvX = vel[k] + (vel[l] - vel[k]) * (yc[J] - by[k]) / (by[l] - by[k]);
+                if (x > xc[I] + IB_EPS) outsideX = !outsideX;
+                if (x > xc[I - 1] + IB_EPS && x < xc[I] - IB_EPS) {
+                    fX = n;
+                    f2X = n + 1;
+                    if (x > midX + IB_EPS) {
+                        w.ghost(1);
+                        intercept_dev(bx, by, k, l, xc[I - 1], yc[J], &ix, &iy);
+                        w.point(1, ix, iy, ix + (ix - xc[I - 1]), iy + (iy - yc[J]));
+                        intercept_dev(bx, by, k, l, xc[I], yc[J], &ix, &iy);
+                        w.point(0, ix, iy, 2 * xc[I] - ix, 2 * yc[J] - iy);
+                    }
+                    Xa = xc[I] - x;
+                    Xb = xc[I + 1] - xc[I];
+                    if (KIND == 0 && x > midX) distA = Xa;
+                } else if (x > xc[I] + IB_EPS && x < xc[I + 1] - IB_EPS) {
+                    fX = n;
+                    f2X = n - 1;
+                    if (x < midX - IB_EPS) {
+                        w.ghost(2);
+                        intercept_dev(bx, by, k, l, xc[I + 1], yc[J], &ix, &iy);
+                        w.point(2, ix, iy, ix + (ix - xc[I + 1]), iy + (iy - yc[J]));
+                        intercept_dev(bx, by, k, l, xc[I], yc[J], &ix, &iy);
+                        w.point(0, ix, iy, 2 * xc[I] - ix, 2 * yc[J] - iy);
+                    }
+                    Xa = x - xc[I];
+                    Xb = xc[I] - xc[I - 1];
+                    if (KIND == 0 && x < midX) {
+                        distB = Xa;
+                        flags_extra |= 1 << 18;
+                    }
+                } else if (fabs(x - xc[I]) < IB_EPS && fabs(midX - xc[I]) > fabs(midY - yc[J])) {
+                    outsideX = true;
+                    fX = n;
+                    if (x < midX) {
+                        w.ghost(2);
+                        f2X = n - 1;
+                        w.point(2, xc[I], yc[J], xc[I - 1], yc[J]);
+                        w.point(0, xc[I], yc[J], xc[I - 1], yc[J]);
+                        Xa = 0;
+                        Xb = xc[I] - xc[I - 1];
+                    }
+                    if (x > midX) {
+                        w.ghost(1);
+                        f2X = n + 1;
+                        w.point(1, xc[I], yc[J], xc[I + 1], yc[J]);
+                        w.point(0, xc[I], yc[J], xc[I + 1], yc[J]);
+                        Xa = 0;
+                        Xb = xc[I + 1] - xc[I];
+                    }
+                    flag = true;
+                }
+            }
+        }
+        if (bx[left] - IB_EPS < xc[I] && bx[right] - IB_EPS > xc[I] && (KIND == 0 || !flag)) {
+            if (fabs(bx[l] - bx[k]) > IB_EPS) {
+                y = by[k] + (by[l] - by[k]) * (xc[I] - bx[k]) / (bx[l] - bx[k]);
+                uvY = vel[k] + (vel[l] - vel[k]) * (xc[I] - bx[k]) / (bx[l] - bx[k]);
+                if (y > yc[J] + IB_EPS) outsideY = !outsideY;
+                if (y > yc[J - 1] + IB_EPS && y < yc[J] - IB_EPS) {
+                    fY = n;
+                    f2Y = n + sv;
+                    if (y > midY + IB_EPS) {
+                        w.ghost(3);
+                        intercept_dev(bx, by, k, l, xc[I], yc[J - 1], &ix, &iy);
+                        w.point(3, ix, iy, ix + (ix - xc[I]), iy + (iy - yc[J - 1]));
+                        intercept_dev(bx, by, k, l, xc[I], yc[J], &ix, &iy);
+                        w.point(0, ix, iy, 2 * xc[I] - ix, 2 * yc[J] - iy);
+                    }
+                    Ya = yc[J] - y;
+                    Yb = yc[J + 1] - yc[J];
+                    if (KIND == 1 && outsideY) {
+                        distA = Ya;
+                        flags_extra |= 1 << 17;
+                    }
+                } else if (y > yc[J] + IB_EPS && y < yc[J + 1] - IB_EPS) {
+                    fY = n;
+                    f2Y = n - sv;
+                    if (y < midY - IB_EPS) {
+                        w.ghost(4);
+                        intercept_dev(bx, by, k, l, xc[I], yc[J + 1], &ix, &iy);
+                        w.point(4, ix, iy, ix + (ix - xc[I]), iy + (iy - yc[J + 1]));
+                        intercept_dev(bx, by, k, l, xc[I], yc[J], &ix, &iy);
+                        w.point(0, ix, iy, 2 * xc[I] - ix, 2 * yc[J] - iy);
+                    }
+                    Ya = y - yc[J];
+                    Yb = yc[J] - yc[J - 1];
+                    if (KIND == 1 && outsideY) {
+                        distB = Ya;
+                        flags_extra |= 1 << 18;
+                    }
+                } else if (KIND == 0 ? (fabs(y - yc[J]) < IB_EPS && fabs(y - midY) > fabs(x - midX))
+                                     : (fabs(y - yc[J]) < IB_EPS && fabs(midY - yc[J]) > fabs(midX - xc[I]))) {
+                    outsideY = true;
+                    fY = n;
+                    if (y < midY) {
+                        w.ghost(4);
+                        f2X = n - sv;  // the reference sets the x-ray second flag here
+                        w.point(4, xc[I], yc[J], xc[I], yc[J - 1]);
+                        w.point(0, xc[I], yc[J], xc[I], yc[J - 1]);
+                        Ya = 0;
+                        Yb = yc[J] - yc[J - 1];
+                    }
+                    if (y > midY) {
+                        w.ghost(3);
+                        f2X = n + sv;
+                        w.point(3, xc[I], yc[J], xc[I], yc[J + 1]);
+                        w.point(0, xc[I], yc[J], xc[I], yc[J + 1]);
+                        Ya = 0;
+                        Yb = yc[J + 1] - yc[J];
+                    }
+                    flag = true;
+                }
+            }
+        }
+        k = l;
+        l = l + 1;
+    }
+    const bool useX = outsideX && fX >= 0, useY = outsideY && fY >= 0;
+    int hy = -1, hy2 = -1;
+    double dn = 0, db = 0, uvv = 0;
+    bool final_ = false;
+    if (KIND == 0 ? useX : (useX && !useY)) {
+        final_ = true;
+        hy = fX;
+        hy2 = f2X;
+        dn = Xa;
+        db = Xb;
+        uvv = uvX;
+    } else if (useY) {
+        final_ = true;
+        hy = fY;
+        hy2 = f2Y;
+        dn = Ya;
+        db = Yb;
+        uvv = uvY;
+    }
+    R.flags[idx] = w.flags | flags_extra | (final_ ? 1 << 16 : 0);
+    R.hyb[idx] = hy;
+    R.hyb2[idx] = hy2;
+    R.dnode[idx] = dn;
+    R.dbetween[idx] = db;
+    R.uv[idx] = uvv;
+    R.distA[idx] = distA;
+    R.distB[idx] = distB;
+    for (int s = 0; s < 5; ++s)
+        if (w.flags & (1 << (8 + s)))
+            for (int q = 0; q < 4; ++q) R.bi[(size_t)idx * 20 + s * 4 + q] = w.bi[s][q];
+}
+
+// one pressure node of tag_p_luo
+__global__ void k_tag_pressure_records(TagGeom G, TagRecords R)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G.nthreads) return;
+    const int nx = G.nx;
+    const int I = G.i0 + idx % G.width, J = G.j0 + idx / G.width, ip = J * nx + I;
+    RecWriter w;
+    int extra = 0;
+    if (ip >= nx * G.ny) {
+        R.flags[idx] = 0;
+        return;
+    }
+    const double *bx = G.bx, *by = G.by, *xv = G.xc, *yu = G.yc;
+    const double midX = G.midX, midY = G.midY;
+    int k = G.total - 1, l = 0;
+    bool flag = false;
+    double x, y, ix, iy;
+    while (l < G.total) {
+        int bottom, top, left, right;
+        if (by[k] > by[l]) { bottom = l; top = k; } else { bottom = k; top = l; }
+        if (bx[k] > bx[l]) { left = l; right = k; } else { left = k; right = l; }
+        if (by[bottom] - IB_EPS < yu[J] && by[top] - IB_EPS > yu[J] && !flag) {
+            if (fabs(by[l] - by[k]) > IB_EPS) {
+                x = bx[k] + (bx[l] - bx[k]) * (yu[J] - by[k]) / (by[l] - by[k]);
+                bool g1 = x > midX + IB_EPS && x > xv[I] + IB_EPS + IB_EPS && x < xv[I + 1] - IB_EPS;
+                bool g2 = x < midX + IB_EPS && x < xv[I] - IB_EPS && x > xv[I - 1] + IB_EPS;
+                if (g1 || g2) {
+                    w.ghost(0);
+                    intercept_dev(bx, by, k, l, xv[I], yu[J], &ix, &iy);
+                    w.point(0, ix, iy, ix + (ix - xv[I]), iy + (iy - yu[J]));
+                }
+                bool h1 = x > midX + IB_EPS && x < xv[I] - IB_EPS && x > xv[I - 1] + IB_EPS;
+                bool h2 = x < midX + IB_EPS && x > xv[I] + IB_EPS && x < xv[I + 1] - IB_EPS;
+                if (h1 || h2) {
+                    extra |= 1 << 19;
+                    intercept_dev(bx, by, k, l, xv[I], yu[J], &ix, &iy);
+                    w.point(0, ix, iy, 2 * xv[I] - ix, 2 * yu[J] - iy);
+                }
+                if (fabs(x - xv[I]) < IB_EPS && fabs(midX - xv[I]) > fabs(midY - yu[J])) {
+                    extra |= 1 << 19;
+                    if (x < midX) {
+                        w.ghost(2);
+                        w.point(2, xv[I], yu[J], xv[I - 1], yu[J]);
+                        w.point(0, xv[I], yu[J], xv[I - 1], yu[J]);
+                    } else if (x > midX) {
+                        w.ghost(1);
+                        w.point(1, xv[I], yu[J], xv[I + 1], yu[J]);
+                        w.point(0, xv[I], yu[J], xv[I + 1], yu[J]);
+                    }
+                    flag = true;
+                }
+            }
+        }
+        if (bx[left] - IB_EPS < xv[I] && bx[right] - IB_EPS > xv[I] && !flag) {
+            if (fabs(bx[l] - bx[k]) > IB_EPS) {
+                y = by[k] + (by[l] - by[k]) * (xv[I] - bx[k]) / (bx[l] - bx[k]);
+                bool g1 = y > midY + IB_EPS && y > yu[J] + IB_EPS && y < yu[J + 1] - IB_EPS;
+                bool g2 = y < midY + IB_EPS && y < yu[J] - IB_EPS && y > yu[J - 1] + IB_EPS;
+                if (g1 || g2) {
+                    w.ghost(0);
+                    intercept_dev(bx, by, k, l, xv[I], yu[J], &ix, &iy);
+                    w.point(0, ix, iy, ix + (ix - xv[I]), iy + (iy - yu[J]));
+                }
+                bool h1 = y > midY + IB_EPS && y < yu[J] - IB_EPS && y > yu[J - 1] + IB_EPS;
+                bool h2 = y < midY + IB_EPS && y > yu[J] + IB_EPS && y < yu[J + 1] - IB_EPS;
+                if (h1 || h2) {
+                    extra |= 1 << 19;
+                    intercept_dev(bx, by, k, l, xv[I], yu[J], &ix, &iy);
+                    w.point(0, ix, iy, 2 * xv[I] - ix, 2 * yu[J] - iy);
+                }
+                if (fabs(y - yu[J]) < IB_EPS && fabs(midY - yu[J]) > fabs(midX - xv[I])) {
+                    extra |= 1 << 19;
+                    if (y < midY) {
+                        w.ghost(4);
+                        w.point(4, xv[I], yu[J], xv[I], yu[J - 1]);
+                        w.point(0, xv[I], yu[J], xv[I], yu[J - 1]);
+                    }
+                    if (y > midY) {
+                        w.ghost(3);
+                        w.point(3, xv[I], yu[J], xv[I], yu[J + 1]);
+                        w.point(0, xv[I], yu[J], xv[I], yu[J + 1]);
+                    }
+                    flag = true;
+                }
+            }
+        }
+        k = l;
+        l = l + 1;
+    }
+    R.flags[idx] = w.flags | extra;
+    for (int s = 0; s < 5; ++s)
+        if (w.flags & (1 << (8 + s)))
+            for (int q = 0; q < 4; ++q) R.bi[(size_t)idx * 20 + s * 4 + q] = w.bi[s][q];
+}
+
+struct TagOut {
+    int *ghost, *hyb, *hyb2;
+    double *dnode, *dbetween, *uv, *bix, *biy, *ipx, *ipy, *dist;
+};
+
+// Resolve the writes of the five possible writers of every target node of the box
+// (extended by one node on each side) in the reference's serial thread order.
+// CLS: 0 u, 1 v, 2 p.
+template <int CLS>
+__global__ void k_tag_resolve(TagGeom G, TagRecords R, TagOut O)
+{
+    const int ew = G.width + 2, rows = (G.nthreads + G.width - 1) / G.width;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ew * (rows + 2)) return;
+    const int i = t % ew - 1, j = t / ew - 1;  // box coordinates of the target
+    const int nx = G.nx, ny = G.ny, nU = (nx - 1) * ny;
+    const int I = G.i0 + i, J = G.j0 + j;
+    if (I < 0 || J < 0 || I >= nx || J >= ny) return;
+    int n, limit;
+    if (CLS == 0) { n = J * (nx - 1) + I; limit = nU; if (I >= nx - 1) return; }
+    else if (CLS == 1) { n = J * nx + I + nU; limit = nU + nx * (ny - 1); if (J >= ny - 1) return; }
+    else { n = J * nx + I; limit = nx * ny; }
+    if (n >= limit) return;
+    // writers in serial order with the slot through which each reaches this target
+    const int wi[5] = {i, i - 1, i, i + 1, i};
+    const int wj[5] = {j - 1, j, j, j, j + 1};
+    const int ws[5] = {4, 2, 0, 1, 3};
+    int ghost = O.ghost[n];
+    double b[4];
+    bool have_b = false;
+    for (int q = 0; q < 5; ++q) {
+        if (wi[q] < 0 || wi[q] >= G.width || wj[q] < 0) continue;
+        const int idx = wj[q] * G.width + wi[q];
+        if (idx >= G.nthreads) continue;
+        const int f = R.flags[idx];
+        const int s = ws[q];
+        if (f & (1 << s)) ghost = n;
+        if (CLS != 2 && s == 0 && (f & (1 << 16))) ghost = -1;
+        if (f & (1 << (8 + s))) {
+            for (int c = 0; c < 4; ++c) b[c] = R.bi[(size_t)idx * 20 + s * 4 + c];
+            have_b = true;
+        }
+    }
+    O.ghost[n] = ghost;
+    if (have_b) {
+        O.bix[n] = b[0];
+        O.biy[n] = b[1];
+        O.ipx[n] = b[2];
+        O.ipy[n] = b[3];
+    }
+    const bool self_exists = i >= 0 && i < G.width && j >= 0 && j * G.width + i < G.nthreads;
+    const int sidx = j * G.width + i;
+    if (CLS == 2) {
+        if (self_exists && (R.flags[sidx] & (1 << 19))) O.hyb[n] = n;
+        return;
+    }
+    if (self_exists && (R.flags[sidx] & (1 << 16))) {
+        O.hyb[n] = R.hyb[sidx];
+        O.hyb2[n] = R.hyb2[sidx];
+        O.dnode[n] = R.dnode[sidx];
+        O.dbetween[n] = R.dbetween[sidx];
+        O.uv[n] = R.uv[sidx];
+    }
+    // dist_u_body / dist_v_body (pressure-indexed): writer before self is the west (u) or south (v) node
+    const int ip = J * nx + I;
+    const int pi = CLS == 0 ? i - 1 : i, pj = CLS == 0 ? j : j - 1;
+    double dv = 0;
+    bool have_d = false;
+    if (pi >= 0 && pi < G.width && pj >= 0 && pj * G.width + pi < G.nthreads) {
+        const int pidx = pj * G.width + pi;
+        if (R.flags[pidx] & (1 << 18)) {
+            dv = R.distB[pidx];
+            have_d = true;
+        }
+    }
+    if (self_exists && (R.flags[sidx] & (1 << 17))) {
+        dv = R.distA[sidx];
+        have_d = true;
+    }
+    if (have_d) O.dist[ip] = dv;
+}
+
+// zero_pressure_luo / zero_x_luo / zero_y_luo: one thread per row, left to right
+__global__ void k_zero_rows(int *tags, int stride, int i0, int i1, int j0, int j1, int rows, int scan_end)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= rows) return;
+    const int J = j0 + j;
+    if (J > j1) return;
+    bool rowIsntDone = true, flag = false;
+    for (int i = i0; i < i1; ++i) {
+        const int I = J * stride + i;
+        if (tags[I - 1] >= 0) {
+            if (tags[I] != -1 && tags[I - 1] == 0) rowIsntDone = false;
+            if (tags[I] == -1 && rowIsntDone) tags[I] = 0;
+            if (tags[I] == 0 && tags[I - 1] != 0) {
+                int k = i;
+                while (k < scan_end) {
+                    k++;
+                    if (tags[J * stride + k] != -1) flag = true;
+                }
+                if (!flag) {
+                    tags[I] = -1;
+                    rowIsntDone = false;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_tag_fill(int nUV, int nP, int *gUV, int *hUV, int *h2UV, double *dn, double *db, double *bix,
+                           double *biy, double *ipx, double *ipy, int *gP, int *hP)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nUV) {
+        gUV[t] = -1;
+        hUV[t] = -1;
+        h2UV[t] = -1;
+        dn[t] = 1;
+        db[t] = 1;
+        bix[t] = 0;
+        biy[t] = 0;
+        ipx[t] = 0;
+        ipy[t] = 0;
+    }
+    if (t < nP) {
+        gP[t] = -1;
+        hP[t] = -1;
+    }
+}
+
+// ---- bilinear interpolation --------------------------------------------------------
+__device__ __forceinline__ void inverse4_dev(const double a[16], double b[16], double *det)
+{
+    const double a11 = a[0], a12 = a[1], a13 = a[2], a14 = a[3];
+    const double a21 = a[4], a22 = a[5], a23 = a[6], a24 = a[7];
+    const double a31 = a[8], a32 = a[9], a33 = a[10], a34 = a[11];
+    const double a41 = a[12], a42 = a[13], a43 = a[14], a44 = a[15];
+    *det = a11 * a22 * a33 * a44 + a11 * a23 * a34 * a42 + a11 * a24 * a32 * a43 + a12 * a21 * a34 * a43 +
+           a12 * a23 * a31 * a44 + a12 * a24 * a33 * a41 + a13 * a21 * a32 * a44 + a13 * a22 * a34 * a41 +
+           a13 * a24 * a31 * a42 + a14 * a21 * a33 * a42 + a14 * a22 * a31 * a43 + a14 * a23 * a32 * a41 -
+           a11 * a22 * a34 * a43 - a11 * a23 * a32 * a44 - a11 * a24 * a33 * a42 - a12 * a21 * a33 * a44 -
+           a12 * a23 * a34 * a41 - a12 * a24 * a31 * a43 - a13 * a21 * a34 * a42 - a13 * a22 * a31 * a44 -
+           a13 * a24 * a32 * a41 - a14 * a21 * a32 * a43 - a14 * a22 * a33 * a41 - a14 * a23 * a31 * a42;
+    b[0] = a22 * a33 * a44 + a23 * a34 * a42 + a24 * a32 * a43 - a22 * a34 * a43 - a23 * a32 * a44 - a24 * a33 * a42;
+    b[1] = a12 * a34 * a43 + a13 * a32 * a44 + a14 * a33 * a42 - a12 * a33 * a44 - a13 * a34 * a42 - a14 * a32 * a43;
+    b[2] = a12 * a23 * a44 + a13 * a24 * a42 + a14 * a22 * a43 - a12 * a24 * a43 - a13 * a22 * a44 - a14 * a23 * a42;
+    b[3] = a12 * a24 * a33 + a13 * a22 * a34 + a14 * a23 * a32 - a12 * a23 * a34 - a13 * a24 * a32 - a14 * a22 * a33;
+    b[4] = a21 * a34 * a43 + a23 * a31 * a44 + a24 * a33 * a41 - a21 * a33 * a44 - a23 * a34 * a41 - a24 * a31 * a43;
+    b[5] = a11 * a33 * a44 + a13 * a34 * a41 + a14 * a31 * a43 - a11 * a34 * a43 - a13 * a31 * a44 - a14 * a33 * a41;
+    b[6] = a11 * a24 * a43 + a13 * a21 * a44 + a14 * a23 * a41 - a11 * a23 * a44 - a13 * a24 * a41 - a14 * a21 * a43;
+    b[7] = a11 * a23 * a34 + a13 * a24 * a31 + a14 * a21 * a33 - a11 * a24 * a33 - a13 * a21 * a34 - a14 * a23 * a31;
+    b[8] = a21 * a32 * a44 + a22 * a34 * a41 + a24 * a31 * a42 - a21 * a34 * a42 - a22 * a31 * a44 - a24 * a32 * a41;
+    b[9] = a11 * a34 * a42 + a12 * a31 * a44 + a14 * a32 * a41 - a11 * a32 * a44 - a12 * a34 * a41 - a14 * a31 * a42;
+    b[10] = a11 * a22 * a44 + a12 * a24 * a41 + a14 * a21 * a42 - a11 * a24 * a42 - a12 * a21 * a44 - a14 * a22 * a41;
+    b[11] = a11 * a24 * a32 + a12 * a21 * a34 + a14 * a22 * a31 - a11 * a22 * a34 - a12 * a24 * a31 - a14 * a21 * a32;
+    b[12] = a21 * a33 * a42 + a22 * a31 * a43 + a23 * a32 * a41 - a21 * a32 * a43 - a22 * a33 * a41 - a23 * a31 * a42;
+    b[13] = a11 * a32 * a43 + a12 * a33 * a41 + a13 * a31 * a42 - a11 * a33 * a42 - a12 * a31 * a43 - a13 * a32 * a41;
+    b[14] = a11 * a23 * a42 + a12 * a21 * a43 + a13 * a22 * a41 - a11 * a22 * a43 - a12 * a23 * a41 - a13 * a21 * a42;
+    b[15] = a11 * a22 * a33 + a12 * a23 * a31 + a13 * a21 * a32 - a11 * a23 * a32 - a12 * a21 * a33 - a13 * a22 * a31;
+}
+
+__device__ __forceinline__ void rows_dev(const double x[4], const double y[4], double a[16])
+{
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        a[4 * l] = 1;
+        a[4 * l + 1] = x[l];
+        a[4 * l + 2] = y[l];
+        a[4 * l + 3] = x[l] * y[l];
+    }
+}
+
+__device__ __forceinline__ void store_dev(int *idx4, double *coef4, int n, const int id[4], const double b[16],
+                                          double det, double px, double py)
+{
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        idx4[4 * (size_t)n + c] = id[c];
+        coef4[4 * (size_t)n + c] = (b[c] + b[4 + c] * px + b[8 + c] * py + b[12 + c] * px * py) / det;
+    }
+}
+
+struct BoxLaunch {
+    int i0, j0, width, nthreads;
+};
+
+// ghost-node velocity (interpolateVelocityToGhostNodeX/Y): image-point value into
+// imageValue and the new ghost value into staging; blockIdx.y selects u (0) or v (1)
+__global__ void k_ghost_velocity(BoxLaunch B, int nx, int ny, const double *__restrict__ u, const int *gtags,
+                                 const double *xu, const double *yu, const double *xv, const double *yv,
+                                 const double *uB, const double *vB, const double *bix, const double *biy,
+                                 const double *ipx, const double *ipy, int *idx4, double *coef4, double *imageValue,
+                                 double *staging)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int dir = blockIdx.y, nU = (nx - 1) * ny;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
+    int n;
+    const double *xc, *yc;
+    double ub;
+    if (dir == 0) {
+        n = J * (nx - 1) + I;
+        if (n >= nU) return;
+        xc = xu; yc = yu; ub = uB[0];
+    } else {
+        if (J * nx + I > nx * (ny - 1)) return;
+        n = J * nx + I + nU;
+        xc = xv; yc = yv; ub = vB[0];
+    }
+    if (gtags[n] <= 0) return;
+    int ii = I - 5, jj = J - 5;
+    while (xc[ii] < ipx[n]) ii++;
+    while (yc[jj] < ipy[n]) jj++;
+    double x[4] = {xc[ii - 1], xc[ii], xc[ii - 1], xc[ii]};
+    double y[4] = {yc[jj - 1], yc[jj - 1], yc[jj], yc[jj]};
+    int id[4];
+    if (dir == 0) {
+        id[0] = (jj - 1) * (nx - 1) + ii - 1; id[1] = id[0] + 1;
+        id[2] = jj * (nx - 1) + ii - 1;       id[3] = id[2] + 1;
+    } else {
+        id[0] = (jj - 1) * nx + ii - 1 + nU; id[1] = id[0] + 1;
+        id[2] = jj * nx + ii - 1 + nU;       id[3] = id[2] + 1;
+    }
+    double q[4] = {u[id[0]], u[id[1]], u[id[2]], u[id[3]]};
+    double mn = 1.0;
+    int close = -1;
+    bool inflag = false;
+    for (int l = 0; l < 4; ++l) {
+        double ex = x[l] - bix[n], ey = y[l] - biy[n];
+        double s = sqrt(ex * ex + ey * ey);
+        if (s < mn) { mn = s; close = id[l]; }
+        if (gtags[id[l]] > 0) inflag = true;
+    }
+    for (int l = 0; l < 4; ++l) {
+        if (gtags[id[l]] == n) { x[l] = bix[id[l]]; y[l] = biy[id[l]]; q[l] = ub; }
+        else if (id[l] == close && !inflag) { x[l] = bix[n]; y[l] = biy[n]; q[l] = ub; }
+    }
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    inverse4_dev(a, b, &det);
+    const double a0 = b[0] / det * q[0] + b[1] / det * q[1] + b[2] / det * q[2] + b[3] / det * q[3];
+    const double a1 = b[4] / det * q[0] + b[5] / det * q[1] + b[6] / det * q[2] + b[7] / det * q[3];
+    const double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
+    const double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
+    store_dev(idx4, coef4, n, id, b, det, ipx[n], ipy[n]);
+    const double val = a0 + a1 * ipx[n] + a2 * ipy[n] + a3 * ipx[n] * ipy[n];
+    imageValue[n] = val;
+    staging[n] = 2 * ub - val;
+}
+
+// apply the staged ghost values (second half of the snapshot update)
+__global__ void k_apply_ghost(BoxLaunch B, int nx, int ny, const int *gtags, const double *staging, double *u)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int dir = blockIdx.y, nU = (nx - 1) * ny;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
+    int n;
+    if (dir == 0) {
+        n = J * (nx - 1) + I;
+        if (n >= nU) return;
+    } else {
+        if (J * nx + I > nx * (ny - 1)) return;
+        n = J * nx + I + nU;
+    }
+    if (gtags[n] > 0) u[n] = staging[n];
+}
+
+// hybrid-node velocity (interpolateVelocityToHybridNodeX/Y) into ustar
+__global__ void k_hybrid_velocity(BoxLaunch B, int nx, int ny, const double *__restrict__ u, const int *htags,
+                                  const double *xu, const double *yu, const double *xv, const double *yv,
+                                  const double *uB, const double *vB, const double *bix, const double *biy,
+                                  const double *ipx, const double *ipy, int *idx4, double *coef4,
+                                  double *imageValue, double *ustar)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int dir = blockIdx.y, nU = (nx - 1) * ny;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
+    int n;
+    const double *xc, *yc;
+    double ub;
+    if (dir == 0) {
+        n = J * (nx - 1) + I;
+        if (n >= nU) return;
+        xc = xu; yc = yu; ub = uB[0];
+    } else {
+        if (J * nx + I > nx * (ny - 1)) return;
+        n = J * nx + I + nU;
+        xc = xv; yc = yv; ub = vB[0];
+    }
+    if (htags[n] <= 0) return;
+    int ii = I - 5, jj = J - 5;
+    while (xc[ii] < ipx[n]) ii++;
+    while (yc[jj] < ipy[n]) jj++;
+    double x[4] = {xc[ii - 1], xc[ii], xc[ii - 1], xc[ii]};
+    double y[4] = {yc[jj - 1], yc[jj - 1], yc[jj], yc[jj]};
+    int id[4];
+    if (dir == 0) {
+        id[0] = (jj - 1) * (nx - 1) + ii - 1; id[1] = id[0] + 1;
+        id[2] = jj * (nx - 1) + ii - 1;       id[3] = id[2] + 1;
+    } else {
+        id[0] = (jj - 1) * nx + ii - 1 + nU; id[1] = id[0] + 1;
+        id[2] = jj * nx + ii - 1 + nU;       id[3] = id[2] + 1;
+    }
+    double q[4] = {u[id[0]], u[id[1]], u[id[2]], u[id[3]]};
+    for (int l = 0; l < 4; ++l)
+        if (htags[id[l]] == n) { x[l] = bix[n]; y[l] = biy[n]; q[l] = ub; }
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    inverse4_dev(a, b, &det);
+    const double a0 = (b[0] * q[0] + b[1] * q[1] + b[2] * q[2] + b[3] * q[3]) / det;
+    const double a1 = (b[4] * q[0] + b[5] * q[1] + b[6] * q[2] + b[7] * q[3]) / det;
+    const double a2 = (b[8] * q[0] + b[9] * q[1] + b[10] * q[2] + b[11] * q[3]) / det;
+    const double a3 = (b[12] * q[0] + b[13] * q[1] + b[14] * q[2] + b[15] * q[3]) / det;
+    store_dev(idx4, coef4, n, id, b, det, xc[I], yc[J]);
+    ustar[n] = a0 + a1 * xc[I] + a2 * yc[J] + a3 * yc[J] * xc[I];
+    imageValue[n] = a0 + a1 * ipx[n] + a2 * ipy[n] + a3 * ipx[n] * ipy[n];
+}
+
+// Neumann row of the pressure fit at a body-intercept corner
+__device__ __forceinline__ void neumann_row(double px, double py, double bx_, double by_, double dudt, double dvdt,
+                                            double *a4, double *q)
+{
+    const double nxv = px - bx_, nyv = py - by_;
+    const double nl = sqrt(nxv * nxv + nyv * nyv);
+    *q = -(nxv / nl * dudt + nyv / nl * dvdt);
+    a4[0] = 0;
+    a4[1] = nxv / nl;
+    a4[2] = nyv / nl;
+    a4[3] = nyv / nl * bx_ + nxv / nl * by_;
+}
+
+// pressure at hybrid nodes (interpolatePressureToHybridNode) into pstar
+__global__ void k_hybrid_pressure(BoxLaunch B, int nx, int ny, const double *__restrict__ p, const int *htags,
+                                  const double *xv, const double *yu, const double *uB, const double *uBk,
+                                  const double *vB, const double *vBk, double dt, const double *bix,
+                                  const double *biy, const double *ipx, const double *ipy, int *idx4,
+                                  double *coef4, double *pstar)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
+    if (ip >= nx * ny || htags[ip] <= 0) return;
+    int ii = I - 5, jj = J - 5;
+    while (xv[ii] < ipx[ip]) ii++;
+    while (yu[jj] < ipy[ip]) jj++;
+    double x[4] = {xv[ii - 1], xv[ii], xv[ii - 1], xv[ii]};
+    double y[4] = {yu[jj - 1], yu[jj - 1], yu[jj], yu[jj]};
+    const int id[4] = {(jj - 1) * nx + ii - 1, (jj - 1) * nx + ii, jj * nx + ii - 1, jj * nx + ii};
+    double q[4] = {p[id[0]], p[id[1]], p[id[2]], p[id[3]]};
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    const double dudt = (uB[0] - uBk[0]) / dt, dvdt = (vB[0] - vBk[0]) / dt;
+    for (int l = 0; l < 4; ++l)
+        if (htags[id[l]] == ip) {
+            x[l] = bix[ip];
+            y[l] = biy[ip];
+            neumann_row(ipx[ip], ipy[ip], x[l], y[l], dudt, dvdt, a + 4 * l, &q[l]);
+        }
+    inverse4_dev(a, b, &det);
+    const double a0 = b[0] / det * q[0] + b[1] / det * q[1] + b[2] / det * q[2] + b[3] / det * q[3];
+    const double a1 = b[4] / det * q[0] + b[5] / det * q[1] + b[6] / det * q[2] + b[7] / det * q[3];
+    const double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
+    const double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
+    store_dev(idx4, coef4, ip, id, b, det, xv[I], yu[J]);
+    pstar[ip] = a0 + a1 * xv[I] + a2 * yu[J] + a3 * xv[I] * yu[J];
+}
+
+// ghost pressure (interpolatePressureToGhostNode): values to staging, dpdn, biP
+__global__ void k_ghost_pressure(BoxLaunch B, int nx, int ny, const double *__restrict__ p, const int *gtags,
+                                 const double *xv, const double *yu, const double *uB, const double *uBk,
+                                 const double *vB, const double *vBk, double dt, const double *bix,
+                                 const double *biy, const double *ipx, const double *ipy, int *idx4, double *coef4,
+                                 double *biP, double *dpdn, double *staging)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
+    if (ip >= nx * ny || gtags[ip] <= 0) return;
+    int ii = I - 5, jj = J - 5;
+    while (xv[ii] < ipx[ip]) ii++;
+    while (yu[jj] < ipy[ip]) jj++;
+    double x[4] = {xv[ii - 1], xv[ii], xv[ii - 1], xv[ii]};
+    double y[4] = {yu[jj - 1], yu[jj - 1], yu[jj], yu[jj]};
+    const int id[4] = {(jj - 1) * nx + ii - 1, (jj - 1) * nx + ii, jj * nx + ii - 1, jj * nx + ii};
+    double q[4] = {p[id[0]], p[id[1]], p[id[2]], p[id[3]]};
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    double mn = 1.0, matD = 0;
+    int close = -1;
+    for (int l = 0; l < 4; ++l) {
+        double ex = x[l] - bix[ip], ey = y[l] - biy[ip];
+        double s = sqrt(ex * ex + ey * ey);
+        if (s < mn) { mn = s; close = id[l]; }
+    }
+    const double dudt = (uB[0] - uBk[0]) / dt, dvdt = (vB[0] - vBk[0]) / dt;
+    for (int l = 0; l < 4; ++l) {
+        if (gtags[id[l]] > 0) {
+            x[l] = bix[id[l]];
+            y[l] = biy[id[l]];
+            neumann_row(ipx[id[l]], ipy[id[l]], x[l], y[l], dudt, dvdt, a + 4 * l, &q[l]);
+        }
+        if (id[l] == close) {
+            x[l] = bix[ip];
+            y[l] = biy[ip];
+            const double nxv = ipx[ip] - x[l], nyv = ipy[ip] - y[l];
+            const double nl = sqrt(nxv * nxv + nyv * nyv);
+            matD = nxv / nl * dudt + nyv / nl * dvdt;
+        }
+    }
+    inverse4_dev(a, b, &det);
+    const double a0 = b[0] / det * q[0] + b[1] / det * q[1] + b[2] / det * q[2] + b[3] / det * q[3];
+    const double a1 = b[4] / det * q[0] + b[5] / det * q[1] + b[6] / det * q[2] + b[7] / det * q[3];
+    const double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
+    const double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
+    store_dev(idx4, coef4, ip, id, b, det, ipx[ip], ipy[ip]);
+    const double ipv = a0 + a1 * ipx[ip] + a2 * ipy[ip] + a3 * ipy[ip] * ipx[ip];
+    biP[ip] = a0 + a1 * bix[ip] + a2 * biy[ip] + a3 * bix[ip] * biy[ip];
+    const double ex = ipx[ip] - xv[I], ey = ipy[ip] - yu[J];
+    const double d = sqrt(ex * ex + ey * ey) * matD;
+    dpdn[ip] = d;
+    staging[ip] = ipv + d;
+}
+
+__global__ void k_apply_ghost_p(BoxLaunch B, int nx, int ny, const int *gtags, const double *staging, double *p)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
+    if (ip < nx * ny && gtags[ip] > 0) p[ip] = staging[ip];
+}
+
+// alpha-blend at hybrid nodes (weightX, weightY: blockIdx.y 0/1; weightP: CLS 2)
+template <int CLS>
+__global__ void k_weight(BoxLaunch B, int nx, int ny, double *f, const double *fstar, const int *gtags,
+                         const int *htags, const double *xa, const double *ya, const double *xb, const double *yb,
+                         const double *bix, const double *biy)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int nU = (nx - 1) * ny;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
+    int n, sv;
+    const double *xc, *yc;
+    if (CLS == 2) {
+        if (J * nx + I > nx * ny) return;
+        n = J * nx + I;
+        sv = nx;
+        xc = xa; yc = ya;
+    } else if (blockIdx.y == 0) {
+        n = J * (nx - 1) + I;
+        sv = nx - 1;
+        xc = xa; yc = ya;
+    } else {
+        if (J * nx + I > nx * (ny - 1)) return;
+        n = J * nx + I + nU;
+        sv = nx;
+        xc = xb; yc = yb;
+    }
+    if (htags[n] <= 0) return;
+    double d1 = 0, d2 = 0;
+    const double dx = xc[I] - xc[I - 1], dy = yc[J] - yc[J - 1];
+    double ex, ey;
+    if (gtags[n - 1] > 0) {
+        ex = bix[n - 1] - xc[I - 1]; ey = biy[n - 1] - yc[J];
+        d1 = sqrt(ex * ex + ey * ey);
+    } else if (gtags[n + 1] > 0) {
+        ex = bix[n + 1] - xc[I + 1]; ey = biy[n + 1] - yc[J];
+        d1 = sqrt(ex * ex + ey * ey);
+    }
+    if (gtags[n - sv] > 0) {
+        ex = bix[n - sv] - xc[I]; ey = biy[n - sv] - yc[J - 1];
+        d2 = sqrt(ex * ex + ey * ey);
+    }
+    if (gtags[n + sv] > 0) {
+        ex = bix[n + sv] - xc[I]; ey = biy[n + sv] - yc[J + 1];
+        d2 = sqrt(ex * ex + ey * ey);
+    }
+    const double r1 = d1 / dx, r2 = d2 / dy;
+    const double alpha = sqrt(r1 * r1 + r2 * r2);
+    f[n] = (1 - alpha) * f[n] + alpha * fstar[n];
+}
+
+// u inside the body := body velocity (setInsideVelocity over the u-index map)
+__global__ void k_set_inside(int nx, int ny, const int *gtags, double *u, const double *uB, const double *vB)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nU = (nx - 1) * ny, nUV = nU + nx * (ny - 1);
+    if (i >= nU) return;
+    const int I = i % (nx - 1), J = i / (nx - 1), iv = J * nx + I + nU;
+    u[i] = (gtags[i] != 0) * u[i] + (gtags[i] == 0) * uB[0];
+    if (iv < nUV) u[iv] = (gtags[iv] != 0) * u[iv] + (gtags[iv] == 0) * vB[0];
+}
+
+// convective outflow on the x+ boundary (updateBoundaryX / updateBoundaryY)
+__global__ void k_robin(int nx, int ny, const double *u, double *xp, const double *dx, double dt, double Uinf,
+                        double Vinf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nU = (nx - 1) * ny;
+    if (t < ny) {
+        const int J = t, I = nx - 1, i = J * (nx - 1) + I;
+        const double beta = Uinf * dt / dx[I];
+        xp[J] = xp[J] * (1 - beta) + beta * u[i - 1];
+    } else if (t < 2 * ny - 1) {
+        const int J = t - ny, I = nx, i = J * nx + I;
+        const double beta = Vinf * dt / dx[I - 1];
+        xp[J + ny] = xp[J + ny] * (1 - beta) + beta * u[i + nU - 1];
+    }
+}
+
+// control-volume force: the six sums of dragLeftRight, dragBottomTop, dragUnsteady,
+// liftLeftRight, liftBottomTop, liftUnsteady in one launch, reduced in a fixed order
+__global__ void k_force(int nx, int ny, const int *bb, const double *u, const double *uold, const double *p,
+                        const int *gtags, double nu, const double *dx, const double *dy, double dt, double *part,
+                        unsigned int *arrive, double *out)
+{
+    const int I = bb[0], J = bb[1], ncx = bb[2], ncy = bb[3];
+    const int nU = (nx - 1) * ny;
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (ncx + 1) * (ncy + 1); idx += stride) {
+        if (idx < ncy) {
+            const int Ip = (J + idx) * nx + I, Iu = (J + idx) * (nx - 1) + I;
+            const double a = u[Iu + ncx] + u[Iu + ncx - 1], b = u[Iu - 1] + u[Iu];
+            s[0] += -((p[Ip + ncx] - p[Ip]) * dy[J + idx] + (a * a / 4 - b * b / 4) * dy[J + idx] -
+                      nu * ((u[Iu + ncx] - u[Iu + ncx - 1]) / dx[I + ncx] - (u[Iu] - u[Iu - 1]) / dx[I]) * dy[J + idx]);
+        }
+        if (idx <= ncx) {
+            const int Iu = J * (nx - 1) + (I - 1 + idx), Iv = nU + (J - 1) * nx + I + idx;
+            s[1] += -((0.25 * (u[Iu + ncy * (nx - 1)] + u[Iu + (ncy - 1) * (nx - 1)]) *
+                           (u[Iv + ncy * nx] + u[Iv + ncy * nx - 1]) -
+                       0.25 * (u[Iu] + u[Iu - (nx - 1)]) * (u[Iv] + u[Iv - 1])) -
+                      nu * (((u[Iu + ncy * (nx - 1)] - u[Iu + (ncy - 1) * (nx - 1)]) / 2.0 / (dy[J + ncy] + dy[J + ncy - 1]) +
+                             (u[Iv + ncy * nx] - u[Iv + ncy * nx - 1]) / 2.0 / (dx[I + idx] + dx[I + idx - 1])) -
+                            ((u[Iu] - u[Iu - (nx - 1)]) / 2.0 / (dy[J] + dy[J - 1]) +
+                             (u[Iv] - u[Iv - 1]) / 2.0 / (dx[I + idx] + dx[I + idx - 1])))) *
+                    0.5 * (dx[I + idx] + dx[I + idx - 1]);
+        }
+        if (idx < (ncx + 1) * ncy) {
+            const int i = idx % (ncx + 1), j = idx / (ncx + 1), Iu = (J + j) * (nx - 1) + (I - 1 + i);
+            s[2] += -(gtags[Iu] == -1) * ((u[Iu] * dy[J + j] - uold[Iu] * dy[J + j]) / dt * 0.5 * (dx[I + i] + dx[I - 1 + i]));
+        }
+        if (idx <= ncy) {
+            const int Iu = (J + idx) * (nx - 1) + (I - 1), Iv = nU + (J - 1 + idx) * nx + I;
+            s[3] += -((0.25 * (u[Iu + ncx] + u[Iu + ncx - (nx - 1)]) * (u[Iv + ncx] + u[Iv + ncx - 1]) -
+                       0.25 * (u[Iu] + u[Iu - (nx - 1)]) * (u[Iv] + u[Iv - 1])) -
+                      nu * (((u[Iu + ncx] - u[Iu + ncx - (nx - 1)]) / 2.0 / (dy[J + idx] + dy[J - 1 + idx]) +
+                             (u[Iv + ncx] - u[Iv + ncx - 1]) / 2.0 / (dx[I + ncx] + dx[I + ncx - 1])) -
+                            ((u[Iu] - u[Iu - (nx - 1)]) / 2.0 / (dy[J + idx] + dy[J - 1 + idx]) +
+                             (u[Iv] - u[Iv - 1]) / 2.0 / (dx[I] + dx[I - 1])))) *
+                    0.5 * (dy[J + idx] + dy[J - 1 + idx]);
+        }
+        if (idx < ncx) {
+            const int Ip = J * nx + I + idx, Iv = nU + (J - 1) * nx + I + idx;
+            const double a = u[Iv + (ncy + 1) * nx] + u[Iv + ncy * nx], b = u[Iv] + u[Iv - nx];
+            s[4] += -((p[Ip + ncy * nx] - p[Ip - nx]) * dx[I + idx] + (0.25 * a * a - 0.25 * b * b) * dx[I + idx] -
+                      nu * ((u[Iv + (ncy + 1) * nx] - u[Iv + ncy * nx]) * dx[I + idx] / dy[J + ncy] -
+                            (u[Iv] - u[Iv - nx]) * dx[I] / dy[J - 1]));
+        }
+        if (idx < ncx * (ncy + 1)) {
+            const int i = idx % ncx, j = idx / ncx, Iv = (J - 1 + j) * nx + (I + i) + nU;
+            s[5] += -(gtags[Iv] == -1) * ((u[Iv] * dx[I + i] - uold[Iv] * dx[I + i]) / dt * 0.5 * (dy[J + j] + dy[J - 1 + j]));
+        }
+    }
+    // block reduction, then the last block sums the block partials in order
+    __shared__ double sh[6][32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < 6; ++k) {
+        double a = s[k];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) sh[k][wid] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double a = 0;
+        for (int q = 0; q < nw; ++q) a += sh[threadIdx.x][q];
+        part[blockIdx.x * 6 + threadIdx.x] = a;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        double t[6] = {0, 0, 0, 0, 0, 0};
+        for (int b = 0; b < (int)gridDim.x; ++b)
+            for (int k = 0; k < 6; ++k) t[k] += __ldcg(part + b * 6 + k);
+        out[0] = t[0] + t[1] + t[2];
+        out[1] = t[3] + t[4] + t[5];
+        *arrive = 0;
+    }
+}
+
+// prescribed motion (luo_base/move.cu set_movement): x = xnew + offset, uB = unew with
+// xnew, unew taken from a table of the host-evaluated motion indexed by the step
+__global__ void k_body_motion(int total, const int *step, int table_len, const double *table, const double *bdx,
+                              double *bx, double *uB, double *motion)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = *step;
+    s = s < 0 ? 0 : (s >= table_len ? table_len - 1 : s);
+    const double xnew = table[2 * s], unew = table[2 * s + 1];
+    if (i < total) {
+        bx[i] = xnew + bdx[i];
+        uB[i] = unew;
+    }
+    if (i == 0) {
+        motion[0] = xnew;
+        motion[2] = unew;
+    }
+}
+
+// _pre_step copies of the body velocities: uB0 = uBk = uB (and v)
+__global__ void k_body_pre_step(int total, const double *uB, const double *vB, double *uBk, double *vBk,
+                                double *motion)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < total) {
+        uBk[i] = uB[i];
+        vBk[i] = vB[i];
+    }
+    if (i == 0) {
+        motion[4] = motion[0];
+        motion[5] = motion[1];
+        motion[6] = motion[2];
+        motion[7] = motion[3];
+    }
+}
 
 __global__ void k_step_counter(int *s) { *s += 1; }
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int ref_threads(int w, int h) { return ((int)(((double)w * h - 0.5) / 256) + 1) * 256; }
+
+struct IbHost {
+    TagRecords rec{};
+    int *bb = nullptr;             // device [i0, j0, ncx, ncy]
+    double *motion_table = nullptr;
+    int table_len = 0;
+    double *staging = nullptr;
+    unsigned int *force_arrive = nullptr;
+    bool moving = false;
+};
+static std::vector<IbHost> g_ib_host;  // one per context (indexed by Context::ib_slot)
+
+static IbHost &hostside(Context &c) { return g_ib_host[c.ib_slot]; }
+
+void setup_ib(Context &c)
+{
+    IbArrays &b = c.ib;
+    const size_t UV = c.g.nUV, P = c.g.nP;
+    const int nb = c.body.total;
+    b.ghostUV = c.carve<int>(UV);
+    b.hybridUV = c.carve<int>(UV);
+    b.hybrid2UV = c.carve<int>(UV);
+    b.ghostP = c.carve<int>(P);
+    b.hybridP = c.carve<int>(P);
+    b.biX = c.carve<double>(UV);
+    b.biY = c.carve<double>(UV);
+    b.ipX = c.carve<double>(UV);
+    b.ipY = c.carve<double>(UV);
+    b.bipX = c.carve<double>(P);
+    b.bipY = c.carve<double>(P);
+    b.ippX = c.carve<double>(P);
+    b.ippY = c.carve<double>(P);
+    b.distNode = c.carve<double>(UV);
+    b.distBetween = c.carve<double>(UV);
+    b.distU = c.carve<double>(P);
+    b.distV = c.carve<double>(P);
+    b.uvBody = c.carve<double>(UV);
+    b.ustar = c.carve<double>(UV);
+    b.pstar = c.carve<double>(P);
+    b.dpdn = c.carve<double>(P);
+    b.biP = c.carve<double>(P);
+    b.imageValue = c.carve<double>(UV);
+    b.gIdx = c.carve<int>(4 * UV);
+    b.hIdx = c.carve<int>(4 * UV);
+    b.gpIdx = c.carve<int>(4 * P);
+    b.hpIdx = c.carve<int>(4 * P);
+    b.gCoef = c.carve<double>(4 * UV);
+    b.hCoef = c.carve<double>(4 * UV);
+    b.gpCoef = c.carve<double>(4 * P);
+    b.hpCoef = c.carve<double>(4 * P);
+    b.gnValue = c.carve<double>(UV > P ? UV : P);
+    b.bx = c.carve<double>(nb);
+    b.by = c.carve<double>(nb);
+    b.uB = c.carve<double>(nb);
+    b.vB = c.carve<double>(nb);
+    b.uBk = c.carve<double>(nb);
+    b.vBk = c.carve<double>(nb);
+    b.bdx = c.carve<double>(nb);
+    b.bdy = c.carve<double>(nb);
+    b.motion = c.carve<double>(8);
+    b.forceOut = c.carve<double>(2);
+    const int fblocks = 64;
+    b.forcePart = c.carve<double>(6 * fblocks);
+
+    if ((int)g_ib_host.size() <= c.ib_slot || c.ib_slot < 0) {
+        c.ib_slot = (int)g_ib_host.size();
+        g_ib_host.emplace_back();
+    }
+    IbHost &H = hostside(c);
+    H = IbHost();
+    H.bb = c.carve<int>(4);
+    H.force_arrive = c.carve<unsigned int>(4);
+    CUIBM_TRY(cudaMemsetAsync(H.force_arrive, 0, 4 * sizeof(unsigned int), c.stream));
+    // records sized for the box, with room for the box to grow as the body moves
+    const int w = c.bb.ncx + 16, h = c.bb.ncy + 16;
+    H.rec.nrec = ref_threads(w, h);
+    const size_t nr = H.rec.nrec;
+    H.rec.flags = c.carve<int>(nr);
+    H.rec.hyb = c.carve<int>(nr);
+    H.rec.hyb2 = c.carve<int>(nr);
+    H.rec.dnode = c.carve<double>(nr);
+    H.rec.dbetween = c.carve<double>(nr);
+    H.rec.uv = c.carve<double>(nr);
+    H.rec.distA = c.carve<double>(nr);
+    H.rec.distB = c.carve<double>(nr);
+    H.rec.bi = c.carve<double>(nr * 20);
+    const BodyState &B = c.body;
+    H.moving = B.xCoeff != 0 || B.uCoeff != 0;
+    // the host-evaluated prescribed motion for every step (luo_base/move.cu:121-146):
+    // xnew = xC sin(2 pi f t + xPhase), unew = uC cos(2 pi f t + uPhase), t = dt * step
+    H.table_len = c.P.nt + c.P.startStep + 2;
+    std::vector<double> tab(2 * (size_t)H.table_len);
+    for (int s = 0; s < H.table_len; ++s) {
+        const double t = c.P.dt * s;
+        tab[2 * s] = B.xCoeff * std::sin(2 * M_PI * B.freq * t + B.xPhase);
+        tab[2 * s + 1] = B.uCoeff * std::cos(2 * M_PI * B.freq * t + B.uPhase);
+    }
+    H.motion_table = c.carve<double>(tab.size());
+    CUIBM_TRY(cudaMemcpy(H.motion_table, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+}
+
+static BoxLaunch box(Context &c)
+{
+    return BoxLaunch{c.bb.i0, c.bb.j0, c.bb.ncx, ref_threads(c.bb.ncx, c.bb.ncy)};
+}
+
+// luo_base::initialise body part (luo_base.cu:48-86): positions and velocities at
+// t = dt*timeStep, then uBk from the velocity at t - dt; the box is the one
+// bodies::initialise computed before this move.
+void initialise_body(Context &c)
+{
+    IbHost &H = hostside(c);
+    const BodyState &B = c.body;
+    const int nb = B.total;
+    const double t = c.P.dt * c.timeStep;
+    const double xnew = B.xCoeff * std::sin(2 * M_PI * B.freq * t + B.xPhase);
+    const double unew = B.uCoeff * std::cos(2 * M_PI * B.freq * t + B.uPhase);
+    const double uoldd = B.uCoeff * std::cos(2 * M_PI * B.freq * (t - c.P.dt) + B.uPhase);
+    std::vector<double> x(nb), y(B.y), uB(nb, unew), vB(nb, 0.0), uBk(nb, uoldd), vBk(nb, 0.0);
+    for (int i = 0; i < nb; ++i) x[i] = xnew + B.dxp[i];
+    auto up = [&](double *d, const std::vector<double> &h) {
+        CUIBM_TRY(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    };
+    up(c.ib.bx, x);
+    up(c.ib.by, y);
+    up(c.ib.uB, uB);
+    up(c.ib.vB, vB);
+    up(c.ib.uBk, uBk);
+    up(c.ib.vBk, vBk);
+    up(c.ib.bdx, B.dxp);
+    up(c.ib.bdy, B.dyp);
+    double motion[8] = {xnew, B.midY, unew, 0, xnew, B.midY, unew, 0};
+    CUIBM_TRY(cudaMemcpyAsync(c.ib.motion, motion, sizeof motion, cudaMemcpyHostToDevice, c.stream));
+    int bb[4] = {c.bb.i0, c.bb.j0, c.bb.ncx, c.bb.ncy};
+    CUIBM_TRY(cudaMemcpyAsync(H.bb, bb, sizeof bb, cudaMemcpyHostToDevice, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    c.ib_midX = xnew;
+    c.ib_midY = B.midY;
+}
+
+void launch_tag_points(Context &c)
+{
+    IbHost &H = hostside(c);
+    IbArrays &b = c.ib;
+    const int nx = c.g.nx, ny = c.g.ny;
+    const int w = c.bb.ncx, h = c.bb.ncy, nthreads = ref_threads(w, h);
+    if (nthreads > H.rec.nrec) throw InputError("the body's box outgrew the tagging records");
+    const int nfill = c.g.nUV > c.g.nP ? c.g.nUV : c.g.nP;
+    k_tag_fill<<<blocks_for(nfill), kBlock, 0, c.stream>>>(c.g.nUV, c.g.nP, b.ghostUV, b.hybridUV, b.hybrid2UV,
+                                                          b.distNode, b.distBetween, b.biX, b.biY, b.ipX, b.ipY,
+                                                          b.ghostP, b.hybridP);
+    // midX is the body's current centre abscissa (the prescribed xnew), midY its centroid
+    TagGeom G{b.bx, b.by, b.uB, c.xu, c.yu, c.bb.i0, c.bb.j0, w, h, nthreads, nx, ny, c.body.total, c.ib_midX,
+              c.ib_midY};
+    TagOut O{b.ghostUV, b.hybridUV, b.hybrid2UV, b.distNode, b.distBetween, b.uvBody, b.biX, b.biY, b.ipX, b.ipY,
+             b.distU};
+    const int rows = (nthreads + w - 1) / w;
+    const int nres = (w + 2) * (rows + 2);
+    k_tag_velocity_records<0><<<blocks_for(nthreads), kBlock, 0, c.stream>>>(G, H.rec);
+    k_tag_resolve<0><<<blocks_for(nres), kBlock, 0, c.stream>>>(G, H.rec, O);
+    G.vel = b.vB;
+    G.xc = c.xv;
+    G.yc = c.yv;
+    O.dist = b.distV;
+    k_tag_velocity_records<1><<<blocks_for(nthreads), kBlock, 0, c.stream>>>(G, H.rec);
+    k_tag_resolve<1><<<blocks_for(nres), kBlock, 0, c.stream>>>(G, H.rec, O);
+    G.xc = c.xv;
+    G.yc = c.yu;
+    TagOut OP{b.ghostP, b.hybridP, nullptr, nullptr, nullptr, nullptr, b.bipX, b.bipY, b.ippX, b.ippY, nullptr};
+    k_tag_pressure_records<<<blocks_for(nthreads), kBlock, 0, c.stream>>>(G, H.rec);
+    k_tag_resolve<2><<<blocks_for(nres), kBlock, 0, c.stream>>>(G, H.rec, OP);
+    const int i0 = c.bb.i0, i1 = c.bb.i0 + w, j0 = c.bb.j0, j1 = c.bb.j0 + h;
+    const int zrows = ref_threads(i1 - i0, 1);
+    k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostP, nx, i0, i1, j0, j1, zrows, nx);
+    k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostUV, nx - 1, i0, i1, j0, j1, zrows, nx - 1);
+    k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostUV + c.g.nU, nx, i0, i1, j0, j1, zrows, nx - 1);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_ghost_velocity(Context &c, double *field, bool set)
+{
+    IbArrays &b = c.ib;
+    BoxLaunch B = box(c);
+    dim3 grid(blocks_for(B.nthreads), 2);
+    k_ghost_velocity<<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, field, b.ghostUV, c.xu, c.yu, c.xv, c.yv,
+                                                    b.uB, b.vB, b.biX, b.biY, b.ipX, b.ipY, b.gIdx, b.gCoef,
+                                                    b.imageValue, b.gnValue);
+    if (set) k_apply_ghost<<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, b.ghostUV, b.gnValue, field);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_hybrid_velocity(Context &c, const double *field)
+{
+    IbArrays &b = c.ib;
+    BoxLaunch B = box(c);
+    dim3 grid(blocks_for(B.nthreads), 2);
+    k_hybrid_velocity<<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, field, b.hybridUV, c.xu, c.yu, c.xv, c.yv,
+                                                     b.uB, b.vB, b.biX, b.biY, b.ipX, b.ipY, b.hIdx, b.hCoef,
+                                                     b.imageValue, b.ustar);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_set_inside(Context &c, double *field)
+{
+    k_set_inside<<<blocks_for(c.g.nU), kBlock, 0, c.stream>>>(c.g.nx, c.g.ny, c.ib.ghostUV, field, c.ib.uB, c.ib.vB);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_weight_uhat(Context &c)
+{
+    IbArrays &b = c.ib;
+    BoxLaunch B = box(c);
+    dim3 grid(blocks_for(B.nthreads), 2);
+    k_weight<0><<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, c.uhat, b.ustar, b.ghostUV, b.hybridUV, c.xu,
+                                               c.yu, c.xv, c.yv, b.biX, b.biY);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_hybrid_pressure(Context &c)
+{
+    IbArrays &b = c.ib;
+    BoxLaunch B = box(c);
+    k_hybrid_pressure<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(
+        B, c.g.nx, c.g.ny, c.p, b.hybridP, c.xv, c.yu, b.uB, b.uBk, b.vB, b.vBk, c.P.dt, b.bipX, b.bipY, b.ippX,
+        b.ippY, b.hpIdx, b.hpCoef, b.pstar);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_weight_pressure(Context &c)
+{
+    IbArrays &b = c.ib;
+    BoxLaunch B = box(c);
+    k_weight<2><<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, c.p, b.pstar, b.ghostP,
+                                                                 b.hybridP, c.xv, c.yu, nullptr, nullptr, b.bipX,
+                                                                 b.bipY);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_ghost_pressure(Context &c, bool set)
+{
+    IbArrays &b = c.ib;
+    BoxLaunch B = box(c);
+    k_ghost_pressure<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(
+        B, c.g.nx, c.g.ny, c.p, b.ghostP, c.xv, c.yu, b.uB, b.uBk, b.vB, b.vBk, c.P.dt, b.bipX, b.bipY, b.ippX, b.ippY,
+        b.gpIdx, b.gpCoef, b.biP, b.dpdn, b.gnValue);
+    if (set) k_apply_ghost_p<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, b.ghostP, b.gnValue, c.p);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_robin(Context &c)
+{
+    // updateRobinBoundary: Uinf = Vinf = 1 (luo_base/intermediateVelocity.cu:216-217)
+    k_robin<<<blocks_for(2 * c.g.ny), kBlock, 0, c.stream>>>(c.g.nx, c.g.ny, c.u, c.bc[XPLUS], c.dx, c.P.dt, 1.0, 1.0);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_force(Context &c)
+{
+    IbHost &H = hostside(c);
+    k_force<<<64, kBlock, 0, c.stream>>>(c.g.nx, c.g.ny, H.bb, c.u, c.uold, c.p, c.ib.ghostUV, c.P.nu, c.dx, c.dy,
+                                         c.P.dt, c.ib.forcePart, H.force_arrive, c.ib.forceOut);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_body_motion(Context &c, double)
+{
+    IbHost &H = hostside(c);
+    k_body_motion<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.step_counter_dev, H.table_len,
+                                                                     H.motion_table, c.ib.bdx, c.ib.bx, c.ib.uB,
+                                                                     c.ib.motion);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+void launch_body_pre_step(Context &c)
+{
+    k_body_pre_step<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.ib.uB, c.ib.vB, c.ib.uBk,
+                                                                       c.ib.vBk, c.ib.motion);
+    CUIBM_TRY(cudaGetLastError());
+}
+
 void launch_step_counter(Context &c) { k_step_counter<<<1, 1, 0, c.stream>>>(c.step_counter_dev); }
+
+bool body_moves(Context &c) { return c.has_body && hostside(c).moving; }
+
 }  // namespace cuibm

@@ -154,6 +154,8 @@ struct Context {
     IbArrays ib{};
     bool has_body = false;
     bool ib_dirty = false;
+    int ib_slot = -1;                   // host-side IB bookkeeping of this context
+    double ib_midX = 0, ib_midY = 0;    // body centre used by the tagging
     double cfl_max = 0;
     double forceX = 0, forceY = 0;
 
@@ -224,6 +226,7 @@ void launch_robin(Context &c);
 void launch_force(Context &c);
 void launch_body_motion(Context &c, double t);
 void launch_body_pre_step(Context &c);
+bool body_moves(Context &c);
 void launch_step_counter(Context &c);
 void initialise_body(Context &c);
 

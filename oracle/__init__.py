@@ -461,3 +461,169 @@ def bounding_box(x, y, g, scale):
     _sig("or_bounding_box", INT, _dp, _dp, _dp, _dp, D, _ip, _ip, _ip, _ip)(
         len(x), _d(f64(x)), _d(f64(y)), _d(g.x), _d(g.y), scale, *(ctypes.byref(v) for v in a))
     return tuple(v.value for v in a)
+
+
+class Amg:
+    """Smoothed-aggregation hierarchy of the oracle (oracle/amg.c)."""
+
+    def __init__(self, A, coarse=256):
+        self.A = A
+        fn = _sig("or_sa_build", INT, _ip, _ip, _dp, D, INT, restype=ctypes.c_void_p)
+        self.h = fn(A.n, _i(A.ptr), _i(A.col), _d(A.val), 0.0, coarse)
+
+    def __del__(self):
+        try:
+            _sig("or_sa_free", ctypes.c_void_p)(self.h)
+        except Exception:
+            pass
+
+
+def bicgstab_pc(A, b, x, rtol, maxit, pc, amg=None):
+    """BiCGSTAB with preconditioner kind pc (0 none, 1 diagonal, 2 smoothed aggregation)."""
+    x = f64(x).copy()
+    res = ctypes.c_double()
+    it = _sig("or_bicgstab", INT, _ip, _ip, _dp, _dp, _dp, D, INT, INT, ctypes.c_void_p, _dp, restype=INT)(
+        A.n, _i(A.ptr), _i(A.col), _d(A.val), _d(f64(b)), _d(x), rtol, maxit, pc, amg.h if amg else None,
+        ctypes.byref(res))
+    return x, (it if it >= 0 else -it - 1), it >= 0
+
+
+_PC = {"NONE": 0, "DIAGONAL": 1, "SMOOTHED_AGGREGATION": 2}
+
+
+class LuoSolver:
+    """The external (Luo) ghost-node method on the CPU: luo_base::stepTime
+    (luo_base.cu:208-233) with luoIBM's phases - generateRHS1
+    (luoIBM/intermediateVelocity.cu:128-167), weightUhat, generateRHS2 and
+    weightPressure (luoIBM/intermediatePressure.cu:280-342), the projection of
+    luo_base/projectVelocity.cu:237-279 and the body update (force, motion) of
+    luo_base.cu:255-264.  solve='direct' solves both systems exactly;
+    solve='krylov' uses BiCGSTAB with the case's preconditioners and tolerances."""
+
+    def __init__(self, folder, solve="direct"):
+        sim, flow, dom, bodies = load_case(folder)
+        self.sim = sim[0]
+        g = self.g = Grid(dom)
+        self.nu = float(flow[0]["nu"])
+        self.dt = float(self.sim["dt"])
+        self.bc = [a.copy() for a in boundary_arrays(flow, g.nx, g.ny)]
+        f0 = flow[0]
+        ip = f0.get("initialPerturbation", [0.0, 0.0])
+        self.u = initial_velocity(g, float(f0["initialVelocity"][0]), float(f0["initialVelocity"][1]),
+                                  float(ip[0]), float(ip[1]))
+        self.uhat = self.u.copy()
+        self.uold = np.zeros(g.nUV)
+        self.N = np.zeros(g.nUV)
+        self.p = np.zeros(g.nP)
+        b0 = bodies[0]
+        o = b0["circleOptions"]
+        n = int(o[3])
+        if len(o) > 5 and o[4] in (True, "true"):
+            n = int(2.0 * float(o[2]) * np.pi / float(o[5]))
+            n += n % 2
+        X, Y = circle_points(float(o[0]), float(o[1]), float(o[2]), n)
+        mx = 0.0
+        for v in X:
+            mx += v
+        my = 0.0
+        for v in Y:
+            my += v
+        mx /= n
+        my /= n
+        self.bdx = np.array([v - mx for v in X])
+        self.bb = bounding_box(X, Y, g, float(self.sim.get("scaleCV", 2.0)))
+        self.coef = {k: float(b0.get(k, 0.0)) for k in ("xCoefficient", "uCoefficient", "xPhase", "uPhase",
+                                                         "xfrequency")}
+        self.timeStep = 0
+        xnew, unew = self.motion(0)
+        self.bx = np.array([xnew + v for v in self.bdx])
+        self.by = Y.copy()
+        self.uB = np.full(n, unew)
+        self.vB = np.zeros(n)
+        self.uBk = np.full(n, self.coef["uCoefficient"] * np.cos(
+            2 * np.pi * self.coef["xfrequency"] * (0 - self.dt) + self.coef["uPhase"]))
+        self.midX, self.midY = xnew, my
+        self.T = tag_points(g, self.bx, self.by, self.uB, self.vB, self.bb, self.midX, self.midY)
+        self.u = set_inside(self.u, self.T, self.uB[0], self.vB[0], g)
+        self.A1 = Csr(g.nUV, *lhs1_coo(g, self.dt, self.nu))
+        self.A2 = Csr(g.nP, *lhs2_coo(g, self.dt, centre_pin=False))
+        self.solve = solve
+        self.fx = self.fy = 0.0
+        if solve == "direct":
+            import scipy.sparse.linalg as spla
+            self._lu1 = spla.splu(self.A1.scipy().tocsc())
+            self._lu2 = spla.splu(self.A2.scipy().tocsc())
+        else:
+            ls = {s["system"]: s for s in self.sim.get("linearSolvers", [])}
+            self.cfg = {k: (float(ls[k].get("tolerance", 1e-5)), int(ls[k].get("maxIterations", 10000)),
+                            _PC.get(ls[k].get("preconditioner", "DIAGONAL"), 1)) for k in ("velocity", "Poisson")}
+            self.amg1 = Amg(self.A1) if self.cfg["velocity"][2] == 2 else None
+            self.amg2 = Amg(self.A2) if self.cfg["Poisson"][2] == 2 else None
+        self.iters = (0, 0)
+
+    def motion(self, step):
+        c = self.coef
+        t = self.dt * step
+        return (c["xCoefficient"] * np.sin(2 * np.pi * c["xfrequency"] * t + c["xPhase"]),
+                c["uCoefficient"] * np.cos(2 * np.pi * c["xfrequency"] * t + c["uPhase"]))
+
+    def _solve(self, which, b, x0):
+        if self.solve == "direct":
+            return (self._lu1 if which == 1 else self._lu2).solve(b), 0
+        key = "velocity" if which == 1 else "Poisson"
+        tol, mx, pc = self.cfg[key]
+        A, amg = (self.A1, self.amg1) if which == 1 else (self.A2, self.amg2)
+        x, it, ok = bicgstab_pc(A, b, x0, tol, mx, pc, amg)
+        if not ok:
+            raise RuntimeError("oracle %s solve did not converge" % key)
+        return x, it
+
+    def step(self):
+        g, T, bb, dt = self.g, self.T, self.bb, self.dt
+        xm, xp, ym, yp = self.bc
+        ub, vb = float(self.uB[0]), float(self.vB[0])
+        # _pre_step
+        self.uold = self.u.copy()
+        self.uBk = self.uB.copy()
+        # generateRHS1: Robin outflow, ghost nodes, inside, hybrid nodes, explicit terms
+        xp[:] = robin(self.u, xp, g, dt)
+        u, _ = ghost_velocity(0, self.u, T, ub, g, bb)
+        u, _ = ghost_velocity(1, u, T, vb, g, bb)
+        u = set_inside(u, T, ub, vb, g)
+        ustar = np.zeros(g.nUV)
+        ustar, _ = hybrid_velocity(0, u, ustar, T, ub, g, bb)
+        ustar, _ = hybrid_velocity(1, u, ustar, T, vb, g, bb)
+        bc = (xm, xp, ym, yp)
+        Nold = self.N
+        self.N = generate_N(u, g, bc)
+        L = generate_L(u, g, bc, self.nu)
+        b1 = generate_bc1(u, g, bc, self.nu, dt)
+        rhs1 = generate_rhs(L, Nold, self.N, u, b1, dt)
+        self.uhat, it1 = self._solve(1, rhs1, self.uhat)
+        uh = weight(0, self.uhat, ustar, T, g, bb)
+        uh = weight(1, uh, ustar, T, g, bb)
+        # generateRHS2 and the Poisson solve
+        uh, _ = ghost_velocity(0, uh, T, ub, g, bb)
+        uh, _ = ghost_velocity(1, uh, T, vb, g, bb)
+        self.uhat = uh
+        rhs2 = generate_rhs2(uh, g, bc)
+        self.p, it2 = self._solve(2, rhs2, self.p)
+        dudt = (float(self.uB[0]) - float(self.uBk[0])) / dt
+        dvdt = (float(self.vB[0]) - 0.0) / dt if False else 0.0
+        pstar, _ = hybrid_pressure(self.p, T, dudt, dvdt, g, bb)
+        p = weight(2, self.p, pstar, T, g, bb)
+        p, _ = ghost_pressure(p, T, dudt, dvdt, g, bb)
+        self.p = p
+        # projection, ghost nodes and inside velocity of the new field
+        u, self.uold = project(u, self.uhat, self.p, g, dt)
+        u, _ = ghost_velocity(0, u, T, ub, g, bb)
+        u, _ = ghost_velocity(1, u, T, vb, g, bb)
+        self.u = set_inside(u, T, ub, vb, g)
+        # body update: control-volume force, then the prescribed motion at t = dt * timeStep
+        self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
+        xnew, unew = self.motion(self.timeStep)
+        self.bx = np.array([xnew + v for v in self.bdx])
+        self.uB = np.full(len(self.bx), unew)
+        self.midX = xnew
+        self.iters = (it1, it2)
+        self.timeStep += 1

@@ -1,0 +1,171 @@
+"""GPU parity of the external (Luo) immersed-boundary path against the oracle,
+through the C ABI: tags bit-exact; interpolation stencils (indices bit-exact,
+weights to RTOL_W); interpolated/blended fields to RTOL_KERNEL; whole steps of
+the impulsively started cylinder to 1e-9 relative L2 and forces to 1e-6."""
+import numpy as np
+import pytest
+
+import oracle
+
+cb = pytest.importorskip("cuibm_gb300")
+from cuibm_gb300 import cases  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+RTOL_W = 1e-12       # weights: CUDA acos/sin/tan vs the C library differ in the last bits
+RTOL_KERNEL = 1e-11  # fields built from those weights
+
+
+def rel_max(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def small_cylinder(path, **kw):
+    args = dict(h=0.05, ratio=1.1, extent=3.0, core=0.6, points=48, nu=0.025, dt=0.01, nt=50, vel_tol=1e-12,
+                pois_tol=1e-12, pois_pc="SMOOTHED_AGGREGATION")
+    args.update(kw)
+    return cases.cylinder(path, **args)
+
+
+def geometry(s):
+    g = oracle.Grid.from_arrays(s.get("x"), s.get("dx"), s.get("xu"), s.get("y"), s.get("dy"), s.get("yv"))
+    i = s.info
+    return g, (i.bb_start_i, i.bb_start_j, i.bb_ncx, i.bb_ncy)
+
+
+@pytest.fixture(params=[(48, 0.5, 0.05), (101, 0.43, 0.025)])
+def luo(request, tmp_path):
+    pts, r, h = request.param
+    f = small_cylinder(str(tmp_path / "c"), points=pts, radius=r, h=h)
+    s = cb.NavierStokesSolver(f)
+    s.set_option("write_output", 0)
+    s.initialise()
+    yield s
+    s.close()
+
+
+def oracle_tags(s):
+    g, bb = geometry(s)
+    bx, by = s.get("body_x"), s.get("body_y")
+    midY = sum(float(v) for v in by) / len(by)
+    T = oracle.tag_points(g, bx, by, s.get("body_uB"), s.get("body_vB"), bb, 0.0, midY)
+    return g, bb, T
+
+
+def test_bounding_box_and_body(luo):
+    g, bb = geometry(luo)
+    X = luo.get("body_x")
+    assert bb == oracle.bounding_box(X, luo.get("body_y"), g, 2.0)
+
+
+def test_tags_bit_exact(luo):
+    g, bb, T = oracle_tags(luo)
+    assert np.array_equal(luo.get("ghost_tags_uv"), T.ghostTagsUV)
+    assert np.array_equal(luo.get("hybrid_tags_uv"), T.hybridTagsUV)
+    assert np.array_equal(luo.get("hybrid_tags_uv2"), T.hybridTagsUV2)
+    assert np.array_equal(luo.get("ghost_tags_p"), T.ghostTagsP)
+    assert np.array_equal(luo.get("hybrid_tags_p"), T.hybridTagsP)
+    assert (T.ghostTagsUV > 0).sum() > 20 and (T.ghostTagsUV == 0).sum() > 20
+    for mine, ref in (("dist_node", T.dist_node), ("dist_between", T.dist_between), ("uv_body", T.uv)):
+        assert np.array_equal(luo.get(mine), ref), mine
+    sel = np.nonzero((T.ghostTagsUV > 0) | (T.hybridTagsUV > 0))[0]
+    for mine, ref in (("bi_x", T.bi_x), ("bi_y", T.bi_y), ("ip_x", T.ip_x), ("ip_y", T.ip_y)):
+        assert rel_max(luo.get(mine)[sel], ref[sel]) < 1e-13, mine
+
+
+def test_interpolation_against_oracle(luo):
+    g, bb, T = oracle_tags(luo)
+    rng = np.random.default_rng(7)
+    u = 1.0 + 0.2 * rng.standard_normal(g.nUV)
+    luo.set("u", u)
+    luo.run("ghost_velocity_u")
+    ub, vb = float(luo.get("body_uB")[0]), float(luo.get("body_vB")[0])
+    ug, S0 = oracle.ghost_velocity(0, u, T, ub, g, bb)
+    ug, S1 = oracle.ghost_velocity(1, ug, T, vb, g, bb)
+    assert rel_max(luo.get("u"), ug) < RTOL_KERNEL
+    gi = luo.get("ghost_uv_index").reshape(-1, 4)
+    gc = luo.get("ghost_uv_coef").reshape(-1, 4)
+    sel = np.nonzero(T.ghostTagsUV > 0)[0]
+    for S, part in ((S0, sel[sel < g.nU]), (S1, sel[sel >= g.nU])):
+        assert np.array_equal(gi[part].T, S.index[:, part])
+        assert rel_max(gc[part].T, S.coef[:, part]) < RTOL_W
+    luo.run("hybrid_velocity")
+    us = np.zeros(g.nUV)
+    us, H0 = oracle.hybrid_velocity(0, ug, us, T, ub, g, bb)
+    us, H1 = oracle.hybrid_velocity(1, ug, us, T, vb, g, bb)
+    sel = np.nonzero(T.hybridTagsUV > 0)[0]
+    assert rel_max(luo.get("ustar")[sel], us[sel]) < RTOL_KERNEL
+    hi = luo.get("hybrid_uv_index").reshape(-1, 4)
+    for S, part in ((H0, sel[sel < g.nU]), (H1, sel[sel >= g.nU])):
+        assert np.array_equal(hi[part].T, S.index[:, part])
+    # velocity blend and inside velocity
+    uh = 1.0 + 0.2 * rng.standard_normal(g.nUV)
+    luo.set("uhat", uh)
+    luo.run("weight_uhat")
+    w = oracle.weight(1, oracle.weight(0, uh, us, T, g, bb), us, T, g, bb)
+    assert rel_max(luo.get("uhat"), w) < RTOL_KERNEL
+    luo.run("set_inside")
+    assert rel_max(luo.get("u"), oracle.set_inside(ug, T, ub, vb, g)) < RTOL_KERNEL
+
+
+def test_pressure_interpolation_against_oracle(luo):
+    g, bb, T = oracle_tags(luo)
+    rng = np.random.default_rng(8)
+    p = 0.1 * rng.standard_normal(g.nP)
+    luo.set("p", p)
+    luo.run("weight_pressure")  # hybrid pstar, blend, ghost values
+    dt = luo.info.dt
+    pstar, H = oracle.hybrid_pressure(p, T, 0.0, 0.0, g, bb)
+    pw = oracle.weight(2, p, pstar, T, g, bb)
+    pg, G = oracle.ghost_pressure(pw, T, 0.0, 0.0, g, bb)
+    sel = np.nonzero(T.hybridTagsP > 0)[0]
+    assert rel_max(luo.get("pstar")[sel], pstar[sel]) < RTOL_KERNEL
+    assert rel_max(luo.get("p"), pg) < RTOL_KERNEL
+    gi = luo.get("ghost_p_index").reshape(-1, 4)
+    sel = np.nonzero(T.ghostTagsP > 0)[0]
+    assert np.array_equal(gi[sel].T, G.index[:, sel])
+    assert rel_max(luo.get("ghost_p_coef").reshape(-1, 4)[sel].T, G.coef[:, sel]) < RTOL_W
+    assert dt > 0
+
+
+def test_robin_and_force(luo):
+    g, bb, T = oracle_tags(luo)
+    rng = np.random.default_rng(9)
+    u = 1.0 + 0.1 * rng.standard_normal(g.nUV)
+    uold = u + 0.01 * rng.standard_normal(g.nUV)
+    p = 0.1 * rng.standard_normal(g.nP)
+    xp = luo.get("bc_xplus")
+    luo.set("u", u)
+    luo.set("uold", uold)
+    luo.set("p", p)
+    luo.run("robin_boundary")
+    assert rel_max(luo.get("bc_xplus"), oracle.robin(u, xp, g, luo.info.dt)) < 1e-15
+    luo.run("force")
+    fx, fy = luo.forces()
+    ofx, ofy = oracle.force(u, uold, p, T, luo.info.nu, g, luo.info.dt, bb)
+    assert abs(fx - ofx) <= 1e-10 * max(1.0, abs(ofx)) and abs(fy - ofy) <= 1e-10 * max(1.0, abs(ofy))
+
+
+@pytest.mark.parametrize("graph", [1, 0])
+def test_cylinder_steps_match_oracle(tmp_path, graph):
+    """Impulsively started cylinder, external method: 30 tightly solved steps."""
+    f = small_cylinder(str(tmp_path / "c"), nt=30)
+    ref = oracle.LuoSolver(f, solve="direct")
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.set_option("use_graph", graph)
+        s.initialise()
+        assert np.array_equal(s.get("ghost_tags_uv"), ref.T.ghostTagsUV)
+        forces = []
+        for k in range(30):
+            s.stepTime(1)
+            ref.step()
+            forces.append((s.forces(), (ref.fx, ref.fy)))
+        assert rel_l2(s.get("u"), ref.u) < 1e-9
+        assert rel_l2(s.get("p"), ref.p) < 1e-8
+        for (fx, fy), (ox, oy) in forces:
+            assert abs(2 * fx - 2 * ox) < 1e-6 and abs(2 * fy - 2 * oy) < 1e-6
