@@ -12,8 +12,9 @@ from cuibm_gb300 import cases  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-RTOL_W = 1e-12       # weights: CUDA acos/sin/tan vs the C library differ in the last bits
-RTOL_KERNEL = 1e-11  # fields built from those weights
+RTOL_W = 1e-10       # weights: CUDA acos/sin/tan vs the C library differ in the last bits,
+                     # amplified by the cofactor inverse of the 4x4 bilinear fit
+RTOL_KERNEL = 1e-10  # fields built from those weights
 
 
 def rel_max(a, b):
