@@ -103,6 +103,8 @@ def library():
         L.cuibm_case_error.restype = cp
         L.cuibm_profile_kernel.argtypes = [vp, cp, ip, dp, dp]
         L.cuibm_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.cuibm_cv_force_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, ip, ip, ip, ip, ip, ip, ctypes.c_double,
+                                             ctypes.c_double, vp, vp]
         _lib = L
     return _lib
 

@@ -265,6 +265,13 @@ static int fail(cuibm_ctx *h, int code, const std::string &msg)
 
 static std::string g_create_error;
 
+// error text of the context-free entry points (read back through cuibm_case_error)
+std::string cuibm_noalloc_error_sink(const std::string &msg)
+{
+    g_create_error = msg;
+    return msg;
+}
+
 extern "C" {
 
 int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx **out)

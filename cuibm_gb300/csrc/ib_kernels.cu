@@ -875,11 +875,11 @@ __global__ void k_robin(int nx, int ny, const double *u, double *xp, const doubl
 
 // control-volume force: the six sums of dragLeftRight, dragBottomTop, dragUnsteady,
 // liftLeftRight, liftBottomTop, liftUnsteady in one launch, reduced in a fixed order
-__global__ void k_force(int nx, int ny, const int *bb, const double *u, const double *uold, const double *p,
-                        const int *gtags, double nu, const double *dx, const double *dy, double dt, double *part,
-                        unsigned int *arrive, double *out)
+__device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx, int ncy, const double *u,
+                                           const double *uold, const double *p, const int *gtags, double nu,
+                                           const double *dx, const double *dy, double dt, double *part,
+                                           unsigned int *arrive, double *out)
 {
-    const int I = bb[0], J = bb[1], ncx = bb[2], ncy = bb[3];
     const int nU = (nx - 1) * ny;
     double s[6] = {0, 0, 0, 0, 0, 0};
     const int stride = gridDim.x * blockDim.x;
@@ -949,13 +949,28 @@ __global__ void k_force(int nx, int ny, const int *bb, const double *u, const do
     if (!last) return;
     __threadfence();
     if (threadIdx.x == 0) {
-        double t[6] = {0, 0, 0, 0, 0, 0};
+        double t[6] = {0, 0, 0, 0, 0, 0};  // blocks in order, then the six terms
         for (int b = 0; b < (int)gridDim.x; ++b)
             for (int k = 0; k < 6; ++k) t[k] += __ldcg(part + b * 6 + k);
         out[0] = t[0] + t[1] + t[2];
         out[1] = t[3] + t[4] + t[5];
         *arrive = 0;
     }
+}
+
+__global__ void k_force(int nx, int ny, const int *bb, const double *u, const double *uold, const double *p,
+                        const int *gtags, double nu, const double *dx, const double *dy, double dt, double *part,
+                        unsigned int *arrive, double *out)
+{
+    force_body(nx, ny, bb[0], bb[1], bb[2], bb[3], u, uold, p, gtags, nu, dx, dy, dt, part, arrive, out);
+}
+
+// k_force with the box passed by value (caller-owned arrays, no context)
+__global__ void k_force_box(int nx, int ny, int I, int J, int ncx, int ncy, const double *u, const double *uold,
+                            const double *p, const int *gtags, double nu, const double *dx, const double *dy,
+                            double dt, double *part, unsigned int *arrive, double *out)
+{
+    force_body(nx, ny, I, J, ncx, ncy, u, uold, p, gtags, nu, dx, dy, dt, part, arrive, out);
 }
 
 // prescribed motion (luo_base/move.cu set_movement): x = xnew + offset, uB = unew with
@@ -1284,4 +1299,68 @@ void launch_step_counter(Context &c) { k_step_counter<<<1, 1, 0, c.stream>>>(c.s
 
 bool body_moves(Context &c) { return c.has_body && hostside(c).moving; }
 
+// ---- control-volume force without allocation -------------------------------------
+// The scratch of k_force (6 partial sums per block, then an arrival counter) as a
+// fixed array in the library image: kCvForceMaxBlocks blocks of 256 threads cover
+// (ncx+1)*(ncy+1) <= 262144 box nodes with one node per thread.
+constexpr int kCvForceMaxBlocks = 1024;
+static __device__ __align__(256) double g_cvforce_scratch[6 * kCvForceMaxBlocks + 32];
+
 }  // namespace cuibm
+
+#include <mutex>
+
+namespace {
+std::mutex g_cvforce_mutex;
+double *g_cvforce_ptr[64] = {};
+}  // namespace
+
+extern std::string cuibm_noalloc_error_sink(const std::string &msg);
+
+extern "C" int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p, const int *ghost_tags_uv,
+                                      const double *dx, const double *dy, int nx, int ny, int bb_i, int bb_j,
+                                      int bb_ncx, int bb_ncy, double nu, double dt, double *force_out, void *stream)
+{
+    using namespace cuibm;
+    auto fail = [](int code, const std::string &m) {
+        cuibm_noalloc_error_sink(m);
+        return code;
+    };
+    if (!u || !uold || !p || !ghost_tags_uv || !dx || !dy || !force_out)
+        return fail(1, "cuibm_cv_force_noalloc: null pointer argument");
+    if (nx < 3 || ny < 3 || bb_ncx < 1 || bb_ncy < 1 || bb_i < 1 || bb_j < 1 || bb_i + bb_ncx >= nx ||
+        bb_j + bb_ncy >= ny || !(dt > 0))
+        return fail(1, "cuibm_cv_force_noalloc: box or grid sizes out of range");
+    const long long nodes = (long long)(bb_ncx + 1) * (bb_ncy + 1);
+    if (nodes > (long long)kCvForceMaxBlocks * kBlock)
+        return fail(1, "cuibm_cv_force_noalloc: box of " + std::to_string(nodes) + " nodes exceeds the limit of " +
+                           std::to_string(kCvForceMaxBlocks * kBlock) + " ((ncx+1)*(ncy+1))");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(3, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) return fail(3, "cuibm_cv_force_noalloc: device ordinal beyond 63");
+    double *scratch;
+    {
+        std::lock_guard<std::mutex> lk(g_cvforce_mutex);
+        if (!g_cvforce_ptr[dev]) {
+            void *ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_cvforce_scratch);
+            if (e != cudaSuccess || !ptr)
+                return fail(3, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_cvforce_ptr[dev] = static_cast<double *>(ptr);
+        }
+        scratch = g_cvforce_ptr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned int *arrive = reinterpret_cast<unsigned int *>(scratch + 6 * kCvForceMaxBlocks);
+    // the arrival counter must start at zero (the previous call's last block resets it, but a
+    // call interrupted by an error would not)
+    e = cudaMemsetAsync(arrive, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return fail(3, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+    const int blocks = (int)((nodes + kBlock - 1) / kBlock);
+    k_force_box<<<blocks, kBlock, 0, st>>>(nx, ny, bb_i, bb_j, bb_ncx, bb_ncy, u, uold, p, ghost_tags_uv, nu, dx, dy,
+                                          dt, scratch, arrive, force_out);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(3, std::string("k_force launch: ") + cudaGetErrorString(e));
+    return 0;
+}

@@ -178,6 +178,30 @@ int cuibm_profile_kernel(cuibm_ctx *ctx, const char *kernel, int reps, double *a
  * of iterations it ran. */
 int cuibm_launch_count(cuibm_ctx *ctx, long long *per_step);
 
+/* Control-volume force on the body (drag, lift) from caller-owned device arrays,
+ * for callers that must not allocate GPU memory: a coupling code or host
+ * framework whose own pool has reserved the device memory (a cudaMalloc there
+ * fails or fragments the pool), and a time-stepping loop that cannot take the
+ * device-wide synchronisation that cudaMalloc/cudaFree imply.  This entry
+ * point calls no cudaMalloc, cudaFree or allocating library routine: the
+ * kernel's scratch (its per-block partial sums and arrival counter) is a fixed
+ * array compiled into the library, which every GPU that loads the library
+ * holds until the process exits.  It has no counterpart in the reference.
+ *
+ * Inputs (device pointers of the current device): u and uold (numUV doubles,
+ * velocity at the new and previous step), p (numP), ghost_tags_uv (numUV ints,
+ * -1 marks fluid nodes), dx (nx), dy (ny); the box (bb_i, bb_j, bb_ncx, bb_ncy)
+ * in cell indices; nu and dt.  Output: force_out[0..1] = (Fx, Fy), device
+ * memory.  Limit: (bb_ncx+1)*(bb_ncy+1) <= 262144 box nodes (a 511 x 511 box);
+ * larger boxes are rejected with CUIBM_ERR_BAD_INPUT.  The first call on a
+ * device looks up the scratch address with cudaGetSymbolAddress; make it
+ * before any stream capture.  Every call shares the one scratch array, so
+ * calls that overlap on the GPU (different streams, or different host
+ * threads) race: order them on one stream.  Error text: cuibm_case_error(). */
+int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p, const int *ghost_tags_uv,
+                           const double *dx, const double *dy, int nx, int ny, int bb_i, int bb_j, int bb_ncx,
+                           int bb_ncy, double nu, double dt, double *force_out, void *stream);
+
 /* Host-only (no GPU needed): parse a case folder and build its grid and body
  * exactly as cuibm_create does.  cuibm_case_array copies CUIBM_F_X..CUIBM_F_YV
  * or CUIBM_F_BODY_X/Y into dst (count doubles).  Replaces the reference's
