@@ -36,7 +36,7 @@ _FIELD_NAMES = [
     "dist_node", "dist_between", "uv_body", "ustar", "pstar", "dpdn", "bi_p",
     "ghost_uv_index", "ghost_uv_coef", "hybrid_uv_index", "hybrid_uv_coef",
     "ghost_p_index", "ghost_p_coef", "hybrid_p_index", "hybrid_p_coef",
-    "image_value_uv", "cfl", "work_x", "work_y",
+    "image_value_uv", "cfl", "work_x", "work_y", "solve_trace",
 ]
 FIELDS = {n: i for i, n in enumerate(_FIELD_NAMES)}
 _INT_FIELDS = {"ghost_tags_uv", "hybrid_tags_uv", "hybrid_tags_uv2", "ghost_tags_p", "hybrid_tags_p",
@@ -49,6 +49,12 @@ _OP_NAMES = [
     "set_inside", "robin_boundary", "force", "cfl",
 ]
 OPS = {n: i for i, n in enumerate(_OP_NAMES)}
+
+
+def _field_dtype(name):
+    if name in _INT_FIELDS:
+        return np.int32
+    return np.uint64 if name == "solve_trace" else np.float64
 
 
 class CuibmError(RuntimeError):
@@ -178,7 +184,7 @@ class NavierStokesSolver:
         sizes = {"bc_xminus": 2 * ny - 1, "bc_xplus": 2 * ny - 1, "bc_yminus": 2 * nx - 1, "bc_yplus": 2 * nx - 1,
                  "x": nx, "dx": nx, "xu": nx - 1, "xv": nx, "y": ny, "dy": ny, "yu": ny, "yv": ny - 1,
                  "body_x": nb, "body_y": nb, "body_uB": nb, "body_vB": nb,
-                 "work_x": max(UV, P), "work_y": max(UV, P)}
+                 "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024}
         if name in sizes:
             return sizes[name]
         if name in ("p", "p_old", "rhs2", "ghost_tags_p", "hybrid_tags_p", "bip_x", "bip_y", "ipp_x", "ipp_y",
@@ -191,13 +197,13 @@ class NavierStokesSolver:
         return UV
 
     def get(self, name):
-        dtype = np.int32 if name in _INT_FIELDS else np.float64
+        dtype = _field_dtype(name)
         out = np.empty(self.field_size(name), dtype=dtype)
         self._check(self._L.cuibm_get_field(self._h, FIELDS[name], out.ctypes.data, out.nbytes, 0))
         return out
 
     def set(self, name, values):
-        dtype = np.int32 if name in _INT_FIELDS else np.float64
+        dtype = _field_dtype(name)
         a = np.ascontiguousarray(values, dtype=dtype)
         if a.size != self.field_size(name):
             raise ValueError("%s needs %d values, got %d" % (name, self.field_size(name), a.size))

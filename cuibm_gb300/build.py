@@ -32,6 +32,7 @@ UNITS = {
     "ns_kernels.cu": [],
     "krylov.cu": [],
     "amg.cu": [],
+    "fused_solve.cu": [],
     "ib_kernels.cu": ["-fmad=false"],
 }
 

@@ -18,32 +18,18 @@
 #include <numeric>
 #include <vector>
 
+#include "amg.h"
 #include "operators.cuh"
 #include "solver.h"
 
 namespace cuibm {
 
-constexpr int kCoarse = 256;
+constexpr int kCoarse = 1500;  // dense solve below this size (about 2M FMAs per cycle)
 
 struct HostCsr {
     int n = 0, m = 0;  // rows, cols
     std::vector<int> ptr, col;
     std::vector<double> val;
-};
-
-struct DevCsr {
-    int n = 0;
-    int *ptr = nullptr, *col = nullptr;
-    double *val = nullptr;
-};
-
-struct SaLevel {
-    int n = 0;
-    double omega = 0;
-    DevCsr A, P, R;      // A unused on level 0 (structured operator)
-    double *dinv = nullptr;
-    double *x = nullptr, *b = nullptr, *r = nullptr, *t = nullptr;
-    double *coarse_inv = nullptr;  // dense inverse on the coarsest level
 };
 
 // ---------------------------------------------------------------------------
@@ -248,7 +234,7 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
     std::vector<HostCsr> hostA;
     hostA.push_back(A);
     // host buffers are kept alive until the uploads below have been issued and synchronised
-    std::vector<HostCsr> keepP, keepR;
+    std::vector<HostCsr> keepP, keepR, keepAP;
     std::vector<std::vector<double>> keepD;
     for (int lev = 0; lev < 25; ++lev) {
         const HostCsr &Al = hostA.back();
@@ -314,11 +300,22 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
             P = Pn;
         }
         HostCsr R = transpose(P);
-        HostCsr Ac = multiply(R, multiply(Al, P));
+        HostCsr AP = multiply(Al, P);
+        HostCsr Ac = multiply(R, AP);
         keepP.push_back(P);
         keepR.push_back(R);
+        keepAP.push_back(AP);
         L->P = upload(c, keepP.back());
         L->R = upload(c, keepR.back());
+        L->AP = upload(c, keepAP.back());
+        {
+            std::vector<double> wd(L->n);
+            for (int i = 0; i < L->n; ++i) wd[i] = L->omega * dinv[i];
+            L->wd = c.carve<double>(L->n);
+            keepD.push_back(wd);
+            CUIBM_TRY(cudaMemcpyAsync(L->wd, keepD.back().data(), L->n * sizeof(double), cudaMemcpyHostToDevice,
+                                      c.stream));
+        }
         S.amg.push_back(L);
         hostA.push_back(Ac);
         CUIBM_TRY(cudaStreamSynchronize(c.stream));  // host vectors may be reallocated
@@ -347,6 +344,8 @@ double sa_vcycle_bytes(const LinearSystem &S)
     }
     return b;
 }
+
+int sa_coarsest_size(const LinearSystem &S) { return S.amg.empty() ? 0 : S.amg.back()->n; }
 
 void free_sa_hierarchy(LinearSystem &S)
 {

@@ -1,0 +1,26 @@
+// Device view of the smoothed-aggregation hierarchy (built in amg.cu, cycled by
+// the V-cycle kernels there and by the persistent solver in fused_solve.cu).
+#pragma once
+#include "solver.h"
+
+namespace cuibm {
+
+struct DevCsr {
+    int n = 0;
+    int *ptr = nullptr, *col = nullptr;
+    double *val = nullptr;
+};
+
+struct SaLevel {
+    int n = 0;
+    double omega = 0;
+    DevCsr A, P, R;      // A unused on level 0 (structured operator)
+    double *dinv = nullptr;
+    double *x = nullptr, *b = nullptr, *r = nullptr, *t = nullptr;
+    double *coarse_inv = nullptr;  // dense inverse on the coarsest level
+    // for the persistent cycle (fused_solve.cu), levels with a coarser one:
+    double *wd = nullptr;  // omega * D^-1 (the damped-Jacobi weights)
+    DevCsr AP;             // A_l P_l: the upward sweep's residual without neighbour values
+};
+
+}  // namespace cuibm

@@ -45,6 +45,8 @@ static void alloc_fields(Context &c)
     c.cfl = c.carve<double>(nP);
     c.work_x = c.carve<double>(nUV > nP ? nUV : nP);
     c.work_y = c.carve<double>(nUV > nP ? nUV : nP);
+    c.solve_trace = c.carve<unsigned long long>(2 * kTraceLen);
+    CUIBM_TRY(cudaMemset(c.solve_trace, 0, 2 * kTraceLen * sizeof(unsigned long long)));
     c.bc[XMINUS] = c.carve<double>(2 * ny - 1);
     c.bc[XPLUS] = c.carve<double>(2 * ny - 1);
     c.bc[YMINUS] = c.carve<double>(2 * nx - 1);
@@ -331,6 +333,8 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
         const char *ev = getenv("CUIBM_GRAPH");
         c.use_graph = !(ev && ev[0] == '0');
+        const char *fv = getenv("CUIBM_FUSED");
+        c.fused_solve = !(fv && fv[0] == '0');
         c.created = true;
     } catch (const CudaError &e) {
         g_create_error = e.msg;
@@ -401,6 +405,7 @@ int cuibm_step(cuibm_ctx *h, int nsteps)
                 record_step(c, false);
             c.timeStep++;
         }
+        if (!c.step_sync && nsteps > 0) return CUIBM_OK;  // enqueued only; checked by a later synchronising call
         int errw = 0;
         CUIBM_TRY(cudaMemcpyAsync(&errw, g_err_word_of(c), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
@@ -408,9 +413,13 @@ int cuibm_step(cuibm_ctx *h, int nsteps)
             int sys = errw / 16, st = errw % 16;
             char msg[256];
             snprintf(msg, sizeof msg, "ERROR: Solve for %s failed (%s) by time step %d",
-                     sys == 1 ? "uhat" : "pressure", st == KS_NAN ? "non-finite residual" : "maxIterations reached",
+                     sys == 1 ? "uhat" : "pressure",
+                     st == KS_NAN       ? "non-finite residual"
+                     : st == KS_TIMEOUT ? "a grid barrier of the persistent solver timed out"
+                                        : "maxIterations reached",
                      c.timeStep);
             c.err = msg;
+            if (st == KS_TIMEOUT) return CUIBM_ERR_CUDA;
             return st == KS_NAN ? CUIBM_ERR_NAN : CUIBM_ERR_NOT_CONVERGED;
         }
     });
@@ -585,6 +594,7 @@ int cuibm_run(cuibm_ctx *h, int op)
             int st = read_solve_status(c, op == CUIBM_OP_SOLVE_VELOCITY ? c.sys1 : c.sys2, &it);
             if (st == KS_MAXIT) return fail(h, CUIBM_ERR_NOT_CONVERGED, "linear solve reached maxIterations");
             if (st == KS_NAN) return fail(h, CUIBM_ERR_NAN, "linear solve produced a non-finite residual");
+            if (st == KS_TIMEOUT) return fail(h, CUIBM_ERR_CUDA, "a grid barrier of the persistent solver timed out");
         }
     });
     return CUIBM_OK;
@@ -626,6 +636,20 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
             });
         }
         c.use_graph = want;
+    } else if (k == "fused_solve") {
+        bool want = value != 0;
+        if (want != c.fused_solve) {
+            c.fused_solve = want;
+            if (c.initialised && c.use_graph) CUIBM_GUARD(h, { build_step_graph(c); });
+        }
+    } else if (k == "trace_solve") {
+        c.trace_solve = value != 0;
+        CUIBM_GUARD(h, {
+            set_fused_trace(c, c.sys1, c.trace_solve);
+            set_fused_trace(c, c.sys2, c.trace_solve);
+        });
+    } else if (k == "step_sync") {
+        c.step_sync = value != 0;
     } else if (k == "write_output") c.P.writeOutput = value != 0;
     else return fail(h, CUIBM_ERR_BAD_INPUT, "unknown option " + k);
     return CUIBM_OK;

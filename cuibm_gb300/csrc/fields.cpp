@@ -40,6 +40,7 @@ void *field_pointer(Context &c, int f, size_t *bytes)
     case CUIBM_F_CFL: return ret(c.cfl, P * D);
     case CUIBM_F_WORK_X: return ret(c.work_x, (UV > P ? UV : P) * D);
     case CUIBM_F_WORK_Y: return ret(c.work_y, (UV > P ? UV : P) * D);
+    case CUIBM_F_SOLVE_TRACE: return ret(c.solve_trace, 2 * kTraceLen * sizeof(unsigned long long));
     default: break;
     }
     if (!c.has_body) return nullptr;

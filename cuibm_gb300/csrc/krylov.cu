@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(256) k_cg_3(int n, double *p, const double *__
 {
     if (ks->status != KS_RUNNING) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = z[i] + ks->beta * p[i];
+    if (i < n) p[i] = ks->it == 0 ? z[i] : z[i] + ks->beta * p[i];
 }
 
 // Jacobi of the (possibly symmetrised) operator: dinv = 1 / (w a_ii)
@@ -472,6 +472,7 @@ void setup_system(Context &c, LinearSystem &S)
         k_dinv<<<blocks_for(n), kBlock, 0, c.stream>>>(op2(c, S.w), n, S.dinv);
     CUIBM_TRY(cudaGetLastError());
     if (S.precond == PC_SMOOTHED_AGGREGATION) build_sa_hierarchy(c, S);
+    setup_fused(c, S);
 }
 
 struct SolveLauncher {
@@ -561,6 +562,11 @@ struct SolveLauncher {
 void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool in_graph)
 {
     int *err = c.err_word;
+    if (c.fused_solve && S.fused_fn) {
+        launch_fused_solve(c, S, b, x);
+        S.body_kernels = 0;
+        return;
+    }
     if (in_graph) {
         cudaStreamCaptureStatus st;
         cudaGraph_t graph;
@@ -641,10 +647,12 @@ int read_body_runs(Context &c, LinearSystem &S)
 int read_solve_status(Context &c, LinearSystem &S, int *iterations)
 {
     KrylovScalars host{};
+    FusedSyncState fs{};
     CUIBM_TRY(cudaMemcpyAsync(&host, S.ks, sizeof(host), cudaMemcpyDeviceToHost, c.stream));
+    if (S.fsync) CUIBM_TRY(cudaMemcpyAsync(&fs, S.fsync, sizeof(fs), cudaMemcpyDeviceToHost, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
     if (iterations) *iterations = host.it;
-    return host.status;
+    return fs.abort ? KS_TIMEOUT : host.status;
 }
 
 }  // namespace cuibm

@@ -28,6 +28,7 @@ struct InputError {
 };
 
 constexpr int kBlock = 256;
+constexpr int kTraceLen = 1024;  // timestamps kept per persistent solve (diagnostic trace)
 inline int blocks_for(long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
 
 // ---- structured operators --------------------------------------------------
@@ -67,7 +68,7 @@ struct RhsCoef {
 };
 
 // ---- Krylov state living in device memory -------------------------------------
-enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3 };
+enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3, KS_TIMEOUT = 4 };
 struct KrylovScalars {
     double rho, alpha, omega, beta;
     double bnorm, tol, rnorm, snorm;
@@ -75,6 +76,13 @@ struct KrylovScalars {
     int it, maxit, status, s_done;
     int body_runs, pad1;  // executions of the iteration body in the last solve
     unsigned int arrive;  // last-block-done counter of the fused reductions
+    int pad;
+};
+
+// grid-barrier state of the persistent solver (fused_solve.cu), zeroed before each launch
+struct FusedSyncState {
+    unsigned long long arrivals;
+    int abort;  // set by a block whose barrier wait timed out
     int pad;
 };
 
@@ -96,6 +104,13 @@ struct LinearSystem {
     std::vector<SaLevel *> amg;  // SA hierarchy (Poisson)
     int last_iterations = 0;
     int body_kernels = 0;  // kernel nodes in one captured iteration body
+    // persistent solver (fused_solve.cu); fused_fn is null where it does not apply
+    void *fused_fn = nullptr;
+    int fused_grid = 0;
+    double *p2 = nullptr, *AMp2 = nullptr, *fpartials = nullptr;
+    double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
+    FusedSyncState *fsync = nullptr;
+    void *fargs = nullptr;  // device copy of the solver arguments
 };
 
 struct Timer {
@@ -167,6 +182,11 @@ struct Context {
 
     // CUDA graph of one step
     bool use_graph = true;
+    bool step_sync = true;    // cuibm_step waits for the steps and checks the solves' status;
+                              // when false it only enqueues them (cuibm_step(ctx, 0) then checks)
+    bool fused_solve = true;  // persistent one-launch solves where available
+    bool trace_solve = false; // persistent solves record per-barrier timestamps
+    unsigned long long *solve_trace = nullptr;  // device, 2 x kTraceLen
     cudaGraphExec_t step_exec = nullptr;
     cudaGraph_t step_graph = nullptr;
     int static_kernels = 0;  // kernel nodes of the step graph outside the solver loops
@@ -206,11 +226,17 @@ int read_solve_status(Context &c, LinearSystem &S, int *iterations);
 int read_body_runs(Context &c, LinearSystem &S);
 int count_kernel_nodes(cudaGraph_t g);
 
+// fused_solve.cu
+void setup_fused(Context &c, LinearSystem &S);
+void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x);
+void set_fused_trace(Context &c, LinearSystem &S, bool on);
+
 // amg.cu
 void build_sa_hierarchy(Context &c, LinearSystem &S);
 void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z);
 void free_sa_hierarchy(LinearSystem &S);
 double sa_vcycle_bytes(const LinearSystem &S);
+int sa_coarsest_size(const LinearSystem &S);
 
 // ib_kernels.cu
 void setup_ib(Context &c);

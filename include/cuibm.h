@@ -107,6 +107,9 @@ enum {
     CUIBM_F_CFL,             /* D P  */
     CUIBM_F_WORK_X,          /* D max(UV,P) operator test input  */
     CUIBM_F_WORK_Y,          /* D max(UV,P) operator test output */
+    CUIBM_F_SOLVE_TRACE,     /* uint64 2*1024: per-barrier timestamps (ns) of the last persistent
+                                velocity (first 1024) and Poisson solve: [count, start, ...];
+                                written only while the option "trace_solve" is 1 */
     CUIBM_F_COUNT
 };
 
@@ -164,6 +167,14 @@ int cuibm_get_stream(cuibm_ctx *ctx, void **stream);
  * reference Logger: "Intermediate Velocity Setup", "Intermediate Velocity Solve",
  * "Poisson Setup", "Poisson Solve", "Velocity Projection", "Update Solver", ... */
 int cuibm_get_timer(cuibm_ctx *ctx, const char *name, double *ms, int *count);
+/* Options (no counterpart in the reference): "use_graph" (1: a step is one CUDA
+ * graph launch), "fused_solve" (1: each linear solve is one persistent
+ * cooperative launch; 0: a launch per Krylov/multigrid phase), "profile_phases"
+ * (1: time each phase with events, steps run without the graph), "step_sync"
+ * (1: cuibm_step waits and checks the solves' status; 0: it only enqueues the
+ * steps on the context's stream and a later cuibm_step(ctx, 0) checks),
+ * "trace_solve" (1: record per-barrier timestamps in CUIBM_F_SOLVE_TRACE),
+ * "write_output" (0: no files). */
 int cuibm_set_option(cuibm_ctx *ctx, const char *key, double value);
 
 /* Time one kernel of the step on the context's stream with CUDA events: reps

@@ -151,14 +151,15 @@ def test_robin_and_force(luo):
     assert abs(fx - ofx) <= 1e-10 * max(1.0, abs(ofx)) and abs(fy - ofy) <= 1e-10 * max(1.0, abs(ofy))
 
 
-@pytest.mark.parametrize("graph", [1, 0])
-def test_cylinder_steps_match_oracle(tmp_path, graph):
+@pytest.mark.parametrize("graph,fused", [(1, 1), (0, 1), (1, 0)])
+def test_cylinder_steps_match_oracle(tmp_path, graph, fused):
     """Impulsively started cylinder, external method: 30 tightly solved steps."""
     f = small_cylinder(str(tmp_path / "c"), nt=30)
     ref = oracle.LuoSolver(f, solve="direct")
     with cb.NavierStokesSolver(f) as s:
         s.set_option("write_output", 0)
         s.set_option("use_graph", graph)
+        s.set_option("fused_solve", fused)
         s.initialise()
         assert np.array_equal(s.get("ghost_tags_uv"), ref.T.ghostTagsUV)
         forces = []

@@ -38,8 +38,9 @@ def stretched_case(path, **kw):
                                           kw.get("vel_maxit", 10000), kw.get("pois_maxit", 20000))}
     flow = [{"type": "flow", "nu": 0.02, "initialVelocity": [0.3, -0.1], "initialPerturbation": [0.1, 0.05],
              "boundaryConditions": cases.bcs((1, 0.1), (0.5, -0.2), (0.2, 0.3), (1, -0.1))}]
-    dom = [cases.axis("x", -2.0, 0.1, [(-0.5, 1.1), (0.5, 1.0), (2.5, 1.08)]),
-           cases.axis("y", -1.5, 0.1, [(-0.4, 1.12), (0.4, 1.0), (1.6, 1.1)])]
+    h = kw.get("h", 0.1)
+    dom = [cases.axis("x", -2.0, h, [(-0.5, 1.1), (0.5, 1.0), (2.5, 1.08)]),
+           cases.axis("y", -1.5, h, [(-0.4, 1.12), (0.4, 1.0), (1.6, 1.1)])]
     return cases.write_case(path, [sim], flow, dom, [])
 
 
@@ -133,13 +134,20 @@ def test_rhs2_and_projection(solver):
     assert np.array_equal(solver.get("uold"), uo)
 
 
+@pytest.mark.parametrize("fused", [1, 0])
 @pytest.mark.parametrize("pc,krylov", [("DIAGONAL", None), ("DIAGONAL", "CG"), ("SMOOTHED_AGGREGATION", None),
-                                       ("SMOOTHED_AGGREGATION", "CG"), ("NONE", None)])
-def test_solves_converge_to_direct_solution(tmp_path, pc, krylov):
+                                       ("SMOOTHED_AGGREGATION", "CG"), ("NONE", None), ("NONE", "CG")])
+def test_solves_converge_to_direct_solution(tmp_path, pc, krylov, fused):
+    """Both solve paths - one persistent launch (fused) and a launch per phase -
+    for every Krylov method and preconditioner."""
+    # smoothed aggregation on a grid large enough for a multilevel hierarchy (the
+    # coarsest level is solved densely below 1500 unknowns)
+    h = 0.03 if pc == "SMOOTHED_AGGREGATION" else 0.1
     f = stretched_case(str(tmp_path / "c"), vel_pc=pc, pois_pc=pc, vel_krylov=krylov, pois_krylov=krylov,
-                       vel_tol=1e-12, pois_tol=1e-12)
+                       vel_tol=1e-12, pois_tol=1e-12, h=h)
     with cb.NavierStokesSolver(f) as s:
         s.set_option("write_output", 0)
+        s.set_option("fused_solve", fused)
         s.initialise()
         g = grid_from(s)
         rng = np.random.default_rng(4)
@@ -157,7 +165,8 @@ def test_solves_converge_to_direct_solution(tmp_path, pc, krylov):
         x2 = oracle.direct_solve(A2, b2)
         assert rel_l2(s.get("p"), x2) < 1e-8
         it1, it2 = s.iterations()
-        assert it1 > 0 and it2 > 0
+        # BiCGSTAB that converges on the half step of its first iteration counts 0 (cusp::monitor)
+        assert it1 >= 0 and it2 >= 0 and it1 + it2 > 0
         # the residual criterion of the reference: ||b - Ax|| <= tol ||b||
         assert np.linalg.norm(b2 - A2.matvec(s.get("p"))) <= 1e-12 * np.linalg.norm(b2) * 1.0001
 
@@ -173,8 +182,8 @@ def test_non_convergence_is_reported_not_fatal(tmp_path):
         assert s.get("u").shape[0] == s.info.numUV  # context still usable
 
 
-@pytest.mark.parametrize("graph", [1, 0])
-def test_cavity_steps_match_oracle(tmp_path, graph):
+@pytest.mark.parametrize("graph,fused", [(1, 1), (0, 1), (1, 0)])
+def test_cavity_steps_match_oracle(tmp_path, graph, fused):
     """Lid-driven cavity (plain method), 40 steps, tight solves: fields within 1e-9."""
     f = cases.cavity(str(tmp_path / "cav"), n=32, nu=0.01, dt=0.01, nt=40, vel_tol=1e-13, pois_tol=1e-13,
                      pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG")
@@ -182,6 +191,7 @@ def test_cavity_steps_match_oracle(tmp_path, graph):
     with cb.NavierStokesSolver(f) as s:
         s.set_option("write_output", 0)
         s.set_option("use_graph", graph)
+        s.set_option("fused_solve", fused)
         s.initialise()
         for k in range(40):
             ref.step()
@@ -191,3 +201,31 @@ def test_cavity_steps_match_oracle(tmp_path, graph):
         assert rel_l2(s.get("uhat"), ref.uhat) < FIELD_L2
         assert rel_l2(s.get("p"), ref.p) < FIELD_L2 * 10
         assert rel_l2(s.get("N"), ref.N) < FIELD_L2
+
+
+def test_fused_and_stepwise_solves_agree(tmp_path):
+    """The persistent solver runs the same recurrences as the per-phase kernels:
+    same iteration counts, solutions equal to rounding (the dot products are
+    summed over a different number of blocks)."""
+    f = stretched_case(str(tmp_path / "c"), vel_pc="DIAGONAL", pois_pc="SMOOTHED_AGGREGATION", vel_tol=1e-10,
+                       pois_tol=1e-10, h=0.03)
+    out = []
+    for fused in (1, 0):
+        with cb.NavierStokesSolver(f) as s:
+            s.set_option("write_output", 0)
+            s.set_option("fused_solve", fused)
+            s.initialise()
+            g = grid_from(s)
+            b1 = np.random.default_rng(11).standard_normal(g.nUV)
+            b2 = np.random.default_rng(12).standard_normal(g.nP)
+            s.set("rhs1", b1)
+            s.set("uhat", np.zeros(g.nUV))
+            s.run("solve_velocity")
+            s.set("rhs2", b2)
+            s.set("p", np.zeros(g.nP))
+            s.run("solve_poisson")
+            assert s.info.amg_levels >= 2
+            out.append((s.get("uhat"), s.get("p"), s.iterations()))
+    (u1, p1, it1), (u0, p0, it0) = out
+    assert it1 == it0
+    assert rel_l2(u1, u0) < 1e-12 and rel_l2(p1, p0) < 1e-9
