@@ -36,14 +36,21 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-steps/s"
 
 
+# Krylov method of both solves in the cylinder workload: BICGSTAB, the
+# reference's; CG (on the symmetrised operators, same stopping rule) for study -
+# on this stretched grid it needs about three times as many V-cycles.
+KRYLOV = os.environ.get("CUIBM_BENCH_KRYLOV", "BICGSTAB")
+
+
 def make_case(workload, folder, tight=False):
     from cuibm_gb300 import cases
     if workload == "cavity64":
         return cases.cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000000, vel_tol=1e-8, pois_tol=1e-8,
                             pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG"), 64 * 64
     if workload == "cylinder_re40":
+        k = KRYLOV
         f = cases.cylinder(folder, h=0.02, ratio=1.03, points=157, nu=1.0 / 40, dt=0.01, nt=1000000,
-                           vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION")
+                           vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k)
         return f, 270 * 270
     raise SystemExit("unknown workload " + workload)
 
@@ -54,7 +61,7 @@ def workload_config(workload):
                 "velocity": "BiCGSTAB + diagonal, rtol 1e-8", "poisson": "CG + smoothed aggregation, rtol 1e-8"}
     return {"workload": "impulsively started cylinder Re 40, external (Luo) ghost-node method, plain FP64",
             "nx": 270, "ny": 270, "body_points": 157, "dt": 0.01,
-            "velocity": "BiCGSTAB + diagonal, rtol 1e-5", "poisson": "BiCGSTAB + smoothed aggregation, rtol 1e-5"}
+            "velocity": KRYLOV + " + diagonal, rtol 1e-5", "poisson": KRYLOV + " + smoothed aggregation, rtol 1e-5"}
 
 
 class ClockSampler:
@@ -146,24 +153,33 @@ def barrier(pg):
         pg.barrier()
 
 
-def run_ours(a, rank, world, local, pg):
-    import numpy as np
-    import torch
-
+def new_solver(a, local):
     import cuibm_gb300 as cb
-
-    torch.cuda.set_device(local)
     tmp = tempfile.mkdtemp(prefix="cuibm_bench_")
     folder, cells = make_case(a.workload, os.path.join(tmp, "case"))
     s = cb.NavierStokesSolver(folder, ["-deviceNumber", str(local)])
     s.set_option("write_output", 0)
     s.initialise()
+    return s, cells
+
+
+def run_ours(a, rank, world, local, pg):
+    import torch
+
+    import cuibm_gb300 as cb
+
+    torch.cuda.set_device(local)
+    s, cells = new_solver(a, local)
     stream = torch.cuda.ExternalStream(s.stream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     s.stepTime(a.warmup)
     torch.cuda.synchronize()
     barrier(pg)
+    # Timed: steps warmup+1 .. warmup+steps of the run.  Each step is one graph
+    # launch enqueued without waiting (step_sync 0) after an L2 flush on the same
+    # stream; events bracket the step alone.  The solves' status is checked after.
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    s.set_option("step_sync", 0)
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         barrier(pg)
@@ -171,50 +187,59 @@ def run_ours(a, rank, world, local, pg):
         for k in range(a.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
-                evs[k][0].record(stream)
+            evs[k][0].record(stream)
             s.stepTime(1)
             evs[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+    s.set_option("step_sync", 1)
+    s.stepTime(0)  # raises if a solve failed
     barrier(pg)
     dev_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
     dev_ms = reduce_max(pg, dev_ms)
     ms_per_step = dev_ms / a.steps
     value = world * cells * a.steps / (dev_ms * 1e-3) / 1e6
     it1, it2 = s.iterations()
+    fx, fy = s.forces()
+    try:
+        launches = s.launch_count()
+    except cb.CuibmError:
+        launches = None  # graphs disabled (profiling runs): no per-node count
 
-    # roofline: the dominant kernel, timed with CUDA events on the solver's stream
+    # roofline: the dominant kernel (the Poisson solve, one persistent launch) and the
+    # others, each timed with CUDA events on the solver's stream
     peak, peak_kind = measured_peaks()
-    roof = {}
-    cand = ["rhs1", "apply_lhs2", "apply_lhs1", "rhs2", "project"]
-    if s.info.amg_levels > 0:
-        cand.append("poisson_vcycle")
+    cand = ["poisson_solve", "velocity_solve", "rhs1", "rhs2", "project"]
     prof = {}
     for k in cand:
-        ms, b = s.profile_kernel(k, reps=50)
-        prof[k] = (ms, b)
-    dom = a.roofline_kernel if a.roofline_kernel in prof else "rhs1"
-    ms, b = prof[dom]
+        ms, b = s.profile_kernel(k, reps=10 if k.endswith("solve") else 50)
+        prof[k] = (ms, b, s.iterations()[1 if k == "poisson_solve" else 0] if k.endswith("solve") else None)
+    dom = a.roofline_kernel if a.roofline_kernel in prof else "poisson_solve"
+    ms, b, its = prof[dom]
     achieved = b / (ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
-            "bytes_per_launch": b, "ms_per_launch": ms,
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+            "traffic": profiled_traffic(dom), "bytes_per_launch": b, "ms_per_launch": round(ms, 5),
+            "iterations_per_launch": its,
             "other_kernels": {k: {"ms": round(v[0], 5), "GB/s": round(v[1] / (v[0] * 1e-3) / 1e9, 1)}
                               for k, v in prof.items()}}
+    s.close()
 
-    # end to end through the public API with host buffers: every step uploads the
-    # step's boundary inputs from pinned memory and reads back the fields and forces
+    # end to end through the public API with host buffers, on a fresh instance over
+    # the same steps: every step uploads the step's boundary inputs from pinned memory
+    # and reads back the velocity, pressure and forces
+    s, _ = new_solver(a, local)
+    s.stepTime(a.warmup)
     bnames = ["bc_xminus", "bc_xplus", "bc_yminus", "bc_yplus"]
     pinned_in = {n: torch.from_numpy(s.get(n)).pin_memory() for n in bnames}
     out_u = torch.empty(s.info.numUV, dtype=torch.float64).pin_memory()
     out_p = torch.empty(s.info.numP, dtype=torch.float64).pin_memory()
     h2d = sum(t.numel() * 8 for t in pinned_in.values())
     d2h = (out_u.numel() + out_p.numel()) * 8 + 16
-    e2e_steps = max(3, a.steps)
     torch.cuda.synchronize()
     barrier(pg)
     t0 = time.perf_counter()
-    for k in range(e2e_steps):
+    for k in range(a.steps):
         for n, t in pinned_in.items():
             s._check(s._L.cuibm_set_field(s._h, cb.FIELDS[n], t.data_ptr(), t.numel() * 8, 0))
         s.stepTime(1)
@@ -223,19 +248,36 @@ def run_ours(a, rank, world, local, pg):
         s.forces()
     torch.cuda.synchronize()
     e2e_s = reduce_max(pg, time.perf_counter() - t0)
-    e2e = {"value": round(world * cells * e2e_steps / e2e_s / 1e6, 3), "unit": METRIC,
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-    try:
-        launches = s.launch_count()
-    except cb.CuibmError:
-        launches = None  # graphs disabled (profiling runs): no per-node count
     s.close()
+    e2e = {"value": round(world * cells * a.steps / e2e_s / 1e6, 3), "unit": METRIC,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     return {"value": value, "ms_per_step": ms_per_step, "wall_s": wall, "roofline": roof, "e2e": e2e,
-            "clocks": clk.summary(), "iterations_last_step": [it1, it2], "gpu_launches": launches * a.steps if launches is not None else None}
+            "clocks": clk.summary(), "iterations_last_step": [it1, it2], "drag_lift_last_step": [2 * fx, 2 * fy],
+            "gpu_launches": launches * a.steps if launches is not None else None}
 
 
-def cpu_baseline(workload, budget_s=15.0):
-    """The oracle port on the host cores, for a bounded number of steps."""
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of the kernel from the committed ncu summary
+    (profiles/*.md, a line 'dram_bytes_per_launch <kernel> <bytes>'); None where
+    there is none."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    d = os.path.join(here, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(d, fn)):
+            f = line.strip().strip("`").split()
+            if len(f) == 3 and f[0] == "dram_bytes_per_launch" and f[1] == kernel:
+                return int(f[2])
+    return None
+
+
+def cpu_baseline(workload, budget_s=15.0, warmup=1, max_steps=200):
+    """The oracle port on the host cores (the reference's algorithm: BiCGSTAB with
+    the case's preconditioners), timed over up to max_steps steps after warmup
+    untimed ones, stopping early after budget_s seconds."""
     import oracle
     tmp = tempfile.mkdtemp(prefix="cuibm_cpu_")
     folder, cells = make_case(workload, os.path.join(tmp, "case"))
@@ -244,28 +286,32 @@ def cpu_baseline(workload, budget_s=15.0):
     if workload == "cavity64":
         solver = oracle.PlainSolver(folder, solve="krylov")
     else:
-        solver = oracle.LuoSolver(folder)
-    solver.step()  # warm-up (setup)
+        solver = oracle.LuoSolver(folder, solve="krylov")
+    for _ in range(max(1, warmup)):
+        solver.step()
     steps, t0 = 0, time.perf_counter()
-    while True:
+    while steps < max_steps:
         solver.step()
         steps += 1
         el = time.perf_counter() - t0
-        if el > budget_s or steps >= 200:
+        if el > budget_s:
             break
+    el = time.perf_counter() - t0
     value = cells * steps / el / 1e6
     return {"value": round(value, 4), "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": "%d steps of the same workload after one warm-up step (%.1f s)" % (steps, el)}
+            "sample": "steps %d-%d of the workload (%d timed, %.1f s, BiCGSTAB as configured)"
+                      % (max(1, warmup) + 1, max(1, warmup) + steps, steps, el), "steps_timed": steps}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    # default: the whole 2000-step cylinder run (3 warm-up steps, 1997 timed)
+    ap.add_argument("--steps", type=int, default=1997)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("CUIBM_BENCH_WORKLOAD", "cylinder_re40"))
-    ap.add_argument("--roofline-kernel", default="rhs1")
+    ap.add_argument("--roofline-kernel", default="poisson_solve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
@@ -276,7 +322,8 @@ def main():
     if a.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(a.workload, budget_s=max(10.0, 2.0 * a.steps))
+        # the same steps as the GPU arm times (warm-up, then K), on all host cores
+        cb = cpu_baseline(a.workload, budget_s=240.0, warmup=a.warmup, max_steps=a.steps)
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": a.gpus,
                 "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "dtype": "f64",
                 "data": "synthetic", "config": cfg, "cpu_baseline": cb,
@@ -290,7 +337,8 @@ def main():
             "warmup": a.warmup, "ms_per_step": round(r["ms_per_step"], 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "roofline": r["roofline"], "e2e": r["e2e"], "clocks": r["clocks"],
-            "gpu_launches": r["gpu_launches"], "iterations_last_step": r["iterations_last_step"]}
+            "gpu_launches": r["gpu_launches"], "iterations_last_step": r["iterations_last_step"],
+            "drag_lift_last_step": r["drag_lift_last_step"]}
     if not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(a.workload)
     print(json.dumps(line))

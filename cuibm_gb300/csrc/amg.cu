@@ -209,6 +209,7 @@ static DevCsr upload(Context &c, const HostCsr &H)
 {
     DevCsr D;
     D.n = H.n;
+    D.nnz = (int)H.col.size();
     D.ptr = c.carve<int>(H.ptr.size());
     D.col = c.carve<int>(std::max<size_t>(1, H.col.size()));
     D.val = c.carve<double>(std::max<size_t>(1, H.val.size()));

@@ -6,7 +6,7 @@
 namespace cuibm {
 
 struct DevCsr {
-    int n = 0;
+    int n = 0, nnz = 0;
     int *ptr = nullptr, *col = nullptr;
     double *val = nullptr;
 };

@@ -681,6 +681,29 @@ int cuibm_profile_kernel(cuibm_ctx *h, const char *kernel, int reps, double *avg
         } else if (k == "apply_lhs2") {
             launch = [&] { launch_apply(c, 2, c.work_x, c.work_y); };
             b = 2 * P * D;
+        } else if (k == "poisson_solve" || k == "velocity_solve") {
+            // the last step's solve again (same right-hand side, same starting guess: the
+            // field before the step), each repetition timed alone
+            LinearSystem &S = k == "poisson_solve" ? c.sys2 : c.sys1;
+            const double *rhs = S.which == 1 ? c.rhs1 : c.rhs2;
+            const double *x0 = S.which == 1 ? c.uold : c.p_old;
+            double total = 0;
+            for (int r = 0; r <= reps; ++r) {
+                launch_copy(c, c.work_x, x0, S.n);
+                CUIBM_TRY(cudaEventRecord(c.ev0, c.stream));
+                launch_solve(c, S, rhs, c.work_x, false);
+                CUIBM_TRY(cudaEventRecord(c.ev1, c.stream));
+                CUIBM_TRY(cudaEventSynchronize(c.ev1));
+                float ms = 0;
+                CUIBM_TRY(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+                if (r > 0) total += ms;
+            }
+            int it = 0;
+            if (read_solve_status(c, S, &it) != KS_CONVERGED)
+                return fail(h, CUIBM_ERR_NOT_CONVERGED, "profiled solve did not converge");
+            if (avg_ms) *avg_ms = total / reps;
+            if (bytes) *bytes = solve_bytes(S, it);
+            return CUIBM_OK;
         } else if (k == "poisson_vcycle") {
             if (c.sys2.amg.empty()) return fail(h, CUIBM_ERR_BAD_INPUT, "the Poisson system has no SA hierarchy");
             launch = [&] { launch_vcycle(c, c.sys2, c.work_x, c.work_y); };

@@ -991,6 +991,44 @@ void set_fused_trace(Context &c, LinearSystem &S, bool on)
     if (S.fused_fn) upload_fargs(c, S);
 }
 
+// Algorithmic bytes of one solve of `it` iterations as the persistent kernel
+// does it: 8 bytes per vector value each phase reads or writes (every vector
+// once per phase), 12 per matrix entry (value and column) and 4 per row pointer.
+// Used to report achieved bandwidth; the phases are latency- and FP64-issue-
+// bound, so this is a floor on traffic, not the bound.
+double solve_bytes(const LinearSystem &S, int it)
+{
+    const double n = S.n, D = 8;
+    auto csr = [](const DevCsr &M) { return 12.0 * M.nnz + 4.0 * (M.n + 1); };
+    double vc = 0;  // one V-cycle without its first sweep's vector reads
+    const int L = (int)S.amg.size();
+    if (L == 1) {
+        vc = D * (double)S.amg[0]->n * S.amg[0]->n + 2 * D * S.amg[0]->n;
+    } else if (L > 1) {
+        vc += 2 * D * n;  // first sweep: omega D^-1 and r_0 (its input is counted by the caller)
+        for (int l = 0; l < L - 1; ++l) {
+            const SaLevel *V = S.amg[l], *C = S.amg[l + 1];
+            if (l > 0) vc += 3 * D * V->n + csr(V->A);
+            vc += D * V->n + csr(V->R) + D * C->n;                           // restriction
+            vc += 4 * D * V->n + csr(V->P) + csr(V->AP) + D * C->n;          // prolongation and sweep
+        }
+        const double nc = S.amg[L - 1]->n;
+        vc += D * nc * nc + 2 * D * nc;
+    }
+    double per_it, init;
+    if (S.krylov == KRYLOV_CG) {
+        init = 6 * D * n + (S.precond == PC_SMOOTHED_AGGREGATION ? vc + D * n : 0);
+        per_it = 6 * D * n + 7 * D * n + (S.precond == PC_SMOOTHED_AGGREGATION ? vc : 2 * D * n);
+    } else {
+        init = 6 * D * n;
+        if (S.precond == PC_SMOOTHED_AGGREGATION)
+            per_it = 7 * D * n + 4 * D * n + 6 * D * n + 4 * D * n + 8 * D * n + 2 * vc;
+        else
+            per_it = 9 * D * n + 7 * D * n + 8 * D * n;
+    }
+    return init + it * per_it;
+}
+
 // Decide whether the system can use the persistent solver, size its grid (one
 // block per SM unless CUIBM_FUSED_BLOCKS_PER_SM asks for more and the kernel's
 // registers allow it) and build its tables.

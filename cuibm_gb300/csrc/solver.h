@@ -230,6 +230,7 @@ int count_kernel_nodes(cudaGraph_t g);
 void setup_fused(Context &c, LinearSystem &S);
 void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x);
 void set_fused_trace(Context &c, LinearSystem &S, bool on);
+double solve_bytes(const LinearSystem &S, int iterations);
 
 // amg.cu
 void build_sa_hierarchy(Context &c, LinearSystem &S);
