@@ -133,12 +133,8 @@ static bool is_luo(const Context &c) { return c.P.solverType == ST_LUO && c.has_
 static void phase_generate_rhs1(Context &c)
 {
     PhaseTimer t(c, "Intermediate Velocity Setup");
-    if (is_luo(c)) {
-        launch_robin(c);                    // updateRobinBoundary
-        launch_ghost_velocity(c, c.u, true);  // rhs1GNInterpolation
-        launch_set_inside(c, c.u);          // zeroVelocity
-        launch_hybrid_velocity(c, c.u);     // rhs1HNInterpolation
-    }
+    // updateRobinBoundary, rhs1GNInterpolation, zeroVelocity, rhs1HNInterpolation
+    if (is_luo(c)) launch_ib_rhs1(c);
     launch_rhs1(c, false);
 }
 
@@ -151,7 +147,6 @@ static void phase_solve_velocity(Context &c, bool in_graph)
 static void phase_generate_rhs2(Context &c)
 {
     PhaseTimer t(c, "Poisson Setup");
-    if (is_luo(c)) launch_ghost_velocity(c, c.uhat, true);  // preRHS2Interpolation
     launch_rhs2(c, c.uhat);
 }
 
@@ -165,10 +160,7 @@ static void phase_project(Context &c)
 {
     PhaseTimer t(c, "Velocity Projection");
     launch_project(c);
-    if (is_luo(c)) {
-        launch_ghost_velocity(c, c.u, true);
-        launch_set_inside(c, c.u);
-    }
+    if (is_luo(c)) launch_ib_after_projection(c);  // ghost u, zeroVelocity
 }
 
 static void phase_update_body(Context &c)
@@ -200,15 +192,13 @@ static void record_step(Context &c, bool in_graph)
     phase_solve_velocity(c, in_graph);
     if (is_luo(c)) {
         PhaseTimer t(c, "Intermediate Velocity Weight");
-        launch_weight_uhat(c);
+        launch_ib_after_velocity(c);  // weightUhat, preRHS2Interpolation
     }
     phase_generate_rhs2(c);
     phase_solve_poisson(c, in_graph);
     if (is_luo(c)) {
         PhaseTimer t(c, "Poisson Weight");
-        launch_hybrid_pressure(c);
-        launch_weight_pressure(c);
-        launch_ghost_pressure(c, true);
+        launch_ib_after_poisson(c);  // hybrid pressure, weightPressure, ghost pressure
     }
     phase_project(c);
     phase_update_body(c);    // motion reads the step counter before it advances
@@ -561,14 +551,15 @@ int cuibm_run(cuibm_ctx *h, int op)
         case CUIBM_OP_GENERATE_RHS1: phase_generate_rhs1(c); break;
         case CUIBM_OP_SOLVE_VELOCITY: phase_solve_velocity(c, false); break;
         case CUIBM_OP_WEIGHT_UHAT: need_ib(); launch_weight_uhat(c); break;
-        case CUIBM_OP_GENERATE_RHS2: phase_generate_rhs2(c); break;
+        case CUIBM_OP_GENERATE_RHS2:  // preRHS2Interpolation, then the right-hand side
+            if (is_luo(c)) launch_ghost_velocity(c, c.uhat, true);
+            phase_generate_rhs2(c);
+            break;
         case CUIBM_OP_RHS2: launch_rhs2(c, c.uhat); break;
         case CUIBM_OP_SOLVE_POISSON: phase_solve_poisson(c, false); break;
         case CUIBM_OP_WEIGHT_PRESSURE:
             need_ib();
-            launch_hybrid_pressure(c);
-            launch_weight_pressure(c);
-            launch_ghost_pressure(c, true);
+            launch_ib_after_poisson(c);
             break;
         case CUIBM_OP_PROJECT: launch_project(c); break;
         case CUIBM_OP_PROJECT_VELOCITY: phase_project(c); break;

@@ -23,6 +23,7 @@
 //  * ghost interpolation stages the new values and applies them in a second
 //    launch, so every node reads the field as it was before (what the
 //    reference's GPU launch does: all loads precede all stores).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -546,282 +547,133 @@ struct BoxLaunch {
     int i0, j0, width, nthreads;
 };
 
-// ghost-node velocity (interpolateVelocityToGhostNodeX/Y): image-point value into
-// imageValue and the new ghost value into staging; blockIdx.y selects u (0) or v (1)
-__global__ void k_ghost_velocity(BoxLaunch B, int nx, int ny, const double *__restrict__ u, const int *gtags,
-                                 const double *xu, const double *yu, const double *xv, const double *yv,
-                                 const double *uB, const double *vB, const double *bix, const double *biy,
-                                 const double *ipx, const double *ipy, int *idx4, double *coef4, double *imageValue,
-                                 double *staging)
-{
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B.nthreads) return;
-    const int dir = blockIdx.y, nU = (nx - 1) * ny;
-    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
-    int n;
-    const double *xc, *yc;
-    double ub;
-    if (dir == 0) {
-        n = J * (nx - 1) + I;
-        if (n >= nU) return;
-        xc = xu; yc = yu; ub = uB[0];
-    } else {
-        if (J * nx + I > nx * (ny - 1)) return;
-        n = J * nx + I + nU;
-        xc = xv; yc = yv; ub = vB[0];
-    }
-    if (gtags[n] <= 0) return;
-    int ii = I - 5, jj = J - 5;
-    while (xc[ii] < ipx[n]) ii++;
-    while (yc[jj] < ipy[n]) jj++;
-    double x[4] = {xc[ii - 1], xc[ii], xc[ii - 1], xc[ii]};
-    double y[4] = {yc[jj - 1], yc[jj - 1], yc[jj], yc[jj]};
-    int id[4];
-    if (dir == 0) {
-        id[0] = (jj - 1) * (nx - 1) + ii - 1; id[1] = id[0] + 1;
-        id[2] = jj * (nx - 1) + ii - 1;       id[3] = id[2] + 1;
-    } else {
-        id[0] = (jj - 1) * nx + ii - 1 + nU; id[1] = id[0] + 1;
-        id[2] = jj * nx + ii - 1 + nU;       id[3] = id[2] + 1;
-    }
-    double q[4] = {u[id[0]], u[id[1]], u[id[2]], u[id[3]]};
-    double mn = 1.0;
-    int close = -1;
-    bool inflag = false;
-    for (int l = 0; l < 4; ++l) {
-        double ex = x[l] - bix[n], ey = y[l] - biy[n];
-        double s = sqrt(ex * ex + ey * ey);
-        if (s < mn) { mn = s; close = id[l]; }
-        if (gtags[id[l]] > 0) inflag = true;
-    }
-    for (int l = 0; l < 4; ++l) {
-        if (gtags[id[l]] == n) { x[l] = bix[id[l]]; y[l] = biy[id[l]]; q[l] = ub; }
-        else if (id[l] == close && !inflag) { x[l] = bix[n]; y[l] = biy[n]; q[l] = ub; }
-    }
-    double a[16], b[16], det;
-    rows_dev(x, y, a);
-    inverse4_dev(a, b, &det);
-    const double a0 = b[0] / det * q[0] + b[1] / det * q[1] + b[2] / det * q[2] + b[3] / det * q[3];
-    const double a1 = b[4] / det * q[0] + b[5] / det * q[1] + b[6] / det * q[2] + b[7] / det * q[3];
-    const double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
-    const double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
-    store_dev(idx4, coef4, n, id, b, det, ipx[n], ipy[n]);
-    const double val = a0 + a1 * ipx[n] + a2 * ipy[n] + a3 * ipx[n] * ipy[n];
-    imageValue[n] = val;
-    staging[n] = 2 * ub - val;
-}
-
-// apply the staged ghost values (second half of the snapshot update)
-__global__ void k_apply_ghost(BoxLaunch B, int nx, int ny, const int *gtags, const double *staging, double *u)
-{
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B.nthreads) return;
-    const int dir = blockIdx.y, nU = (nx - 1) * ny;
-    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
-    int n;
-    if (dir == 0) {
-        n = J * (nx - 1) + I;
-        if (n >= nU) return;
-    } else {
-        if (J * nx + I > nx * (ny - 1)) return;
-        n = J * nx + I + nU;
-    }
-    if (gtags[n] > 0) u[n] = staging[n];
-}
-
-// hybrid-node velocity (interpolateVelocityToHybridNodeX/Y) into ustar
-__global__ void k_hybrid_velocity(BoxLaunch B, int nx, int ny, const double *__restrict__ u, const int *htags,
-                                  const double *xu, const double *yu, const double *xv, const double *yv,
-                                  const double *uB, const double *vB, const double *bix, const double *biy,
-                                  const double *ipx, const double *ipy, int *idx4, double *coef4,
-                                  double *imageValue, double *ustar)
-{
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B.nthreads) return;
-    const int dir = blockIdx.y, nU = (nx - 1) * ny;
-    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
-    int n;
-    const double *xc, *yc;
-    double ub;
-    if (dir == 0) {
-        n = J * (nx - 1) + I;
-        if (n >= nU) return;
-        xc = xu; yc = yu; ub = uB[0];
-    } else {
-        if (J * nx + I > nx * (ny - 1)) return;
-        n = J * nx + I + nU;
-        xc = xv; yc = yv; ub = vB[0];
-    }
-    if (htags[n] <= 0) return;
-    int ii = I - 5, jj = J - 5;
-    while (xc[ii] < ipx[n]) ii++;
-    while (yc[jj] < ipy[n]) jj++;
-    double x[4] = {xc[ii - 1], xc[ii], xc[ii - 1], xc[ii]};
-    double y[4] = {yc[jj - 1], yc[jj - 1], yc[jj], yc[jj]};
-    int id[4];
-    if (dir == 0) {
-        id[0] = (jj - 1) * (nx - 1) + ii - 1; id[1] = id[0] + 1;
-        id[2] = jj * (nx - 1) + ii - 1;       id[3] = id[2] + 1;
-    } else {
-        id[0] = (jj - 1) * nx + ii - 1 + nU; id[1] = id[0] + 1;
-        id[2] = jj * nx + ii - 1 + nU;       id[3] = id[2] + 1;
-    }
-    double q[4] = {u[id[0]], u[id[1]], u[id[2]], u[id[3]]};
-    for (int l = 0; l < 4; ++l)
-        if (htags[id[l]] == n) { x[l] = bix[n]; y[l] = biy[n]; q[l] = ub; }
-    double a[16], b[16], det;
-    rows_dev(x, y, a);
-    inverse4_dev(a, b, &det);
-    const double a0 = (b[0] * q[0] + b[1] * q[1] + b[2] * q[2] + b[3] * q[3]) / det;
-    const double a1 = (b[4] * q[0] + b[5] * q[1] + b[6] * q[2] + b[7] * q[3]) / det;
-    const double a2 = (b[8] * q[0] + b[9] * q[1] + b[10] * q[2] + b[11] * q[3]) / det;
-    const double a3 = (b[12] * q[0] + b[13] * q[1] + b[14] * q[2] + b[15] * q[3]) / det;
-    store_dev(idx4, coef4, n, id, b, det, xc[I], yc[J]);
-    ustar[n] = a0 + a1 * xc[I] + a2 * yc[J] + a3 * yc[J] * xc[I];
-    imageValue[n] = a0 + a1 * ipx[n] + a2 * ipy[n] + a3 * ipx[n] * ipy[n];
-}
-
-// Neumann row of the pressure fit at a body-intercept corner
-__device__ __forceinline__ void neumann_row(double px, double py, double bx_, double by_, double dudt, double dvdt,
-                                            double *a4, double *q)
+// Neumann row of the pressure fit at a body-intercept corner: the row of the
+// 4x4 system and the unit normal (the corner's value is then -(n . dU/dt))
+__device__ __forceinline__ void neumann_row(double px, double py, double bx_, double by_, double *a4, double *n2)
 {
     const double nxv = px - bx_, nyv = py - by_;
     const double nl = sqrt(nxv * nxv + nyv * nyv);
-    *q = -(nxv / nl * dudt + nyv / nl * dvdt);
+    n2[0] = nxv / nl;
+    n2[1] = nyv / nl;
     a4[0] = 0;
     a4[1] = nxv / nl;
     a4[2] = nyv / nl;
     a4[3] = nyv / nl * bx_ + nxv / nl * by_;
 }
 
-// pressure at hybrid nodes (interpolatePressureToHybridNode) into pstar
-__global__ void k_hybrid_pressure(BoxLaunch B, int nx, int ny, const double *__restrict__ p, const int *htags,
-                                  const double *xv, const double *yu, const double *uB, const double *uBk,
-                                  const double *vB, const double *vBk, double dt, const double *bix,
-                                  const double *biy, const double *ipx, const double *ipy, int *idx4,
-                                  double *coef4, double *pstar)
+// ---- interpolation plan ---------------------------------------------------------------
+// The ghost and hybrid interpolations are linear in the field: the value at a
+// node is sum_l w_l q_l over the four corners of the image point's cell, where
+// q_l is the field at the corner or, for corners replaced by the body, the body
+// velocity (velocity) or -(n . dU/dt) (pressure Neumann rows).  Which corners
+// are replaced, the corner indices and the weights w_l (the rows of the inverse
+// 4x4 bilinear fit evaluated at the point) depend only on the tags and the body
+// geometry, so they are computed once per tagging (luo_base::tagPoints) into a
+// plan of compact node lists; each step then only gathers.  The weights are the
+// reference's own q*coef of its biLinearInterpolation kernels, so the values
+// agree with its a0 + a1 x + a2 y + a3 x y to rounding.
+struct IbPlan {
+    int *count;  // [0] ghost velocity, [1] hybrid velocity, [2] ghost pressure, [3] hybrid pressure, [4] inside
+    int cap_v, cap_p, cap_in;
+    int *gvNode, *gvIdx, *gvMask;  // mask bit l: corner l takes the body value
+    double *gvW;
+    int *hvNode, *hvIdx, *hvMask;
+    double *hvW, *hvWi, *hvAlpha;  // weights at the node and at its image point; blend factor
+    int *gpNode, *gpIdx, *gpMask;  // mask bit l: corner l is a Neumann row
+    double *gpN, *gpW, *gpWb, *gpCn, *gpDist;  // corner normals; weights at image point and intercept;
+                                               // normal and distance of the dp/dn correction
+    int *hpNode, *hpIdx, *hpMask;
+    double *hpN, *hpW, *hpAlpha;
+    int *inNode;  // nodes inside the body (tag 0)
+};
+
+// weights of the fit at (px, py): coefficient c of store_dev
+__device__ __forceinline__ void fit_weights(const double b[16], double det, double px, double py, double *w)
 {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B.nthreads) return;
-    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
-    if (ip >= nx * ny || htags[ip] <= 0) return;
-    int ii = I - 5, jj = J - 5;
-    while (xv[ii] < ipx[ip]) ii++;
-    while (yu[jj] < ipy[ip]) jj++;
-    double x[4] = {xv[ii - 1], xv[ii], xv[ii - 1], xv[ii]};
-    double y[4] = {yu[jj - 1], yu[jj - 1], yu[jj], yu[jj]};
-    const int id[4] = {(jj - 1) * nx + ii - 1, (jj - 1) * nx + ii, jj * nx + ii - 1, jj * nx + ii};
-    double q[4] = {p[id[0]], p[id[1]], p[id[2]], p[id[3]]};
-    double a[16], b[16], det;
-    rows_dev(x, y, a);
-    const double dudt = (uB[0] - uBk[0]) / dt, dvdt = (vB[0] - vBk[0]) / dt;
-    for (int l = 0; l < 4; ++l)
-        if (htags[id[l]] == ip) {
-            x[l] = bix[ip];
-            y[l] = biy[ip];
-            neumann_row(ipx[ip], ipy[ip], x[l], y[l], dudt, dvdt, a + 4 * l, &q[l]);
-        }
-    inverse4_dev(a, b, &det);
-    const double a0 = b[0] / det * q[0] + b[1] / det * q[1] + b[2] / det * q[2] + b[3] / det * q[3];
-    const double a1 = b[4] / det * q[0] + b[5] / det * q[1] + b[6] / det * q[2] + b[7] / det * q[3];
-    const double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
-    const double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
-    store_dev(idx4, coef4, ip, id, b, det, xv[I], yu[J]);
-    pstar[ip] = a0 + a1 * xv[I] + a2 * yu[J] + a3 * xv[I] * yu[J];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) w[c] = (b[c] + b[4 + c] * px + b[8 + c] * py + b[12 + c] * px * py) / det;
 }
 
-// ghost pressure (interpolatePressureToGhostNode): values to staging, dpdn, biP
-__global__ void k_ghost_pressure(BoxLaunch B, int nx, int ny, const double *__restrict__ p, const int *gtags,
-                                 const double *xv, const double *yu, const double *uB, const double *uBk,
-                                 const double *vB, const double *vBk, double dt, const double *bix,
-                                 const double *biy, const double *ipx, const double *ipy, int *idx4, double *coef4,
-                                 double *biP, double *dpdn, double *staging)
+// ---- plan: node lists (the nodes the reference's interpolation threads act on) ----------
+// Same launch ranges and index arithmetic as the reference's kernels; list order
+// does not matter (every entry writes its own node).
+__global__ void k_plan_scan_velocity(BoxLaunch B, int nx, int ny, const int *gtags, const int *htags, IbPlan P)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= B.nthreads) return;
-    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
-    if (ip >= nx * ny || gtags[ip] <= 0) return;
-    int ii = I - 5, jj = J - 5;
-    while (xv[ii] < ipx[ip]) ii++;
-    while (yu[jj] < ipy[ip]) jj++;
-    double x[4] = {xv[ii - 1], xv[ii], xv[ii - 1], xv[ii]};
-    double y[4] = {yu[jj - 1], yu[jj - 1], yu[jj], yu[jj]};
-    const int id[4] = {(jj - 1) * nx + ii - 1, (jj - 1) * nx + ii, jj * nx + ii - 1, jj * nx + ii};
-    double q[4] = {p[id[0]], p[id[1]], p[id[2]], p[id[3]]};
-    double a[16], b[16], det;
-    rows_dev(x, y, a);
-    double mn = 1.0, matD = 0;
-    int close = -1;
-    for (int l = 0; l < 4; ++l) {
-        double ex = x[l] - bix[ip], ey = y[l] - biy[ip];
-        double s = sqrt(ex * ex + ey * ey);
-        if (s < mn) { mn = s; close = id[l]; }
-    }
-    const double dudt = (uB[0] - uBk[0]) / dt, dvdt = (vB[0] - vBk[0]) / dt;
-    for (int l = 0; l < 4; ++l) {
-        if (gtags[id[l]] > 0) {
-            x[l] = bix[id[l]];
-            y[l] = biy[id[l]];
-            neumann_row(ipx[id[l]], ipy[id[l]], x[l], y[l], dudt, dvdt, a + 4 * l, &q[l]);
-        }
-        if (id[l] == close) {
-            x[l] = bix[ip];
-            y[l] = biy[ip];
-            const double nxv = ipx[ip] - x[l], nyv = ipy[ip] - y[l];
-            const double nl = sqrt(nxv * nxv + nyv * nyv);
-            matD = nxv / nl * dudt + nyv / nl * dvdt;
-        }
-    }
-    inverse4_dev(a, b, &det);
-    const double a0 = b[0] / det * q[0] + b[1] / det * q[1] + b[2] / det * q[2] + b[3] / det * q[3];
-    const double a1 = b[4] / det * q[0] + b[5] / det * q[1] + b[6] / det * q[2] + b[7] / det * q[3];
-    const double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
-    const double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
-    store_dev(idx4, coef4, ip, id, b, det, ipx[ip], ipy[ip]);
-    const double ipv = a0 + a1 * ipx[ip] + a2 * ipy[ip] + a3 * ipy[ip] * ipx[ip];
-    biP[ip] = a0 + a1 * bix[ip] + a2 * biy[ip] + a3 * bix[ip] * biy[ip];
-    const double ex = ipx[ip] - xv[I], ey = ipy[ip] - yu[J];
-    const double d = sqrt(ex * ex + ey * ey) * matD;
-    dpdn[ip] = d;
-    staging[ip] = ipv + d;
-}
-
-__global__ void k_apply_ghost_p(BoxLaunch B, int nx, int ny, const int *gtags, const double *staging, double *p)
-{
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B.nthreads) return;
-    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
-    if (ip < nx * ny && gtags[ip] > 0) p[ip] = staging[ip];
-}
-
-// alpha-blend at hybrid nodes (weightX, weightY: blockIdx.y 0/1; weightP: CLS 2)
-template <int CLS>
-__global__ void k_weight(BoxLaunch B, int nx, int ny, double *f, const double *fstar, const int *gtags,
-                         const int *htags, const double *xa, const double *ya, const double *xb, const double *yb,
-                         const double *bix, const double *biy)
-{
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B.nthreads) return;
-    const int nU = (nx - 1) * ny;
+    const int dir = blockIdx.y, nU = (nx - 1) * ny;
     const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width;
-    int n, sv;
-    const double *xc, *yc;
-    if (CLS == 2) {
-        if (J * nx + I > nx * ny) return;
-        n = J * nx + I;
-        sv = nx;
-        xc = xa; yc = ya;
-    } else if (blockIdx.y == 0) {
+    int n;
+    if (dir == 0) {
         n = J * (nx - 1) + I;
-        sv = nx - 1;
-        xc = xa; yc = ya;
+        if (n >= nU) return;
     } else {
         if (J * nx + I > nx * (ny - 1)) return;
         n = J * nx + I + nU;
-        sv = nx;
-        xc = xb; yc = yb;
     }
-    if (htags[n] <= 0) return;
+    if (gtags[n] > 0) P.gvNode[atomicAdd(&P.count[0], 1)] = n;
+    if (htags[n] > 0) P.hvNode[atomicAdd(&P.count[1], 1)] = n;
+}
+
+__global__ void k_plan_scan_pressure(BoxLaunch B, int nx, int ny, const int *gtags, const int *htags, IbPlan P)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B.nthreads) return;
+    const int I = B.i0 + idx % B.width, J = B.j0 + idx / B.width, ip = J * nx + I;
+    if (ip >= nx * ny) return;
+    if (gtags[ip] > 0) P.gpNode[atomicAdd(&P.count[2], 1)] = ip;
+    if (htags[ip] > 0) P.hpNode[atomicAdd(&P.count[3], 1)] = ip;
+}
+
+// inside nodes over the reference's u-index map (setInsideVelocity): u node i and
+// the v node at the same (I, J)
+__global__ void k_plan_scan_inside(int nx, int ny, const int *gtags, IbPlan P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nU = (nx - 1) * ny, nUV = nU + nx * (ny - 1);
+    if (i >= nU) return;
+    const int I = i % (nx - 1), J = i / (nx - 1), iv = J * nx + I + nU;
+    if (gtags[i] == 0) P.inNode[atomicAdd(&P.count[4], 1)] = i;
+    if (iv < nUV && gtags[iv] == 0) P.inNode[atomicAdd(&P.count[4], 1)] = iv;
+}
+
+// ---- plan: per-node geometry (the reference's interpolation kernels minus the field) --------
+struct PlanGeom {
+    int nx, ny;
+    const double *xu, *yu, *xv, *yv;
+    const int *gUV, *hUV, *gP, *hP;                 // tags
+    const double *biX, *biY, *ipX, *ipY;            // velocity intercepts and image points
+    const double *bipX, *bipY, *ippX, *ippY;        // pressure intercepts and image points
+    int *gIdx, *hIdx, *gpIdx, *hpIdx;               // per-node stencils (the reference's index/coef arrays)
+    double *gCoef, *hCoef, *gpCoef, *hpCoef;
+};
+
+__device__ __forceinline__ void node_ij(int n, int nx, int nU, int *I, int *J)
+{
+    if (n < nU) {
+        *I = n % (nx - 1);
+        *J = n / (nx - 1);
+    } else {
+        *I = (n - nU) % nx;
+        *J = (n - nU) / nx;
+    }
+}
+
+// corner cell of the image point (the reference's search from I-5, J-5)
+__device__ __forceinline__ void image_cell(const double *xc, const double *yc, int I, int J, double px, double py,
+                                           int *ii, int *jj)
+{
+    int a = I - 5, b = J - 5;
+    while (xc[a] < px) a++;
+    while (yc[b] < py) b++;
+    *ii = a;
+    *jj = b;
+}
+
+// alpha of luoIBM weight (weightX / weightY / weightP) at hybrid node n
+__device__ __forceinline__ double blend_alpha(int n, int I, int J, int sv, const double *xc, const double *yc,
+                                              const int *gtags, const double *bix, const double *biy)
+{
     double d1 = 0, d2 = 0;
     const double dx = xc[I] - xc[I - 1], dy = yc[J] - yc[J - 1];
     double ex, ey;
@@ -841,35 +693,329 @@ __global__ void k_weight(BoxLaunch B, int nx, int ny, double *f, const double *f
         d2 = sqrt(ex * ex + ey * ey);
     }
     const double r1 = d1 / dx, r2 = d2 / dy;
-    const double alpha = sqrt(r1 * r1 + r2 * r2);
-    f[n] = (1 - alpha) * f[n] + alpha * fstar[n];
+    return sqrt(r1 * r1 + r2 * r2);
 }
 
-// u inside the body := body velocity (setInsideVelocity over the u-index map)
-__global__ void k_set_inside(int nx, int ny, const int *gtags, double *u, const double *uB, const double *vB)
+// ghost velocity node (interpolateVelocityToGhostNodeX/Y): value at the image point
+__device__ void plan_ghost_velocity(int k, const PlanGeom &G, const IbPlan &P)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nU = (nx - 1) * ny, nUV = nU + nx * (ny - 1);
-    if (i >= nU) return;
-    const int I = i % (nx - 1), J = i / (nx - 1), iv = J * nx + I + nU;
-    u[i] = (gtags[i] != 0) * u[i] + (gtags[i] == 0) * uB[0];
-    if (iv < nUV) u[iv] = (gtags[iv] != 0) * u[iv] + (gtags[iv] == 0) * vB[0];
+    const int nx = G.nx, ny = G.ny, nU = (nx - 1) * ny, n = P.gvNode[k];
+    const int dir = n >= nU;
+    int I, J, ii, jj;
+    node_ij(n, nx, nU, &I, &J);
+    const double *xc = dir ? G.xv : G.xu, *yc = dir ? G.yv : G.yu;
+    image_cell(xc, yc, I, J, G.ipX[n], G.ipY[n], &ii, &jj);
+    double x[4] = {xc[ii - 1], xc[ii], xc[ii - 1], xc[ii]};
+    double y[4] = {yc[jj - 1], yc[jj - 1], yc[jj], yc[jj]};
+    int id[4];
+    if (dir == 0) {
+        id[0] = (jj - 1) * (nx - 1) + ii - 1; id[1] = id[0] + 1;
+        id[2] = jj * (nx - 1) + ii - 1;       id[3] = id[2] + 1;
+    } else {
+        id[0] = (jj - 1) * nx + ii - 1 + nU; id[1] = id[0] + 1;
+        id[2] = jj * nx + ii - 1 + nU;       id[3] = id[2] + 1;
+    }
+    double mn = 1.0;
+    int close = -1, mask = 0;
+    bool inflag = false;
+    for (int l = 0; l < 4; ++l) {
+        double ex = x[l] - G.biX[n], ey = y[l] - G.biY[n];
+        double s = sqrt(ex * ex + ey * ey);
+        if (s < mn) { mn = s; close = id[l]; }
+        if (G.gUV[id[l]] > 0) inflag = true;
+    }
+    for (int l = 0; l < 4; ++l) {
+        if (G.gUV[id[l]] == n) { x[l] = G.biX[id[l]]; y[l] = G.biY[id[l]]; mask |= 1 << l; }
+        else if (id[l] == close && !inflag) { x[l] = G.biX[n]; y[l] = G.biY[n]; mask |= 1 << l; }
+    }
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    inverse4_dev(a, b, &det);
+    store_dev(G.gIdx, G.gCoef, n, id, b, det, G.ipX[n], G.ipY[n]);
+    fit_weights(b, det, G.ipX[n], G.ipY[n], P.gvW + 4 * (size_t)k);
+    for (int l = 0; l < 4; ++l) P.gvIdx[4 * (size_t)k + l] = id[l];
+    P.gvMask[k] = mask;
 }
 
-// convective outflow on the x+ boundary (updateBoundaryX / updateBoundaryY)
-__global__ void k_robin(int nx, int ny, const double *u, double *xp, const double *dx, double dt, double Uinf,
-                        double Vinf)
+// hybrid velocity node (interpolateVelocityToHybridNodeX/Y): value at the node, at
+// its image point, and the blend factor of weightX/Y
+__device__ void plan_hybrid_velocity(int k, const PlanGeom &G, const IbPlan &P)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nU = (nx - 1) * ny;
-    if (t < ny) {
-        const int J = t, I = nx - 1, i = J * (nx - 1) + I;
-        const double beta = Uinf * dt / dx[I];
-        xp[J] = xp[J] * (1 - beta) + beta * u[i - 1];
-    } else if (t < 2 * ny - 1) {
-        const int J = t - ny, I = nx, i = J * nx + I;
-        const double beta = Vinf * dt / dx[I - 1];
-        xp[J + ny] = xp[J + ny] * (1 - beta) + beta * u[i + nU - 1];
+    const int nx = G.nx, ny = G.ny, nU = (nx - 1) * ny, n = P.hvNode[k];
+    const int dir = n >= nU;
+    int I, J, ii, jj;
+    node_ij(n, nx, nU, &I, &J);
+    const double *xc = dir ? G.xv : G.xu, *yc = dir ? G.yv : G.yu;
+    image_cell(xc, yc, I, J, G.ipX[n], G.ipY[n], &ii, &jj);
+    double x[4] = {xc[ii - 1], xc[ii], xc[ii - 1], xc[ii]};
+    double y[4] = {yc[jj - 1], yc[jj - 1], yc[jj], yc[jj]};
+    int id[4];
+    if (dir == 0) {
+        id[0] = (jj - 1) * (nx - 1) + ii - 1; id[1] = id[0] + 1;
+        id[2] = jj * (nx - 1) + ii - 1;       id[3] = id[2] + 1;
+    } else {
+        id[0] = (jj - 1) * nx + ii - 1 + nU; id[1] = id[0] + 1;
+        id[2] = jj * nx + ii - 1 + nU;       id[3] = id[2] + 1;
+    }
+    int mask = 0;
+    for (int l = 0; l < 4; ++l)
+        if (G.hUV[id[l]] == n) { x[l] = G.biX[n]; y[l] = G.biY[n]; mask |= 1 << l; }
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    inverse4_dev(a, b, &det);
+    store_dev(G.hIdx, G.hCoef, n, id, b, det, xc[I], yc[J]);
+    fit_weights(b, det, xc[I], yc[J], P.hvW + 4 * (size_t)k);
+    fit_weights(b, det, G.ipX[n], G.ipY[n], P.hvWi + 4 * (size_t)k);
+    for (int l = 0; l < 4; ++l) P.hvIdx[4 * (size_t)k + l] = id[l];
+    P.hvMask[k] = mask;
+    P.hvAlpha[k] = blend_alpha(n, I, J, dir ? nx : nx - 1, xc, yc, G.gUV, G.biX, G.biY);
+}
+
+// hybrid pressure node (interpolatePressureToHybridNode): value at the node, blend of weightP
+__device__ void plan_hybrid_pressure(int k, const PlanGeom &G, const IbPlan &P)
+{
+    const int nx = G.nx, ip = P.hpNode[k];
+    const int I = ip % nx, J = ip / nx;
+    int ii, jj;
+    image_cell(G.xv, G.yu, I, J, G.ippX[ip], G.ippY[ip], &ii, &jj);
+    double x[4] = {G.xv[ii - 1], G.xv[ii], G.xv[ii - 1], G.xv[ii]};
+    double y[4] = {G.yu[jj - 1], G.yu[jj - 1], G.yu[jj], G.yu[jj]};
+    const int id[4] = {(jj - 1) * nx + ii - 1, (jj - 1) * nx + ii, jj * nx + ii - 1, jj * nx + ii};
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    int mask = 0;
+    for (int l = 0; l < 4; ++l) {
+        P.hpN[8 * (size_t)k + 2 * l] = 0;
+        P.hpN[8 * (size_t)k + 2 * l + 1] = 0;
+        if (G.hP[id[l]] == ip) {
+            x[l] = G.bipX[ip];
+            y[l] = G.bipY[ip];
+            neumann_row(G.ippX[ip], G.ippY[ip], x[l], y[l], a + 4 * l, P.hpN + 8 * (size_t)k + 2 * l);
+            mask |= 1 << l;
+        }
+    }
+    inverse4_dev(a, b, &det);
+    store_dev(G.hpIdx, G.hpCoef, ip, id, b, det, G.xv[I], G.yu[J]);
+    fit_weights(b, det, G.xv[I], G.yu[J], P.hpW + 4 * (size_t)k);
+    for (int l = 0; l < 4; ++l) P.hpIdx[4 * (size_t)k + l] = id[l];
+    P.hpMask[k] = mask;
+    P.hpAlpha[k] = blend_alpha(ip, I, J, nx, G.xv, G.yu, G.gP, G.bipX, G.bipY);
+}
+
+// ghost pressure node (interpolatePressureToGhostNode): value at the image point, at the
+// body intercept, and the dp/dn correction's normal and distance
+__device__ void plan_ghost_pressure(int k, const PlanGeom &G, const IbPlan &P)
+{
+    const int nx = G.nx, ip = P.gpNode[k];
+    const int I = ip % nx, J = ip / nx;
+    int ii, jj;
+    image_cell(G.xv, G.yu, I, J, G.ippX[ip], G.ippY[ip], &ii, &jj);
+    double x[4] = {G.xv[ii - 1], G.xv[ii], G.xv[ii - 1], G.xv[ii]};
+    double y[4] = {G.yu[jj - 1], G.yu[jj - 1], G.yu[jj], G.yu[jj]};
+    const int id[4] = {(jj - 1) * nx + ii - 1, (jj - 1) * nx + ii, jj * nx + ii - 1, jj * nx + ii};
+    double a[16], b[16], det;
+    rows_dev(x, y, a);
+    double mn = 1.0, cn[2] = {0, 0};
+    int close = -1, mask = 0;
+    for (int l = 0; l < 4; ++l) {
+        double ex = x[l] - G.bipX[ip], ey = y[l] - G.bipY[ip];
+        double s = sqrt(ex * ex + ey * ey);
+        if (s < mn) { mn = s; close = id[l]; }
+    }
+    for (int l = 0; l < 4; ++l) {
+        P.gpN[8 * (size_t)k + 2 * l] = 0;
+        P.gpN[8 * (size_t)k + 2 * l + 1] = 0;
+        if (G.gP[id[l]] > 0) {
+            x[l] = G.bipX[id[l]];
+            y[l] = G.bipY[id[l]];
+            neumann_row(G.ippX[id[l]], G.ippY[id[l]], x[l], y[l], a + 4 * l, P.gpN + 8 * (size_t)k + 2 * l);
+            mask |= 1 << l;
+        }
+        if (id[l] == close) {
+            x[l] = G.bipX[ip];
+            y[l] = G.bipY[ip];
+            const double nxv = G.ippX[ip] - x[l], nyv = G.ippY[ip] - y[l];
+            const double nl = sqrt(nxv * nxv + nyv * nyv);
+            cn[0] = nxv / nl;
+            cn[1] = nyv / nl;
+        }
+    }
+    inverse4_dev(a, b, &det);
+    store_dev(G.gpIdx, G.gpCoef, ip, id, b, det, G.ippX[ip], G.ippY[ip]);
+    fit_weights(b, det, G.ippX[ip], G.ippY[ip], P.gpW + 4 * (size_t)k);
+    fit_weights(b, det, G.bipX[ip], G.bipY[ip], P.gpWb + 4 * (size_t)k);
+    for (int l = 0; l < 4; ++l) P.gpIdx[4 * (size_t)k + l] = id[l];
+    P.gpMask[k] = mask;
+    const double ex = G.ippX[ip] - G.xv[I], ey = G.ippY[ip] - G.yu[J];
+    P.gpCn[2 * (size_t)k] = cn[0];
+    P.gpCn[2 * (size_t)k + 1] = cn[1];
+    P.gpDist[k] = sqrt(ex * ex + ey * ey);
+}
+
+// blockIdx.y: 0 ghost velocity, 1 hybrid velocity, 2 ghost pressure, 3 hybrid pressure
+__global__ void k_plan_build(PlanGeom G, IbPlan P)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cls = blockIdx.y;
+    if (k >= P.count[cls]) return;
+    if (cls == 0) plan_ghost_velocity(k, G, P);
+    else if (cls == 1) plan_hybrid_velocity(k, G, P);
+    else if (cls == 2) plan_ghost_pressure(k, G, P);
+    else plan_hybrid_pressure(k, G, P);
+}
+
+// ---- per-step immersed-boundary phases -------------------------------------------------
+// One block runs a sequence of the reference's IB phases on the plan's node lists
+// (a few hundred to a few thousand nodes), with __syncthreads between them.  Ghost
+// phases stage their new values and write them after a barrier, so every node
+// reads the field as it was before the phase (the reference's launch: all loads
+// precede all stores).  Phases run in this order, which contains each of the
+// reference's sequences (rhs1: Robin, ghost, inside, hybrid; after the velocity
+// solve: weight, ghost; after the Poisson solve: hybrid, weight, ghost pressure;
+// after the projection: ghost, inside).
+enum IbPhase {
+    PH_ROBIN = 1,      // updateRobinBoundary (Uinf = Vinf = 1)
+    PH_WEIGHT_U = 2,   // weightX/Y: vel = (1 - alpha) vel + alpha ustar at hybrid nodes
+    PH_GHOST_U = 4,    // interpolateVelocityToGhostNodeX/Y on vel
+    PH_INSIDE = 8,     // setInsideVelocity on vel
+    PH_HYBRID_U = 16,  // interpolateVelocityToHybridNodeX/Y: ustar from vel
+    PH_HYBRID_P = 32,  // interpolatePressureToHybridNode: pstar from p
+    PH_WEIGHT_P = 64,  // weightP
+    PH_GHOST_P = 128   // interpolatePressureToGhostNode on p
+};
+
+struct IbStep {
+    IbPlan P;
+    int nx, ny;
+    double *vel, *p;
+    const double *uB, *vB, *uBk, *vBk;
+    double dt;
+    double *ustar, *pstar, *imageValue, *biP, *dpdn, *stage;
+    double *xp;
+    const double *dx;
+};
+
+constexpr int kIbThreads = 512;
+
+__global__ void __launch_bounds__(kIbThreads) k_ib_step(IbStep S, int phases)
+{
+    const int t = threadIdx.x, T = blockDim.x;
+    const int nx = S.nx, ny = S.ny, nU = (nx - 1) * ny;
+    const IbPlan &P = S.P;
+    double *f = S.vel;
+    if (phases & PH_ROBIN) {
+        for (int r = t; r < 2 * ny - 1; r += T) {
+            if (r < ny) {
+                const int J = r, I = nx - 1, i = J * (nx - 1) + I;
+                const double beta = 1.0 * S.dt / S.dx[I];
+                S.xp[J] = S.xp[J] * (1 - beta) + beta * f[i - 1];
+            } else {
+                const int J = r - ny, I = nx, i = J * nx + I;
+                const double beta = 1.0 * S.dt / S.dx[I - 1];
+                S.xp[J + ny] = S.xp[J + ny] * (1 - beta) + beta * f[i + nU - 1];
+            }
+        }
+    }
+    if (phases & PH_WEIGHT_U) {
+        const int cnt = P.count[1];
+        for (int k = t; k < cnt; k += T) {
+            const int n = P.hvNode[k];
+            const double a = P.hvAlpha[k];
+            f[n] = (1 - a) * f[n] + a * S.ustar[n];
+        }
+        __syncthreads();
+    }
+    if (phases & PH_GHOST_U) {
+        const int cnt = P.count[0];
+        const double ub = S.uB[0], vb = S.vB[0];
+        for (int k = t; k < cnt; k += T) {
+            const int n = P.gvNode[k], m = P.gvMask[k];
+            const double qb = n >= nU ? vb : ub;
+            double val = 0;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const double q = (m >> l & 1) ? qb : f[P.gvIdx[4 * k + l]];
+                val += P.gvW[4 * k + l] * q;
+            }
+            S.imageValue[n] = val;
+            S.stage[k] = 2 * qb - val;
+        }
+        __syncthreads();
+        for (int k = t; k < cnt; k += T) f[P.gvNode[k]] = S.stage[k];
+        __syncthreads();
+    }
+    if (phases & PH_INSIDE) {
+        const int cnt = P.count[4];
+        const double ub = S.uB[0], vb = S.vB[0];
+        for (int k = t; k < cnt; k += T) {
+            const int n = P.inNode[k];
+            f[n] = n >= nU ? vb : ub;
+        }
+        __syncthreads();
+    }
+    if (phases & PH_HYBRID_U) {
+        const int cnt = P.count[1];
+        const double ub = S.uB[0], vb = S.vB[0];
+        for (int k = t; k < cnt; k += T) {
+            const int n = P.hvNode[k], m = P.hvMask[k];
+            const double qb = n >= nU ? vb : ub;
+            double s = 0, si = 0;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const double q = (m >> l & 1) ? qb : f[P.hvIdx[4 * k + l]];
+                s += P.hvW[4 * k + l] * q;
+                si += P.hvWi[4 * k + l] * q;
+            }
+            S.ustar[n] = s;
+            S.imageValue[n] = si;
+        }
+        __syncthreads();
+    }
+    const double dudt = (S.uB[0] - S.uBk[0]) / S.dt, dvdt = (S.vB[0] - S.vBk[0]) / S.dt;
+    if (phases & PH_HYBRID_P) {
+        const int cnt = P.count[3];
+        for (int k = t; k < cnt; k += T) {
+            const int ip = P.hpNode[k], m = P.hpMask[k];
+            double s = 0;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const double *nn = P.hpN + 8 * k + 2 * l;
+                const double q = (m >> l & 1) ? -(nn[0] * dudt + nn[1] * dvdt) : S.p[P.hpIdx[4 * k + l]];
+                s += P.hpW[4 * k + l] * q;
+            }
+            S.pstar[ip] = s;
+        }
+        __syncthreads();
+    }
+    if (phases & PH_WEIGHT_P) {
+        const int cnt = P.count[3];
+        for (int k = t; k < cnt; k += T) {
+            const int ip = P.hpNode[k];
+            const double a = P.hpAlpha[k];
+            S.p[ip] = (1 - a) * S.p[ip] + a * S.pstar[ip];
+        }
+        __syncthreads();
+    }
+    if (phases & PH_GHOST_P) {
+        const int cnt = P.count[2];
+        for (int k = t; k < cnt; k += T) {
+            const int ip = P.gpNode[k], m = P.gpMask[k];
+            double v = 0, vb = 0;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const double *nn = P.gpN + 8 * k + 2 * l;
+                const double q = (m >> l & 1) ? -(nn[0] * dudt + nn[1] * dvdt) : S.p[P.gpIdx[4 * k + l]];
+                v += P.gpW[4 * k + l] * q;
+                vb += P.gpWb[4 * k + l] * q;
+            }
+            S.biP[ip] = vb;
+            const double matD = P.gpCn[2 * k] * dudt + P.gpCn[2 * k + 1] * dvdt;
+            const double d = P.gpDist[k] * matD;
+            S.dpdn[ip] = d;
+            S.stage[k] = v + d;
+        }
+        __syncthreads();
+        for (int k = t; k < cnt; k += T) S.p[P.gpNode[k]] = S.stage[k];
     }
 }
 
@@ -1024,6 +1170,7 @@ struct IbHost {
     double *staging = nullptr;
     unsigned int *force_arrive = nullptr;
     bool moving = false;
+    IbPlan plan{};
 };
 static std::vector<IbHost> g_ib_host;  // one per context (indexed by Context::ib_slot)
 
@@ -1065,7 +1212,7 @@ void setup_ib(Context &c)
     b.hCoef = c.carve<double>(4 * UV);
     b.gpCoef = c.carve<double>(4 * P);
     b.hpCoef = c.carve<double>(4 * P);
-    b.gnValue = c.carve<double>(UV > P ? UV : P);
+    b.gnValue = c.carve<double>(std::max<size_t>(UV > P ? UV : P, 2 * (size_t)ref_threads(c.bb.ncx + 16, c.bb.ncy + 16)));
     b.bx = c.carve<double>(nb);
     b.by = c.carve<double>(nb);
     b.uB = c.carve<double>(nb);
@@ -1101,6 +1248,39 @@ void setup_ib(Context &c)
     H.rec.distA = c.carve<double>(nr);
     H.rec.distB = c.carve<double>(nr);
     H.rec.bi = c.carve<double>(nr * 20);
+    // interpolation plan: lists sized for every node the box launch can visit
+    IbPlan &L = H.plan;
+    L.cap_v = 2 * (int)nr;
+    L.cap_p = (int)nr;
+    L.cap_in = (int)UV;
+    const size_t cv = L.cap_v, cp = L.cap_p;
+    L.count = c.carve<int>(8);
+    L.gvNode = c.carve<int>(cv);
+    L.gvIdx = c.carve<int>(4 * cv);
+    L.gvMask = c.carve<int>(cv);
+    L.gvW = c.carve<double>(4 * cv);
+    L.hvNode = c.carve<int>(cv);
+    L.hvIdx = c.carve<int>(4 * cv);
+    L.hvMask = c.carve<int>(cv);
+    L.hvW = c.carve<double>(4 * cv);
+    L.hvWi = c.carve<double>(4 * cv);
+    L.hvAlpha = c.carve<double>(cv);
+    L.gpNode = c.carve<int>(cp);
+    L.gpIdx = c.carve<int>(4 * cp);
+    L.gpMask = c.carve<int>(cp);
+    L.gpN = c.carve<double>(8 * cp);
+    L.gpW = c.carve<double>(4 * cp);
+    L.gpWb = c.carve<double>(4 * cp);
+    L.gpCn = c.carve<double>(2 * cp);
+    L.gpDist = c.carve<double>(cp);
+    L.hpNode = c.carve<int>(cp);
+    L.hpIdx = c.carve<int>(4 * cp);
+    L.hpMask = c.carve<int>(cp);
+    L.hpN = c.carve<double>(8 * cp);
+    L.hpW = c.carve<double>(4 * cp);
+    L.hpAlpha = c.carve<double>(cp);
+    L.inNode = c.carve<int>(UV);
+    CUIBM_TRY(cudaMemsetAsync(L.count, 0, 8 * sizeof(int), c.stream));
     const BodyState &B = c.body;
     H.moving = B.xCoeff != 0 || B.uCoeff != 0;
     // the host-evaluated prescribed motion for every step (luo_base/move.cu:121-146):
@@ -1191,85 +1371,45 @@ void launch_tag_points(Context &c)
     k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostP, nx, i0, i1, j0, j1, zrows, nx);
     k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostUV, nx - 1, i0, i1, j0, j1, zrows, nx - 1);
     k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostUV + c.g.nU, nx, i0, i1, j0, j1, zrows, nx - 1);
+    // the interpolation plan of these tags
+    IbPlan &P = H.plan;
+    BoxLaunch B = box(c);
+    CUIBM_TRY(cudaMemsetAsync(P.count, 0, 8 * sizeof(int), c.stream));
+    k_plan_scan_velocity<<<dim3(blocks_for(B.nthreads), 2), kBlock, 0, c.stream>>>(B, nx, ny, b.ghostUV, b.hybridUV, P);
+    k_plan_scan_pressure<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(B, nx, ny, b.ghostP, b.hybridP, P);
+    k_plan_scan_inside<<<blocks_for(c.g.nU), kBlock, 0, c.stream>>>(nx, ny, b.ghostUV, P);
+    PlanGeom G2{nx, ny, c.xu, c.yu, c.xv, c.yv, b.ghostUV, b.hybridUV, b.ghostP, b.hybridP, b.biX, b.biY, b.ipX,
+                b.ipY, b.bipX, b.bipY, b.ippX, b.ippY, b.gIdx, b.hIdx, b.gpIdx, b.hpIdx, b.gCoef, b.hCoef,
+                b.gpCoef, b.hpCoef};
+    k_plan_build<<<dim3(blocks_for(P.cap_v), 4), kBlock, 0, c.stream>>>(G2, P);
     CUIBM_TRY(cudaGetLastError());
 }
 
-void launch_ghost_velocity(Context &c, double *field, bool set)
+// one block runs the phases in k_ib_step's order on the plan of the current tags
+static void launch_ib(Context &c, int phases, double *vel)
 {
     IbArrays &b = c.ib;
-    BoxLaunch B = box(c);
-    dim3 grid(blocks_for(B.nthreads), 2);
-    k_ghost_velocity<<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, field, b.ghostUV, c.xu, c.yu, c.xv, c.yv,
-                                                    b.uB, b.vB, b.biX, b.biY, b.ipX, b.ipY, b.gIdx, b.gCoef,
-                                                    b.imageValue, b.gnValue);
-    if (set) k_apply_ghost<<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, b.ghostUV, b.gnValue, field);
+    IbStep S{hostside(c).plan, c.g.nx, c.g.ny, vel, c.p, b.uB, b.vB, b.uBk, b.vBk, c.P.dt, b.ustar, b.pstar,
+             b.imageValue, b.biP, b.dpdn, b.gnValue, c.bc[XPLUS], c.dx};
+    k_ib_step<<<1, kIbThreads, 0, c.stream>>>(S, phases);
     CUIBM_TRY(cudaGetLastError());
 }
 
-void launch_hybrid_velocity(Context &c, const double *field)
-{
-    IbArrays &b = c.ib;
-    BoxLaunch B = box(c);
-    dim3 grid(blocks_for(B.nthreads), 2);
-    k_hybrid_velocity<<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, field, b.hybridUV, c.xu, c.yu, c.xv, c.yv,
-                                                     b.uB, b.vB, b.biX, b.biY, b.ipX, b.ipY, b.hIdx, b.hCoef,
-                                                     b.imageValue, b.ustar);
-    CUIBM_TRY(cudaGetLastError());
-}
+void launch_ghost_velocity(Context &c, double *field, bool) { launch_ib(c, PH_GHOST_U, field); }
+void launch_hybrid_velocity(Context &c, const double *field) { launch_ib(c, PH_HYBRID_U, const_cast<double *>(field)); }
+void launch_set_inside(Context &c, double *field) { launch_ib(c, PH_INSIDE, field); }
+void launch_weight_uhat(Context &c) { launch_ib(c, PH_WEIGHT_U, c.uhat); }
+void launch_hybrid_pressure(Context &c) { launch_ib(c, PH_HYBRID_P, c.u); }
+void launch_weight_pressure(Context &c) { launch_ib(c, PH_WEIGHT_P, c.u); }
+void launch_ghost_pressure(Context &c, bool) { launch_ib(c, PH_GHOST_P, c.u); }
+// updateRobinBoundary: Uinf = Vinf = 1 (luo_base/intermediateVelocity.cu:216-217)
+void launch_robin(Context &c) { launch_ib(c, PH_ROBIN, c.u); }
 
-void launch_set_inside(Context &c, double *field)
-{
-    k_set_inside<<<blocks_for(c.g.nU), kBlock, 0, c.stream>>>(c.g.nx, c.g.ny, c.ib.ghostUV, field, c.ib.uB, c.ib.vB);
-    CUIBM_TRY(cudaGetLastError());
-}
-
-void launch_weight_uhat(Context &c)
-{
-    IbArrays &b = c.ib;
-    BoxLaunch B = box(c);
-    dim3 grid(blocks_for(B.nthreads), 2);
-    k_weight<0><<<grid, kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, c.uhat, b.ustar, b.ghostUV, b.hybridUV, c.xu,
-                                               c.yu, c.xv, c.yv, b.biX, b.biY);
-    CUIBM_TRY(cudaGetLastError());
-}
-
-void launch_hybrid_pressure(Context &c)
-{
-    IbArrays &b = c.ib;
-    BoxLaunch B = box(c);
-    k_hybrid_pressure<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(
-        B, c.g.nx, c.g.ny, c.p, b.hybridP, c.xv, c.yu, b.uB, b.uBk, b.vB, b.vBk, c.P.dt, b.bipX, b.bipY, b.ippX,
-        b.ippY, b.hpIdx, b.hpCoef, b.pstar);
-    CUIBM_TRY(cudaGetLastError());
-}
-
-void launch_weight_pressure(Context &c)
-{
-    IbArrays &b = c.ib;
-    BoxLaunch B = box(c);
-    k_weight<2><<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, c.p, b.pstar, b.ghostP,
-                                                                 b.hybridP, c.xv, c.yu, nullptr, nullptr, b.bipX,
-                                                                 b.bipY);
-    CUIBM_TRY(cudaGetLastError());
-}
-
-void launch_ghost_pressure(Context &c, bool set)
-{
-    IbArrays &b = c.ib;
-    BoxLaunch B = box(c);
-    k_ghost_pressure<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(
-        B, c.g.nx, c.g.ny, c.p, b.ghostP, c.xv, c.yu, b.uB, b.uBk, b.vB, b.vBk, c.P.dt, b.bipX, b.bipY, b.ippX, b.ippY,
-        b.gpIdx, b.gpCoef, b.biP, b.dpdn, b.gnValue);
-    if (set) k_apply_ghost_p<<<blocks_for(B.nthreads), kBlock, 0, c.stream>>>(B, c.g.nx, c.g.ny, b.ghostP, b.gnValue, c.p);
-    CUIBM_TRY(cudaGetLastError());
-}
-
-void launch_robin(Context &c)
-{
-    // updateRobinBoundary: Uinf = Vinf = 1 (luo_base/intermediateVelocity.cu:216-217)
-    k_robin<<<blocks_for(2 * c.g.ny), kBlock, 0, c.stream>>>(c.g.nx, c.g.ny, c.u, c.bc[XPLUS], c.dx, c.P.dt, 1.0, 1.0);
-    CUIBM_TRY(cudaGetLastError());
-}
+// the step's IB sequences, one launch each
+void launch_ib_rhs1(Context &c) { launch_ib(c, PH_ROBIN | PH_GHOST_U | PH_INSIDE | PH_HYBRID_U, c.u); }
+void launch_ib_after_velocity(Context &c) { launch_ib(c, PH_WEIGHT_U | PH_GHOST_U, c.uhat); }
+void launch_ib_after_poisson(Context &c) { launch_ib(c, PH_HYBRID_P | PH_WEIGHT_P | PH_GHOST_P, c.u); }
+void launch_ib_after_projection(Context &c) { launch_ib(c, PH_GHOST_U | PH_INSIDE, c.u); }
 
 void launch_force(Context &c)
 {

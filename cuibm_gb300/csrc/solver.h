@@ -250,6 +250,10 @@ void launch_hybrid_pressure(Context &c);
 void launch_ghost_pressure(Context &c, bool set);
 void launch_weight_pressure(Context &c);
 void launch_robin(Context &c);
+void launch_ib_rhs1(Context &c);             // Robin, ghost u, inside, hybrid u
+void launch_ib_after_velocity(Context &c);   // weight uhat, ghost uhat
+void launch_ib_after_poisson(Context &c);    // hybrid p, weight p, ghost p
+void launch_ib_after_projection(Context &c); // ghost u, inside
 void launch_force(Context &c);
 void launch_body_motion(Context &c, double t);
 void launch_body_pre_step(Context &c);
