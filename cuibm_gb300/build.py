@@ -33,6 +33,7 @@ UNITS = {
     "krylov.cu": [],
     "amg.cu": [],
     "fused_solve.cu": [],
+    "fadlun.cu": ["-fmad=false"],
     "ib_kernels.cu": ["-fmad=false"],
 }
 

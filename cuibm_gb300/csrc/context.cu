@@ -29,6 +29,8 @@ static void alloc_fields(Context &c)
     if (c.has_body) est += (nUV + nP) * 400;
     CUIBM_TRY(cudaMalloc(&c.arena, est));
     c.arena_bytes = est;
+    // device arrays start at zero, as the reference's value-initialised cusp arrays do
+    CUIBM_TRY(cudaMemset(c.arena, 0, est));
     c.arena_used = 0;
     CUIBM_TRY(cudaMemsetAsync(c.arena, 0, est, c.stream));
     c.u = c.carve<double>(nUV);
@@ -129,13 +131,17 @@ struct PhaseTimer {
 
 // ---- phases ---------------------------------------------------------------------
 static bool is_luo(const Context &c) { return c.P.solverType == ST_LUO && c.has_body; }
+static bool is_fadlun(const Context &c) { return c.P.solverType == ST_FADLUN && c.has_body; }
+static bool is_ib(const Context &c) { return is_luo(c) || is_fadlun(c); }
 
 static void phase_generate_rhs1(Context &c)
 {
     PhaseTimer t(c, "Intermediate Velocity Setup");
     // updateRobinBoundary, rhs1GNInterpolation, zeroVelocity, rhs1HNInterpolation
     if (is_luo(c)) launch_ib_rhs1(c);
+    if (is_fadlun(c)) launch_robin(c);
     launch_rhs1(c, false);
+    if (is_fadlun(c)) launch_fadlun_rhs1(c);  // updateRHS1forIBX/Y
 }
 
 static void phase_solve_velocity(Context &c, bool in_graph)
@@ -147,7 +153,10 @@ static void phase_solve_velocity(Context &c, bool in_graph)
 static void phase_generate_rhs2(Context &c)
 {
     PhaseTimer t(c, "Poisson Setup");
-    launch_rhs2(c, c.uhat);
+    if (is_fadlun(c))
+        launch_fadlun_rhs2(c);
+    else
+        launch_rhs2(c, c.uhat);
 }
 
 static void phase_solve_poisson(Context &c, bool in_graph)
@@ -159,13 +168,17 @@ static void phase_solve_poisson(Context &c, bool in_graph)
 static void phase_project(Context &c)
 {
     PhaseTimer t(c, "Velocity Projection");
+    if (is_fadlun(c)) {
+        launch_fadlun_project(c);
+        return;
+    }
     launch_project(c);
     if (is_luo(c)) launch_ib_after_projection(c);  // ghost u, zeroVelocity
 }
 
 static void phase_update_body(Context &c)
 {
-    if (!is_luo(c)) return;
+    if (!is_ib(c)) return;
     {
         PhaseTimer t(c, "Calculate Force");
         launch_force(c);
@@ -183,7 +196,7 @@ static void phase_update_body(Context &c)
 
 static void record_step(Context &c, bool in_graph)
 {
-    if (is_luo(c)) {
+    if (is_ib(c)) {
         launch_copy(c, c.p_old, c.p, c.g.nP);    // _pre_step: pressure_old = pressure
         launch_copy(c, c.uold, c.u, c.g.nUV);    //            uold = u
         launch_body_pre_step(c);                 //            uB0 = uB, ...
@@ -295,10 +308,13 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         g.nUV = g.nU + g.nV;
         g.nP = g.nx * g.ny;
         c.has_body = c.body.total > 0 && c.P.solverType != ST_NAVIERSTOKES;
-        if (c.P.solverType != ST_NAVIERSTOKES && c.P.solverType != ST_LUO)
-            throw InputError("SolverType FADLUN / OSC_CYLINDER is not implemented by this build yet");
-        if (c.P.solverType == ST_LUO && c.body.total > 0 && (c.body.xCoeff != 0 || c.body.uCoeff != 0))
-            throw InputError("a moving body with the external method is not implemented by this build yet");
+        if (c.P.solverType == ST_OSC)
+            throw InputError("SolverType OSC_CYLINDER is not implemented by this build yet");
+        if ((c.P.solverType == ST_LUO || c.P.solverType == ST_FADLUN) && c.body.total > 0 &&
+            (c.body.xCoeff != 0 || c.body.uCoeff != 0))
+            throw InputError("a moving body with the external or Fadlun method is not implemented by this build yet");
+        if (c.P.solverType == ST_FADLUN && (c.P.krylovVelocity == KRYLOV_CG || c.P.krylovPoisson == KRYLOV_CG))
+            throw InputError("the Fadlun operators are not symmetric: use BICGSTAB (krylov: CG is for the other methods)");
         if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
             throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
         if (c.has_body) {
@@ -317,9 +333,17 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         upload_ns_tables(c);
         c.sys1.which = 1;
         c.sys2.which = 2;
+        if (c.has_body) setup_ib(c);
+        if (c.P.solverType == ST_FADLUN && c.has_body) {
+            // the Fadlun operators are assembled from the tags of the initial body
+            // position (fadlunModified::initialise), before the solvers are set up
+            c.timeStep = c.P.startStep;
+            initialise_body(c);
+            launch_tag_points(c);
+            setup_fadlun(c);
+        }
         setup_system(c, c.sys1);
         setup_system(c, c.sys2);
-        if (c.has_body) setup_ib(c);
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
         const char *ev = getenv("CUIBM_GRAPH");
         c.use_graph = !(ev && ev[0] == '0');
@@ -362,7 +386,7 @@ int cuibm_initialise(cuibm_ctx *h)
         if (c.has_body) {
             initialise_body(c);       // luo_base::initialise movement at t = dt*timeStep
             launch_tag_points(c);     // tagPoints()
-            launch_set_inside(c, c.u);  // luoIBM::zeroVelocity
+            if (c.P.solverType == ST_LUO) launch_set_inside(c, c.u);  // luoIBM::zeroVelocity
         }
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
         c.cfl_max = 0;
@@ -447,6 +471,10 @@ int cuibm_get_info(const cuibm_ctx *h, cuibm_info *info)
     const int nx = c.g.nx, ny = c.g.ny;
     info->nnz_lhs1 = (nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + (ny - 1) * nx * 5 - 2 * (ny - 1) - 2 * nx;
     info->nnz_lhs2 = 5 * nx * ny - 2 * ny - 2 * nx;
+    if (is_fadlun(c)) {
+        info->nnz_lhs1 = c.fadlun.nnz1;
+        info->nnz_lhs2 = c.fadlun.nnz2;
+    }
     info->velocity_precond = c.P.velocity.precond;
     info->poisson_precond = c.P.poisson.precond;
     info->velocity_krylov = c.P.krylovVelocity;
@@ -555,13 +583,17 @@ int cuibm_run(cuibm_ctx *h, int op)
             if (is_luo(c)) launch_ghost_velocity(c, c.uhat, true);
             phase_generate_rhs2(c);
             break;
-        case CUIBM_OP_RHS2: launch_rhs2(c, c.uhat); break;
+        case CUIBM_OP_RHS2:
+            if (is_fadlun(c)) launch_fadlun_rhs2(c); else launch_rhs2(c, c.uhat);
+            break;
         case CUIBM_OP_SOLVE_POISSON: phase_solve_poisson(c, false); break;
         case CUIBM_OP_WEIGHT_PRESSURE:
             need_ib();
             launch_ib_after_poisson(c);
             break;
-        case CUIBM_OP_PROJECT: launch_project(c); break;
+        case CUIBM_OP_PROJECT:
+            if (is_fadlun(c)) launch_fadlun_project(c); else launch_project(c);
+            break;
         case CUIBM_OP_PROJECT_VELOCITY: phase_project(c); break;
         case CUIBM_OP_UPDATE_BODY: need_ib(); phase_update_body(c); break;
         case CUIBM_OP_APPLY_LHS1: launch_apply(c, 1, c.work_x, c.work_y); break;

@@ -96,6 +96,13 @@ struct Op1D {
     template <class X>
     __device__ __forceinline__ double row_x(int i, double xi, const X &x) const
     {
+        if (c.patch.pid) {
+            const int k = c.patch.pid[i];
+            if (k >= 0) {
+                const double y = patch_row(c.patch, k, xi, x);
+                return w ? w[i] * y : y;
+            }
+        }
         const int wu = g.nx - 1;
         double y = diag[i] * xi;
         if (i < g.nU) {
@@ -126,6 +133,13 @@ struct Op2D {
     template <class X>
     __device__ __forceinline__ double row_x(int i, double xi, const X &x) const
     {
+        if (c.patch.pid) {
+            const int k = c.patch.pid[i];
+            if (k >= 0) {
+                const double y = patch_row(c.patch, k, xi, x);
+                return w ? w[i] * y : y;
+            }
+        }
         const int I = i % g.nx, J = i / g.nx;
         double y = diag[i] * xi;
         if (I != g.nx - 1) y -= c.E[I] * x(i + 1);

@@ -1024,7 +1024,7 @@ __global__ void __launch_bounds__(kIbThreads) k_ib_step(IbStep S, int phases)
 __device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx, int ncy, const double *u,
                                            const double *uold, const double *p, const int *gtags, double nu,
                                            const double *dx, const double *dy, double dt, double *part,
-                                           unsigned int *arrive, double *out)
+                                           unsigned int *arrive, double *out, double *comp)
 {
     const int nU = (nx - 1) * ny;
     double s[6] = {0, 0, 0, 0, 0, 0};
@@ -1100,6 +1100,8 @@ __device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx
             for (int k = 0; k < 6; ++k) t[k] += __ldcg(part + b * 6 + k);
         out[0] = t[0] + t[1] + t[2];
         out[1] = t[3] + t[4] + t[5];
+        if (comp)
+            for (int k = 0; k < 6; ++k) comp[k] = t[k];
         *arrive = 0;
     }
 }
@@ -1108,7 +1110,8 @@ __global__ void k_force(int nx, int ny, const int *bb, const double *u, const do
                         const int *gtags, double nu, const double *dx, const double *dy, double dt, double *part,
                         unsigned int *arrive, double *out)
 {
-    force_body(nx, ny, bb[0], bb[1], bb[2], bb[3], u, uold, p, gtags, nu, dx, dy, dt, part, arrive, out);
+    // the six sums (dragLeftRight, dragBottomTop, dragUnsteady, lift...) follow the force
+    force_body(nx, ny, bb[0], bb[1], bb[2], bb[3], u, uold, p, gtags, nu, dx, dy, dt, part, arrive, out, out + 2);
 }
 
 // k_force with the box passed by value (caller-owned arrays, no context)
@@ -1116,7 +1119,7 @@ __global__ void k_force_box(int nx, int ny, int I, int J, int ncx, int ncy, cons
                             const double *p, const int *gtags, double nu, const double *dx, const double *dy,
                             double dt, double *part, unsigned int *arrive, double *out)
 {
-    force_body(nx, ny, I, J, ncx, ncy, u, uold, p, gtags, nu, dx, dy, dt, part, arrive, out);
+    force_body(nx, ny, I, J, ncx, ncy, u, uold, p, gtags, nu, dx, dy, dt, part, arrive, out, nullptr);
 }
 
 // prescribed motion (luo_base/move.cu set_movement): x = xnew + offset, uB = unew with
@@ -1222,7 +1225,7 @@ void setup_ib(Context &c)
     b.bdx = c.carve<double>(nb);
     b.bdy = c.carve<double>(nb);
     b.motion = c.carve<double>(8);
-    b.forceOut = c.carve<double>(2);
+    b.forceOut = c.carve<double>(8);  // Fx, Fy, then the six partial sums
     const int fblocks = 64;
     b.forcePart = c.carve<double>(6 * fblocks);
 

@@ -7,7 +7,8 @@
 //   NNNNNNN/lambda   same, pressure
 //   NNNNNNN/bodies   src/bodies.cu:459-471 (body point coordinates)
 //   iterations       NavierStokesSolver.cu:350 (timeStep, velocity and Poisson iterations)
-//   forces           luoIBM.cu:76-78 (time, Fx, Fy)
+//   forces           luoIBM.cu:76-78 (time, Fx, Fy); fadlunModified.cu:64-78 (time, Fx,
+//                    FxX, FxY, FxU, Fy)
 //   midPosition      luo_base.cu:193-205 (timeStep, X, Y, U, V)
 #include <sys/stat.h>
 
@@ -76,11 +77,15 @@ void write_step_output(Context &c)
         }
     }
     if (c.has_body) {
-        double f[2] = {0, 0}, m[4] = {0, 0, 0, 0};
+        double f[8] = {0, 0, 0, 0, 0, 0, 0, 0}, m[4] = {0, 0, 0, 0};
         CUIBM_TRY(cudaMemcpyAsync(f, c.ib.forceOut, sizeof f, cudaMemcpyDeviceToHost, c.stream));
         CUIBM_TRY(cudaMemcpyAsync(m, c.ib.motion, sizeof m, cudaMemcpyDeviceToHost, c.stream));
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
-        if (c.forceFile) {
+        if (c.forceFile && c.P.solverType == ST_FADLUN) {
+            // fadlunModified.cu:64-78: time, Fx and its three parts, Fy
+            if (c.timeStep == 0) fprintf(c.forceFile, "timestep\tFx\tFxX\tFxY\tFxU\tFy\n");
+            fprintf(c.forceFile, "%g\t%g\t%g\t%g\t%g\t%g\n", c.timeStep * c.P.dt, f[0], f[2], f[3], f[4], f[1]);
+        } else if (c.forceFile) {
             if (c.timeStep == 1) fprintf(c.forceFile, "timestep\tFx\tFy\n");
             fprintf(c.forceFile, "%g\t%g\t%g\n", c.timeStep * c.P.dt, f[0], f[1]);
         }

@@ -17,6 +17,7 @@
 //   lhs1_row / lhs2_row   the COO matrices of LHS1.cu / LHS2.cu applied matrix-free
 //   k_init_velocity  initialise.cu;  k_cfl  CFL.cu
 #include <cmath>
+#include <algorithm>
 #include <vector>
 
 #include "operators.cuh"
@@ -301,11 +302,29 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
         col.push_back(cc);
         val.push_back(v);
     };
+    // a patched row of the modified Fadlun method: its entries in column order (the
+    // reference sorts its Fadlun matrices by row and column; zero entries dropped)
+    auto patched = [&](int i, const std::vector<int> &pid, const std::vector<int> &pcol,
+                       const std::vector<double> &pval, const std::vector<double> &pdiag) {
+        if (pid.empty() || pid[i] < 0) return false;
+        const int k = pid[i];
+        std::vector<std::pair<int, double>> e;
+        if (pdiag[k] != 0) e.push_back({i, pdiag[k]});
+        for (int m = 0; m < 5; ++m)
+            if (pcol[5 * k + m] >= 0) e.push_back({pcol[5 * k + m], pval[5 * k + m]});
+        std::sort(e.begin(), e.end(), [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
+            return a.first < b.first;
+        });
+        for (auto &q : e) push(i, q.first, q.second);
+        return true;
+    };
+    const auto &F = c.fadlun;
     if (which == 1) {
         const double *E = T("1uE"), *W = T("1uW"), *Nn = T("1uN"), *S = T("1uS");
         for (int J = 0; J < ny; ++J)
             for (int I = 0; I < nx - 1; ++I) {
                 int i = J * (nx - 1) + I;
+                if (patched(i, F.pid1, F.pcol1, F.pval1, F.pdiag1)) continue;
                 if (I != nx - 2) push(i, i + 1, -E[I]);
                 if (I != 0) push(i, i - 1, -W[I]);
                 if (J != ny - 1) push(i, i + nx - 1, -Nn[J]);
@@ -316,6 +335,7 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
         for (int J = 0; J < ny - 1; ++J)
             for (int I = 0; I < nx; ++I) {
                 int i = c.g.nU + J * nx + I;
+                if (patched(i, F.pid1, F.pcol1, F.pval1, F.pdiag1)) continue;
                 if (I != nx - 1) push(i, i + 1, -vE[I]);
                 if (I != 0) push(i, i - 1, -vW[I]);
                 if (J != ny - 2) push(i, i + nx, -vN[J]);
@@ -327,6 +347,7 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
         for (int J = 0; J < ny; ++J)
             for (int I = 0; I < nx; ++I) {
                 int i = J * nx + I;
+                if (patched(i, F.pid2, F.pcol2, F.pval2, F.pdiag2)) continue;
                 if (I != nx - 1) push(i, i + 1, -E[I]);
                 if (I != 0) push(i, i - 1, -W[I]);
                 if (J != ny - 1) push(i, i + nx, -Nn[J]);

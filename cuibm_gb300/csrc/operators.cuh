@@ -11,19 +11,26 @@ namespace cuibm {
 // ---------------------------------------------------------------------------
 // operator rows (device)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double lhs1_diag(const Lhs1Coef &c, const Grid &g, int i)
+// a patched row (RowPatch), the own value given
+template <class X>
+__device__ __forceinline__ double patch_row(const RowPatch &P, int k, double xi, const X &x)
 {
-    if (i < g.nU) {
-        int I = i % (g.nx - 1), J = i / (g.nx - 1);
-        return (((1 + c.uE[I]) + c.uW[I]) + c.uN[J]) + c.uS[J];
+    double y = P.pdiag[k] * xi;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        const int j = P.pcol[5 * k + m];
+        if (j >= 0) y += P.pval[5 * k + m] * x(j);
     }
-    int k = i - g.nU, I = k % g.nx, J = k / g.nx;
-    return (((1 + c.vE[I]) + c.vW[I]) + c.vN[J]) + c.vS[J];
+    return y;
 }
 
 template <class X>
 __device__ __forceinline__ double lhs1_row_f(const Lhs1Coef &c, const Grid &g, int i, const X &x)
 {
+    if (c.patch.pid) {
+        const int k = c.patch.pid[i];
+        if (k >= 0) return patch_row(c.patch, k, x(i), x);
+    }
     const int w = g.nx - 1;
     if (i < g.nU) {
         int I = i % w, J = i / w;
@@ -45,17 +52,13 @@ __device__ __forceinline__ double lhs1_row_f(const Lhs1Coef &c, const Grid &g, i
     return y;
 }
 
-__device__ __forceinline__ double lhs2_diag(const Lhs2Coef &c, const Grid &g, int i)
-{
-    int I = i % g.nx, J = i / g.nx;
-    double d = (((0 + c.E[I]) + c.W[I]) + c.N[J]) + c.S[J];
-    if (i == c.pin0 || i == c.pinc) d += d;
-    return d;
-}
-
 template <class X>
 __device__ __forceinline__ double lhs2_row_f(const Lhs2Coef &c, const Grid &g, int i, const X &x)
 {
+    if (c.patch.pid) {
+        const int k = c.patch.pid[i];
+        if (k >= 0) return patch_row(c.patch, k, x(i), x);
+    }
     int I = i % g.nx, J = i / g.nx;
     double d = (((0 + c.E[I]) + c.W[I]) + c.N[J]) + c.S[J];
     if (i == c.pin0 || i == c.pinc) d += d;

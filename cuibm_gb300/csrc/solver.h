@@ -35,16 +35,25 @@ inline int blocks_for(long n, int bs = kBlock) { return (int)((n + bs - 1) / bs)
 // 1-D coefficient tables of the separable 5-point operators.  Index ranges are
 // noted per array; every value is computed on the host with the reference's
 // formula and operation order.
+// Rows that replace the structured stencil (the modified Fadlun method's rows at
+// tagged nodes): row i with pid[i] = k >= 0 is pdiag[k] x_i + sum_m pval[5k+m] x_pcol[5k+m]
+// over the entries with pcol >= 0.  pid is null for the other methods.
+struct RowPatch {
+    const int *pid, *pcol;
+    const double *pval, *pdiag;
+};
 struct Lhs1Coef {
     // u rows: E/W depend on I (0..nx-2), N/S on J (0..ny-1, boundary spacing folded in)
     const double *uE, *uW, *uN, *uS;
     // v rows: E/W on I (0..nx-1), N/S on J (0..ny-2)
     const double *vE, *vW, *vN, *vS;
+    RowPatch patch;
 };
 struct Lhs2Coef {
     const double *E, *W;  // on I (0..nx-1), zero where the neighbour is missing
     const double *N, *S;  // on J (0..ny-1)
     int pin0, pinc;       // doubled diagonals: cell 0 and (if >= 0) the centre cell
+    RowPatch patch;
 };
 struct Grid {
     int nx, ny, nU, nV, nUV, nP;
@@ -191,6 +200,13 @@ struct Context {
     cudaGraph_t step_graph = nullptr;
     int static_kernels = 0;  // kernel nodes of the step graph outside the solver loops
 
+    // modified Fadlun: host copies of the patched rows (for the host matrices)
+    struct FadlunRows {
+        std::vector<int> pid1, pcol1, pid2, pcol2;
+        std::vector<double> pval1, pdiag1, pval2, pdiag2;
+        int nnz1 = 0, nnz2 = 0;  // entries of the matrices cuibm_get_matrix returns
+    } fadlun;
+
     // output files
     FILE *iterationsFile = nullptr, *forceFile = nullptr, *midPositionFile = nullptr;
 
@@ -231,6 +247,12 @@ void setup_fused(Context &c, LinearSystem &S);
 void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x);
 void set_fused_trace(Context &c, LinearSystem &S, bool on);
 double solve_bytes(const LinearSystem &S, int iterations);
+
+// fadlun.cu
+void setup_fadlun(Context &c);
+void launch_fadlun_rhs1(Context &c);
+void launch_fadlun_rhs2(Context &c);
+void launch_fadlun_project(Context &c);
 
 // amg.cu
 void build_sa_hierarchy(Context &c, LinearSystem &S);

@@ -372,6 +372,48 @@ def tag_points(g, bx, by, uB, vB, bb, midX, midY):
     return T
 
 
+# ---- modified Fadlun (oracle/fadlun.c) ------------------------------------------------
+def fadlun_lhs1_coo(g, dt, nu, T):
+    """fadlunModified::generateLHS1 before the reference's sort (unsorted COO)."""
+    row, col, val = lhs1_coo(g, dt, nu)
+    _sig("or_fadlun_lhs1_coo", _ip, _ip, _dp, INT, _ip, _ip, _ip, _dp, _dp, _dp, _dp, D, D, INT, INT)(
+        _i(row), _i(col), _d(val), len(row), _i(T.hybridTagsUV), _i(T.hybridTagsUV2), _i(T.ghostTagsUV),
+        _d(T.dist_node), _d(T.dist_between), _d(g.dx), _d(g.dy), dt, nu, g.nx, g.ny)
+    return row, col, val
+
+
+def fadlun_lhs2_coo(g, dt, T):
+    """fadlunModified::generateLHS2 before the reference's sort (unsorted COO)."""
+    row, col, val = lhs2_coo(g, dt, centre_pin=False)
+    _sig("or_fadlun_lhs2_coo", _ip, _ip, _dp, _dp, _dp, _ip, _ip, _dp, _dp, INT, INT, D)(
+        _i(row), _i(col), _d(val), _d(T.dist_u_body), _d(T.dist_v_body), _i(T.ghostTagsP), _i(T.hybridTagsP),
+        _d(g.dx), _d(g.dy), g.nx, g.ny, dt)
+    return row, col, val
+
+
+def fadlun_update_rhs1(rhs, T, g):
+    r = f64(rhs).copy()
+    _sig("or_fadlun_update_rhs1", _ip, _ip, _dp, _dp, _dp, _dp, INT, INT)(
+        _i(T.hybridTagsUV), _i(T.ghostTagsUV), _d(r), _d(T.dist_node), _d(T.dist_between), _d(T.uv), g.nx, g.ny)
+    return r
+
+
+def fadlun_rhs2(uhat, T, g, bc):
+    r = np.zeros(g.nP)
+    xm, xp, ym, yp = bc
+    _sig("or_fadlun_rhs2", _dp, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT)(
+        _d(r), _d(f64(uhat)), _i(T.ghostTagsP), _i(T.hybridTagsP), _d(T.dist_u_body), _d(T.dist_v_body), _d(ym),
+        _d(yp), _d(xm), _d(xp), _d(g.dx), _d(g.dy), g.nx, g.ny)
+    return r
+
+
+def fadlun_project(uhat, p, T, g, dt):
+    u = np.zeros(g.nUV)
+    _sig("or_fadlun_project", _dp, _dp, _dp, _ip, _dp, _dp, D, INT, INT)(
+        _d(u), _d(f64(uhat)), _d(f64(p)), _i(T.ghostTagsP), _d(g.dx), _d(g.dy), dt, g.nx, g.ny)
+    return u
+
+
 def ghost_velocity(direc, u, T, uB0, g, bb, set_=True):
     u = f64(u).copy()
     S = Stencils(g.nUV)
@@ -549,7 +591,9 @@ class LuoSolver:
         self.A2 = Csr(g.nP, *lhs2_coo(g, self.dt, centre_pin=False))
         self.solve = solve
         self.fx = self.fy = 0.0
-        if solve == "direct":
+        if solve == "none":  # a subclass assembles its own operators
+            pass
+        elif solve == "direct":
             import scipy.sparse.linalg as spla
             self._lu1 = spla.splu(self.A1.scipy().tocsc())
             self._lu2 = spla.splu(self.A2.scipy().tocsc())
@@ -619,6 +663,85 @@ class LuoSolver:
         u, _ = ghost_velocity(0, u, T, ub, g, bb)
         u, _ = ghost_velocity(1, u, T, vb, g, bb)
         self.u = set_inside(u, T, ub, vb, g)
+        # body update: control-volume force, then the prescribed motion at t = dt * timeStep
+        self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
+        xnew, unew = self.motion(self.timeStep)
+        self.bx = np.array([xnew + v for v in self.bdx])
+        self.uB = np.full(len(self.bx), unew)
+        self.midX = xnew
+        self.iters = (it1, it2)
+        self.timeStep += 1
+
+
+def csr_from_coo_summed(n, row, col, val):
+    """CSR with duplicate COO entries summed and explicit zeros dropped (the matrix the
+    reference's COO SpMV applies)."""
+    import scipy.sparse as sp
+    keep = f64(val) != 0  # zero entries, some with columns outside the matrix (LHS_mid_Y's 1 - nx)
+    A = sp.coo_matrix((f64(val)[keep], (np.asarray(row)[keep], np.asarray(col)[keep])), shape=(n, n)).tocsr()
+    A.sum_duplicates()
+    A.eliminate_zeros()
+    A.sort_indices()
+    C = Csr.__new__(Csr)
+    C.n = n
+    C.ptr = np.ascontiguousarray(A.indptr, np.int32)
+    C.col = np.ascontiguousarray(A.indices, np.int32)
+    C.val = np.ascontiguousarray(A.data, np.float64)
+    return C
+
+
+class FadlunSolver(LuoSolver):
+    """The modified Fadlun method on the CPU: luo_base::stepTime (luo_base.cu:208-233)
+    with fadlunModified's phases - generateRHS1 (FadlunModified/intermediateVelocity.cu:
+    15-38: Robin outflow, explicit terms, updateRHS1forIB), generateRHS2 and the solves
+    on the Fadlun LHS1/LHS2 assembled once from the initial tags (fadlunModified.cu:
+    48-62; updateSolver does not rebuild them), the masked projection
+    (fadlunModified.cu:109-127) and the body update (force, motion)."""
+
+    def __init__(self, folder, solve="direct"):
+        super().__init__(folder, solve="none")
+        g = self.g
+        # luo_base::initialise does not set the inside velocity for this method
+        f0 = load_case(folder)[1][0]
+        ip = f0.get("initialPerturbation", [0.0, 0.0])
+        self.u = initial_velocity(g, float(f0["initialVelocity"][0]), float(f0["initialVelocity"][1]),
+                                  float(ip[0]), float(ip[1]))
+        self.uhat = self.u.copy()
+        self.A1 = csr_from_coo_summed(g.nUV, *fadlun_lhs1_coo(g, self.dt, self.nu, self.T))
+        self.A2 = csr_from_coo_summed(g.nP, *fadlun_lhs2_coo(g, self.dt, self.T))
+        self.solve = solve
+        if solve == "direct":
+            import scipy.sparse.linalg as spla
+            self._lu1 = spla.splu(self.A1.scipy().tocsc())
+            self._lu2 = spla.splu(self.A2.scipy().tocsc())
+        else:
+            ls = {s["system"]: s for s in self.sim.get("linearSolvers", [])}
+            self.cfg = {k: (float(ls[k].get("tolerance", 1e-5)), int(ls[k].get("maxIterations", 10000)),
+                            _PC.get(ls[k].get("preconditioner", "DIAGONAL"), 1)) for k in ("velocity", "Poisson")}
+            self.amg1 = Amg(self.A1) if self.cfg["velocity"][2] == 2 else None
+            self.amg2 = Amg(self.A2) if self.cfg["Poisson"][2] == 2 else None
+
+    def step(self):
+        g, T, bb, dt = self.g, self.T, self.bb, self.dt
+        xm, xp, ym, yp = self.bc
+        # _pre_step
+        self.uold = self.u.copy()
+        self.uBk = self.uB.copy()
+        Nold = self.N
+        # generateRHS1
+        xp[:] = robin(self.u, xp, g, dt)
+        bc = (xm, xp, ym, yp)
+        self.N = generate_N(self.u, g, bc)
+        L = generate_L(self.u, g, bc, self.nu)
+        b1 = generate_bc1(self.u, g, bc, self.nu, dt)
+        rhs1 = generate_rhs(L, Nold, self.N, self.u, b1, dt)
+        rhs1 = fadlun_update_rhs1(rhs1, T, g)
+        self.uhat, it1 = self._solve(1, rhs1, self.uhat)
+        # generateRHS2, Poisson
+        rhs2 = fadlun_rhs2(self.uhat, T, g, bc)
+        self.p, it2 = self._solve(2, rhs2, self.p)
+        # masked projection
+        self.u = fadlun_project(self.uhat, self.p, T, g, dt)
         # body update: control-volume force, then the prescribed motion at t = dt * timeStep
         self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
         xnew, unew = self.motion(self.timeStep)

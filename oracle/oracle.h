@@ -114,6 +114,20 @@ void or_calculateForce(const double *u, const double *uold, const double *p, con
                        const double *dx, const double *dy, double dt, int nx, int ny, int I, int J, int ncx,
                        int ncy, double *fx, double *fy);
 
+/* ---- fadlun.c : FadlunModified kernels (modified Fadlun method) ---- */
+void or_fadlun_lhs1_coo(int *row, int *col, double *val, int nnz, const int *hyb, const int *hyb2, const int *ghost,
+                        const double *dn, const double *db, const double *dx, const double *dy, double dt,
+                        double nu, int nx, int ny);
+void or_fadlun_lhs2_coo(int *row, int *col, double *val, const double *du, const double *dv, const int *ghostP,
+                        const int *hybP, const double *dx, const double *dy, int nx, int ny, double dt);
+void or_fadlun_update_rhs1(const int *hyb, const int *ghost, double *rhs, const double *dn, const double *db,
+                           const double *uv, int nx, int ny);
+void or_fadlun_rhs2(double *rhs2, const double *uhat, const int *ghostP, const int *hybP, const double *du,
+                    const double *dv, const double *ym, const double *yp, const double *xm, const double *xp,
+                    const double *dx, const double *dy, int nx, int ny);
+void or_fadlun_project(double *u, const double *uhat, const double *p, const int *ghostP, const double *dx,
+                       const double *dy, double dt, int nx, int ny);
+
 #ifdef __cplusplus
 }
 #endif

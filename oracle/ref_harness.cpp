@@ -45,6 +45,10 @@ thread_local ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
 #include "solvers/NavierStokes/luoIBM/kernels/weight.h"
 #include "solvers/NavierStokes/FadlunModified/kernels/intermediateVelocity.h"
 #include "solvers/NavierStokes/FadlunModified/kernels/calculateForce.h"
+#include "solvers/NavierStokes/FadlunModified/kernels/LHS1.h"
+#include "solvers/NavierStokes/FadlunModified/kernels/LHS2.h"
+#include "solvers/NavierStokes/FadlunModified/kernels/intermediatePressure.h"
+#include "solvers/NavierStokes/FadlunModified/kernels/projectVelocity.h"
 
 namespace {
 const int BS = 256;
@@ -441,6 +445,61 @@ void ref_update_body_viv(double *Bx, double *uB, double *Bdx, double unew, doubl
         if (i >= totalPoints) return;
         kernels::update_body_viv(Bx, uB, Bdx, unew, midX, totalPoints);
     });
+}
+
+// ---- modified Fadlun (fadlunModified.cu, FadlunModified/*.cu) ----------------------------
+// fadlunModified::generateLHS1 on zero-initialised COO arrays (the reference's
+// cusp::coo_matrix resize value-initialises them): Fadlun mid rows, base boundary rows
+void ref_fadlun_lhs1(int *row, int *col, double *val, int nnz, int *hybridTagsUV, int *hybridTagsUV2,
+                     int *ghostTagsUV, double *dist_node, double *dist_between, double *dx, double *dy, double dt,
+                     double nu, int nx, int ny)
+{
+    for (int k = 0; k < nnz; ++k) row[k] = col[k] = 0, val[k] = 0;
+    int gU = grid_for((nx - 1) * ny), gV = grid_for(nx * (ny - 1));
+    launch(gU, BS, [&] { kernels::LHS_mid_X(row, col, val, hybridTagsUV, hybridTagsUV2, ghostTagsUV, dist_node,
+                                            dist_between, dx, dy, dt, nu, nx, ny); });
+    launch(gV, BS, [&] { kernels::LHS_mid_Y(row, col, val, hybridTagsUV, hybridTagsUV2, ghostTagsUV, dist_node,
+                                            dist_between, dx, dy, dt, nu, nx, ny); });
+    launch(gU, BS, [&] { kernels::LHS_BC_X(row, col, val, dx, dy, dt, nu, nx, ny); });
+    launch(gV, BS, [&] { kernels::LHS_BC_Y(row, col, val, dx, dy, dt, nu, nx, ny); });
+}
+
+// fadlunModified::generateLHS2: values filled with 0, Fadlun mid rows, base boundary rows
+void ref_fadlun_lhs2(int *row, int *col, double *val, int nnz, double *dist_u, double *dist_v, int *ghostTagsP,
+                     int *hybridTagsP, double *dx, double *dy, int nx, int ny, double dt)
+{
+    for (int k = 0; k < nnz; ++k) row[k] = col[k] = 0, val[k] = 0;
+    int g = grid_for(nx * ny);
+    launch(g, BS, [&] { kernels::LHS2_mid(row, col, val, dist_u, dist_v, ghostTagsP, hybridTagsP, dx, dy, nx, ny, dt); });
+    launch(g, BS, [&] { kernels::LHS2_BC(row, col, val, dx, dy, nx, ny, dt); });
+}
+
+// the IB part of fadlunModified::generateRHS1 (after generateRHS)
+void ref_fadlun_update_rhs1(int *hybridTagsUV, int *ghostTagsUV, double *rhs, double *dist_node,
+                            double *dist_between, double *uv, int nx, int ny)
+{
+    int gU = grid_for((nx - 1) * ny), gV = grid_for(nx * (ny - 1));
+    launch(gU, BS, [&] { kernels::updateRHS1forIBX(hybridTagsUV, ghostTagsUV, rhs, dist_node, dist_between, uv, nx, ny); });
+    launch(gV, BS, [&] { kernels::updateRHS1forIBY(hybridTagsUV, ghostTagsUV, rhs, dist_node, dist_between, uv, nx, ny); });
+}
+
+// fadlunModified::generateRHS2
+void ref_fadlun_rhs2(double *rhs2, double *uhat, int *ghostTagsP, int *hybridTagsP, int *ghostTagsUV,
+                     double *dist_u, double *dist_v, double *ym, double *yp, double *xm, double *xp, double *dx,
+                     double *dy, int nx, int ny)
+{
+    int g = grid_for(nx * ny);
+    launch(g, BS, [&] { kernels::intermediatePressure(rhs2, uhat, ghostTagsP, hybridTagsP, ghostTagsUV, dist_u,
+                                                      dist_v, ym, yp, xm, xp, dx, dy, nx, ny); });
+}
+
+// fadlunModified::_project_velocity
+void ref_fadlun_project(double *u, double *uhat, double *uold, double *p, int *ghostTagsP, double *dx, double *dy,
+                        double dt, int nx, int ny)
+{
+    int gU = grid_for((nx - 1) * ny), gV = grid_for(nx * (ny - 1));
+    launch(gU, BS, [&] { kernels::project_velocity_X(u, uhat, uold, p, ghostTagsP, dx, dt, nx, ny); });
+    launch(gV, BS, [&] { kernels::project_velocity_Y(u, uhat, uold, p, ghostTagsP, dy, dt, nx, ny); });
 }
 
 }  // extern "C"

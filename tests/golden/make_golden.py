@@ -330,11 +330,109 @@ def ib_case(K, IO, name, folder, rng, nu, dt, uB0=0.25, vB0=-0.15, uBk=0.2, vBk=
         nx, ny, (i0, j0, ncx, ncy), (gU > 0).sum(), (hU > 0).sum(), (gP > 0).sum(), (hP > 0).sum()))
 
 
+def fadlun_case(K, IO, name, folder, rng, nu, dt, scale=2.0):
+    """The modified-Fadlun kernels (fadlunModified.cu) on the tags of a circle: LHS1 and
+    LHS2 as the reference leaves them before its sort, the IB update of rhs1, rhs2
+    and the masked projection."""
+    nx, ny, G = ref_grid(IO, folder)
+    nU, nV = (nx - 1) * ny, nx * (ny - 1)
+    nUV, nP = nU + nV, nx * ny
+    X, Y, _ = ref_body(IO, folder)
+    n = len(X)
+    mx = 0.0
+    my = 0.0
+    for v in X:
+        mx += v
+    for v in Y:
+        my += v
+    mx /= n
+    my /= n
+    i0, j0, ncx, ncy = bounding_box(X, Y, G["x"], G["y"], scale)
+    bx = np.array([0.0 + (v - mx) for v in X])
+    by = Y.copy()
+    uB = np.zeros(n)
+    vB = np.zeros(n)
+    p_sized = {"ghostTagsP", "hybridTagsP", "distance_from_u_to_body", "distance_from_v_to_body",
+               "body_intercept_p_x", "body_intercept_p_y", "image_point_p_x", "image_point_p_y",
+               "x1_p", "y1_p", "x2_p", "y2_p"}
+    arr = {}
+    for f, _ in RefTagArrays._fields_:
+        size = nP if f in p_sized else nUV
+        arr[f] = np.zeros(size + 2 * max(nx, ny), np.int32 if "Tags" in f else np.float64)[:size].copy()
+    ta = RefTagArrays(**{f: (i(arr[f]) if "Tags" in f else d(arr[f])) for f, _ in RefTagArrays._fields_})
+    K.ref_tagPoints.argtypes = [ctypes.POINTER(RefTagArrays)] + [_dp] * 8 + [ctypes.c_int] * 7 + \
+        [ctypes.c_double, ctypes.c_double]
+    K.ref_tagPoints(ctypes.byref(ta), d(bx), d(by), d(uB), d(vB), d(G["xu"]), d(G["yu"]), d(G["xv"]), d(G["yv"]),
+                    i0, j0, ncx, ncy, nx, ny, n, 0.0, my)
+    out = {"nx": np.int32(nx), "ny": np.int32(ny), "nu": np.float64(nu), "dt": np.float64(dt),
+           "bb": np.array([i0, j0, ncx, ncy], np.int32), "bx": bx, "by": by, "midY": np.float64(my)}
+    out.update({"grid_" + k: v for k, v in G.items()})
+    for f in ("ghostTagsUV", "ghostTagsP", "hybridTagsUV", "hybridTagsP", "hybridTagsUV2",
+              "distance_from_intersection_to_node", "distance_between_nodes_at_IB", "uv",
+              "distance_from_u_to_body", "distance_from_v_to_body"):
+        out["tag_" + f] = arr[f].copy()
+    gU, hU, h2U, gP, hP = (arr[k] for k in ("ghostTagsUV", "hybridTagsUV", "hybridTagsUV2", "ghostTagsP",
+                                              "hybridTagsP"))
+    dn, db, uv = (arr[k] for k in ("distance_from_intersection_to_node", "distance_between_nodes_at_IB", "uv"))
+    du, dv = arr["distance_from_u_to_body"], arr["distance_from_v_to_body"]
+    nnz1 = (nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + (ny - 1) * nx * 5 - 2 * (ny - 1) - 2 * nx
+    r1, c1, v1 = np.zeros(nnz1, np.int32), np.zeros(nnz1, np.int32), np.zeros(nnz1)
+    K.ref_fadlun_lhs1.argtypes = [_ip, _ip, _dp, ctypes.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _dp, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_int, ctypes.c_int]
+    K.ref_fadlun_lhs1(i(r1), i(c1), d(v1), nnz1, i(hU), i(h2U), i(gU), d(dn), d(db), d(G["dx"]), d(G["dy"]), dt, nu,
+                      nx, ny)
+    out.update({"lhs1_row": r1, "lhs1_col": c1, "lhs1_val": v1})
+    nnz2 = 5 * nx * ny - 2 * ny - 2 * nx
+    r2, c2, v2 = np.zeros(nnz2, np.int32), np.zeros(nnz2, np.int32), np.zeros(nnz2)
+    K.ref_fadlun_lhs2.argtypes = [_ip, _ip, _dp, ctypes.c_int, _dp, _dp, _ip, _ip, _dp, _dp, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_double]
+    K.ref_fadlun_lhs2(i(r2), i(c2), d(v2), nnz2, d(du), d(dv), i(gP), i(hP), d(G["dx"]), d(G["dy"]), nx, ny, dt)
+    out.update({"lhs2_row": r2, "lhs2_col": c2, "lhs2_val": v2})
+    rhs1 = rng.standard_normal(nUV)
+    out["rhs1_in"] = rhs1.copy()
+    K.ref_fadlun_update_rhs1.argtypes = [_ip, _ip, _dp, _dp, _dp, _dp, ctypes.c_int, ctypes.c_int]
+    K.ref_fadlun_update_rhs1(i(hU), i(gU), d(rhs1), d(dn), d(db), d(uv), nx, ny)
+    out["rhs1_out"] = rhs1
+    uhat = 1.0 + 0.2 * rng.standard_normal(nUV)
+    bcs = {k: 1.0 + 0.1 * rng.standard_normal(2 * ny - 1 if k in ("xm", "xp") else 2 * nx - 1)
+           for k in ("xm", "xp", "ym", "yp")}
+    out["uhat_in"] = uhat
+    out.update({"bc_" + k: v for k, v in bcs.items()})
+    rhs2 = np.zeros(nP)
+    K.ref_fadlun_rhs2.argtypes = [_dp, _dp, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                  ctypes.c_int]
+    K.ref_fadlun_rhs2(d(rhs2), d(uhat), i(gP), i(hP), i(gU), d(du), d(dv), d(bcs["ym"]), d(bcs["yp"]),
+                      d(bcs["xm"]), d(bcs["xp"]), d(G["dx"]), d(G["dy"]), nx, ny)
+    out["rhs2"] = rhs2
+    p = 0.1 * rng.standard_normal(nP)
+    out["p_in"] = p
+    u = np.zeros(nUV)
+    uold = np.zeros(nUV)
+    K.ref_fadlun_project.argtypes = [_dp, _dp, _dp, _dp, _ip, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+    K.ref_fadlun_project(d(u), d(uhat), d(uold), d(p), i(gP), d(G["dx"]), d(G["dy"]), dt, nx, ny)
+    out["u_projected"] = u
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "nx=%d ny=%d ghostUV=%d hybridUV=%d ghostP=%d hybridP=%d" % (
+        nx, ny, (gU > 0).sum(), (hU > 0).sum(), (gP > 0).sum(), (hP > 0).sum()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
+    ap.add_argument("--only", default=None, help="generate one group: fadlun")
     a = ap.parse_args()
     K, IO = ref_libs(a.ref)
+    if a.only == "fadlun":
+        with tempfile.TemporaryDirectory() as tmp:
+            rng = np.random.default_rng(20261204)
+            f = os.path.join(tmp, "fad1")
+            cases.cylinder(f, h=0.05, ratio=1.1, extent=2.0, core=0.6, points=48, nu=0.02, dt=0.01, nt=1)
+            fadlun_case(K, IO, "fadlun_circle48", f, rng, nu=0.02, dt=0.01)
+            f = os.path.join(tmp, "fad2")
+            cases.cylinder(f, h=0.025, ratio=1.08, extent=2.5, core=0.7, points=101, nu=0.02, dt=0.005, nt=1,
+                           radius=0.43)
+            fadlun_case(K, IO, "fadlun_circle101", f, rng, nu=0.02, dt=0.005)
+        return
     rng = np.random.default_rng(20261203)
     with tempfile.TemporaryDirectory() as tmp:
         # stretched grid with all three sub-domain kinds in both directions
