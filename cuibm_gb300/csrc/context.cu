@@ -10,6 +10,7 @@
 // conditional nodes: one graph launch per step, no host synchronisation inside a
 // step.  cuibm_step checks the solver status once at the end of the call.
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <sys/stat.h>
@@ -188,8 +189,10 @@ static void phase_update_body(Context &c)
         launch_body_motion(c, -1.0);  // time taken from the device step counter
     }
     if (body_moves(c)) {
-        // a static body keeps its tags: re-tagging it reproduces them exactly
+        // updateSolver: the box of the moved body, then its tags (and the interpolation
+        // plan); a static body keeps its tags: re-tagging it reproduces them exactly
         PhaseTimer t(c, "Update Solver");
+        launch_body_box(c);
         launch_tag_points(c);
     }
 }
@@ -310,17 +313,30 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         c.has_body = c.body.total > 0 && c.P.solverType != ST_NAVIERSTOKES;
         if (c.P.solverType == ST_OSC)
             throw InputError("SolverType OSC_CYLINDER is not implemented by this build yet");
-        if ((c.P.solverType == ST_LUO || c.P.solverType == ST_FADLUN) && c.body.total > 0 &&
-            (c.body.xCoeff != 0 || c.body.uCoeff != 0))
-            throw InputError("a moving body with the external or Fadlun method is not implemented by this build yet");
         if (c.P.solverType == ST_FADLUN && (c.P.krylovVelocity == KRYLOV_CG || c.P.krylovPoisson == KRYLOV_CG))
             throw InputError("the Fadlun operators are not symmetric: use BICGSTAB (krylov: CG is for the other methods)");
         if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
             throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
         if (c.has_body) {
             c.bb = bounding_box(c.body.x.data(), c.body.y.data(), c.body.total, c.gx, c.gy, c.P.scaleCV);
-            if (c.bb.i0 < 6 || c.bb.j0 < 6 || c.bb.i0 + c.bb.ncx > g.nx - 7 || c.bb.j0 + c.bb.ncy > g.ny - 7)
-                throw InputError("the body's scaled bounding box reaches the domain boundary");
+            c.bb_tag = c.bb;
+            if (c.body.xCoeff != 0 || c.body.uCoeff != 0) {
+                // a prescribed motion x = xnew + (x0 - midX), |xnew| <= |xCoefficient|: tag
+                // over the box of the body at both ends of its travel (tags near the body
+                // do not depend on how far the scanned box reaches)
+                const int n = c.body.total;
+                const double a = std::fabs(c.body.xCoeff);
+                std::vector<double> xs(2 * n), ys(2 * n);
+                for (int k = 0; k < n; ++k) {
+                    xs[k] = -a + c.body.dxp[k];
+                    xs[n + k] = a + c.body.dxp[k];
+                    ys[k] = ys[n + k] = c.body.y[k];
+                }
+                c.bb_tag = bounding_box(xs.data(), ys.data(), 2 * n, c.gx, c.gy, c.P.scaleCV);
+            }
+            for (const BoundingBox &b : {c.bb, c.bb_tag})
+                if (b.i0 < 6 || b.j0 < 6 || b.i0 + b.ncx > g.nx - 7 || b.j0 + b.ncy > g.ny - 7)
+                    throw InputError("the body's scaled bounding box reaches the domain boundary");
         }
         CUIBM_TRY(cudaSetDevice(c.P.deviceNumber));
         c.device = c.P.deviceNumber;

@@ -51,6 +51,7 @@ struct TagGeom {
     int i0, j0, width, height, nthreads;
     int nx, ny, total;
     double midX, midY;
+    const double *motion;  // moving body: the centre is motion[0], motion[1] (set on the device)
 };
 
 __device__ __forceinline__ void intercept_dev(const double *bx, const double *by, int k, int l, double px,
@@ -99,7 +100,7 @@ __global__ void k_tag_velocity_records(TagGeom G, TagRecords R)
         return;
     }
     const double *bx = G.bx, *by = G.by, *vel = G.vel, *xc = G.xc, *yc = G.yc;
-    const double midX = G.midX, midY = G.midY;
+    const double midX = G.motion ? G.motion[0] : G.midX, midY = G.motion ? G.motion[1] : G.midY;
     int k = G.total - 1, l = 0;
     bool outsideX = true, outsideY = true, flag = false;
     int fX = -1, fY = -1, f2X = -1, f2Y = -1;
@@ -278,7 +279,7 @@ __global__ void k_tag_pressure_records(TagGeom G, TagRecords R)
         return;
     }
     const double *bx = G.bx, *by = G.by, *xv = G.xc, *yu = G.yc;
-    const double midX = G.midX, midY = G.midY;
+    const double midX = G.motion ? G.motion[0] : G.midX, midY = G.motion ? G.motion[1] : G.midY;
     int k = G.total - 1, l = 0;
     bool flag = false;
     double x, y, ix, iy;
@@ -1160,6 +1161,36 @@ __global__ void k_body_pre_step(int total, const double *uB, const double *vB, d
 
 __global__ void k_step_counter(int *s) { *s += 1; }
 
+// bodies::calculateBoundingBoxes (bodies.cu:257-293, 303-326): the box of the body
+// points scaled by scaleCV about its centre, in cell indices of the centre arrays
+// x, y; one thread (the reference's boundingBox kernel), bounded searches
+__global__ void k_body_box(int total, const double *bx, const double *by, const double *x, const double *y, int nx,
+                           int ny, double scale, int *bb)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double xmax = bx[0], xmin = bx[0], ymax = by[0], ymin = by[0];
+    for (int i = 1; i < total; ++i) {
+        xmax = bx[i] > xmax ? bx[i] : xmax;
+        xmin = bx[i] < xmin ? bx[i] : xmin;
+        ymax = by[i] > ymax ? by[i] : ymax;
+        ymin = by[i] < ymin ? by[i] : ymin;
+    }
+    const double ex = xmax - xmin, ey = ymax - ymin;
+    xmax += 0.5 * ex * (scale - 1.0);
+    xmin -= 0.5 * ex * (scale - 1.0);
+    ymax += 0.5 * ey * (scale - 1.0);
+    ymin -= 0.5 * ey * (scale - 1.0);
+    int i = 0, j = 0;
+    while (i + 1 < nx && x[i + 1] < xmin) i++;
+    while (j + 1 < ny && y[j + 1] < ymin) j++;
+    bb[0] = i;
+    bb[1] = j;
+    while (i < nx - 1 && x[i] < xmax) i++;
+    while (j < ny - 1 && y[j] < ymax) j++;
+    bb[2] = i - bb[0];
+    bb[3] = j - bb[1];
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -1215,7 +1246,8 @@ void setup_ib(Context &c)
     b.hCoef = c.carve<double>(4 * UV);
     b.gpCoef = c.carve<double>(4 * P);
     b.hpCoef = c.carve<double>(4 * P);
-    b.gnValue = c.carve<double>(std::max<size_t>(UV > P ? UV : P, 2 * (size_t)ref_threads(c.bb.ncx + 16, c.bb.ncy + 16)));
+    b.gnValue = c.carve<double>(
+        std::max<size_t>(UV > P ? UV : P, 2 * (size_t)ref_threads(c.bb_tag.ncx + 16, c.bb_tag.ncy + 16)));
     b.bx = c.carve<double>(nb);
     b.by = c.carve<double>(nb);
     b.uB = c.carve<double>(nb);
@@ -1239,7 +1271,7 @@ void setup_ib(Context &c)
     H.force_arrive = c.carve<unsigned int>(4);
     CUIBM_TRY(cudaMemsetAsync(H.force_arrive, 0, 4 * sizeof(unsigned int), c.stream));
     // records sized for the box, with room for the box to grow as the body moves
-    const int w = c.bb.ncx + 16, h = c.bb.ncy + 16;
+    const int w = c.bb_tag.ncx + 16, h = c.bb_tag.ncy + 16;
     H.rec.nrec = ref_threads(w, h);
     const size_t nr = H.rec.nrec;
     H.rec.flags = c.carve<int>(nr);
@@ -1301,7 +1333,7 @@ void setup_ib(Context &c)
 
 static BoxLaunch box(Context &c)
 {
-    return BoxLaunch{c.bb.i0, c.bb.j0, c.bb.ncx, ref_threads(c.bb.ncx, c.bb.ncy)};
+    return BoxLaunch{c.bb_tag.i0, c.bb_tag.j0, c.bb_tag.ncx, ref_threads(c.bb_tag.ncx, c.bb_tag.ncy)};
 }
 
 // luo_base::initialise body part (luo_base.cu:48-86): positions and velocities at
@@ -1343,15 +1375,15 @@ void launch_tag_points(Context &c)
     IbHost &H = hostside(c);
     IbArrays &b = c.ib;
     const int nx = c.g.nx, ny = c.g.ny;
-    const int w = c.bb.ncx, h = c.bb.ncy, nthreads = ref_threads(w, h);
+    const int w = c.bb_tag.ncx, h = c.bb_tag.ncy, nthreads = ref_threads(w, h);
     if (nthreads > H.rec.nrec) throw InputError("the body's box outgrew the tagging records");
     const int nfill = c.g.nUV > c.g.nP ? c.g.nUV : c.g.nP;
     k_tag_fill<<<blocks_for(nfill), kBlock, 0, c.stream>>>(c.g.nUV, c.g.nP, b.ghostUV, b.hybridUV, b.hybrid2UV,
                                                           b.distNode, b.distBetween, b.biX, b.biY, b.ipX, b.ipY,
                                                           b.ghostP, b.hybridP);
     // midX is the body's current centre abscissa (the prescribed xnew), midY its centroid
-    TagGeom G{b.bx, b.by, b.uB, c.xu, c.yu, c.bb.i0, c.bb.j0, w, h, nthreads, nx, ny, c.body.total, c.ib_midX,
-              c.ib_midY};
+    TagGeom G{b.bx, b.by, b.uB, c.xu, c.yu, c.bb_tag.i0, c.bb_tag.j0, w, h, nthreads, nx, ny, c.body.total, c.ib_midX,
+              c.ib_midY, H.moving ? b.motion : nullptr};
     TagOut O{b.ghostUV, b.hybridUV, b.hybrid2UV, b.distNode, b.distBetween, b.uvBody, b.biX, b.biY, b.ipX, b.ipY,
              b.distU};
     const int rows = (nthreads + w - 1) / w;
@@ -1369,7 +1401,7 @@ void launch_tag_points(Context &c)
     TagOut OP{b.ghostP, b.hybridP, nullptr, nullptr, nullptr, nullptr, b.bipX, b.bipY, b.ippX, b.ippY, nullptr};
     k_tag_pressure_records<<<blocks_for(nthreads), kBlock, 0, c.stream>>>(G, H.rec);
     k_tag_resolve<2><<<blocks_for(nres), kBlock, 0, c.stream>>>(G, H.rec, OP);
-    const int i0 = c.bb.i0, i1 = c.bb.i0 + w, j0 = c.bb.j0, j1 = c.bb.j0 + h;
+    const int i0 = c.bb_tag.i0, i1 = c.bb_tag.i0 + w, j0 = c.bb_tag.j0, j1 = c.bb_tag.j0 + h;
     const int zrows = ref_threads(i1 - i0, 1);
     k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostP, nx, i0, i1, j0, j1, zrows, nx);
     k_zero_rows<<<blocks_for(zrows), kBlock, 0, c.stream>>>(b.ghostUV, nx - 1, i0, i1, j0, j1, zrows, nx - 1);
@@ -1441,6 +1473,14 @@ void launch_body_pre_step(Context &c)
 void launch_step_counter(Context &c) { k_step_counter<<<1, 1, 0, c.stream>>>(c.step_counter_dev); }
 
 bool body_moves(Context &c) { return c.has_body && hostside(c).moving; }
+
+// updateSolver: the control-volume box of the moved body (the force of the next step uses it)
+void launch_body_box(Context &c)
+{
+    k_body_box<<<1, 32, 0, c.stream>>>(c.body.total, c.ib.bx, c.ib.by, c.x, c.y, c.g.nx, c.g.ny, c.P.scaleCV,
+                                        hostside(c).bb);
+    CUIBM_TRY(cudaGetLastError());
+}
 
 // ---- control-volume force without allocation -------------------------------------
 // The scratch of k_force (6 partial sums per block, then an arrival counter) as a

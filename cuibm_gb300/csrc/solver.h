@@ -150,7 +150,9 @@ struct Context {
     Params P;
     Axis gx, gy;
     BodyState body;
-    BoundingBox bb;
+    BoundingBox bb;      // control-volume box of the initial body (the force's box until the body moves)
+    BoundingBox bb_tag;  // the box the tagging and interpolation scan: bb, or for a moving body a box
+                         // holding every position of its prescribed motion
     Grid g{};
     int device = 0;
     cudaStream_t stream = nullptr, side_stream = nullptr;
@@ -280,6 +282,7 @@ void launch_force(Context &c);
 void launch_body_motion(Context &c, double t);
 void launch_body_pre_step(Context &c);
 bool body_moves(Context &c);
+void launch_body_box(Context &c);
 void launch_step_counter(Context &c);
 void initialise_body(Context &c);
 

@@ -362,8 +362,16 @@ class Stencils:
                        q3coef=_d(self.coef[2]), q4coef=_d(self.coef[3]), value=_d(self.value), dpdn=_d(self.dpdn))
 
 
-def tag_points(g, bx, by, uB, vB, bb, midX, midY):
+# arrays luo_base::tagPoints does not refill (luo_base/tagPoints.cu:26-40): a re-tagging
+# keeps their values where the kernels do not write
+_TAG_CARRIED = ("dist_u_body", "dist_v_body", "uv", "bip_x", "bip_y", "ipp_x", "ipp_y")
+
+
+def tag_points(g, bx, by, uB, vB, bb, midX, midY, prev=None):
     T = Tags(g)
+    if prev is not None:
+        for k in _TAG_CARRIED:
+            setattr(T, k, getattr(prev, k).copy())
     ct = T.c()
     i0, j0, ncx, ncy = (int(v) for v in bb)
     _sig("or_tagPoints", ctypes.POINTER(_Tags), _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
@@ -573,7 +581,8 @@ class LuoSolver:
         mx /= n
         my /= n
         self.bdx = np.array([v - mx for v in X])
-        self.bb = bounding_box(X, Y, g, float(self.sim.get("scaleCV", 2.0)))
+        self.scale = float(self.sim.get("scaleCV", 2.0))
+        self.bb = bounding_box(X, Y, g, self.scale)
         self.coef = {k: float(b0.get(k, 0.0)) for k in ("xCoefficient", "uCoefficient", "xPhase", "uPhase",
                                                          "xfrequency")}
         self.timeStep = 0
@@ -604,6 +613,17 @@ class LuoSolver:
             self.amg1 = Amg(self.A1) if self.cfg["velocity"][2] == 2 else None
             self.amg2 = Amg(self.A2) if self.cfg["Poisson"][2] == 2 else None
         self.iters = (0, 0)
+
+    @property
+    def moving(self):
+        return self.coef["xCoefficient"] != 0 or self.coef["uCoefficient"] != 0
+
+    def _update_solver(self):
+        """luo_base::updateSolver (luo_base.cu:137-146): the box of the moved body, its tags."""
+        if not self.moving:
+            return
+        self.bb = bounding_box(self.bx, self.by, self.g, self.scale)
+        self.T = tag_points(self.g, self.bx, self.by, self.uB, self.vB, self.bb, self.midX, self.midY, prev=self.T)
 
     def motion(self, step):
         c = self.coef
@@ -669,6 +689,7 @@ class LuoSolver:
         self.bx = np.array([xnew + v for v in self.bdx])
         self.uB = np.full(len(self.bx), unew)
         self.midX = xnew
+        self._update_solver()
         self.iters = (it1, it2)
         self.timeStep += 1
 
@@ -748,5 +769,6 @@ class FadlunSolver(LuoSolver):
         self.bx = np.array([xnew + v for v in self.bdx])
         self.uB = np.full(len(self.bx), unew)
         self.midX = xnew
+        self._update_solver()
         self.iters = (it1, it2)
         self.timeStep += 1
