@@ -326,7 +326,7 @@ class _Tags(ctypes.Structure):
 
 class _Interp(ctypes.Structure):
     _fields_ = [(n, _ip) for n in ("index1", "index2", "index3", "index4")] + \
-               [(n, _dp) for n in ("q1coef", "q2coef", "q3coef", "q4coef", "value", "dpdn")]
+               [(n, _dp) for n in ("q1coef", "q2coef", "q3coef", "q4coef", "value", "dpdn", "q1", "q2", "q3", "q4")]
 
 
 class Tags:
@@ -355,11 +355,13 @@ class Stencils:
         self.coef = np.zeros((4, n))
         self.value = np.zeros(n)
         self.dpdn = np.zeros(n)
+        self.q = np.zeros((4, n))
 
     def c(self):
         return _Interp(index1=_i(self.index[0]), index2=_i(self.index[1]), index3=_i(self.index[2]),
                        index4=_i(self.index[3]), q1coef=_d(self.coef[0]), q2coef=_d(self.coef[1]),
-                       q3coef=_d(self.coef[2]), q4coef=_d(self.coef[3]), value=_d(self.value), dpdn=_d(self.dpdn))
+                       q3coef=_d(self.coef[2]), q4coef=_d(self.coef[3]), value=_d(self.value), dpdn=_d(self.dpdn),
+                       q1=_d(self.q[0]), q2=_d(self.q[1]), q3=_d(self.q[2]), q4=_d(self.q[3]))
 
 
 # arrays luo_base::tagPoints does not refill (luo_base/tagPoints.cu:26-40): a re-tagging
@@ -422,9 +424,86 @@ def fadlun_project(uhat, p, T, g, dt):
     return u
 
 
-def ghost_velocity(direc, u, T, uB0, g, bb, set_=True):
+# ---- embedded method (oracle/embedded.c) ----------------------------------------------
+def _plain_nnz(g, system):
+    nx, ny = g.nx, g.ny
+    if system == 1:
+        return (nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + nx * (ny - 1) * 5 - 2 * nx - 2 * (ny - 1)
+    return nx * ny * 5 - 2 * nx - 2 * ny
+
+
+def iter_alpha(kind, T, g, bb, alpha=None):
+    """alpha_u (kind 0), alpha_v (1), alpha_p (2) of luo_iter/kernels/weight.cu into alpha."""
+    n = g.nP if kind == 2 else g.nUV
+    alpha = np.zeros(n) if alpha is None else alpha
+    i0, j0, ncx, _ = (int(v) for v in bb)
+    if kind == 2:
+        gt, ht, xc, yc, bix, biy = T.ghostTagsP, T.hybridTagsP, g.xv, g.yu, T.bip_x, T.bip_y
+    else:
+        gt, ht, bix, biy = T.ghostTagsUV, T.hybridTagsUV, T.bi_x, T.bi_y
+        xc, yc = (g.xu, g.yu) if kind == 0 else (g.xv, g.yv)
+    _sig("or_iter_alpha", INT, _dp, _ip, _ip, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT)(
+        kind, _d(alpha), _i(gt), _i(ht), _d(yc), _d(xc), _d(bix), _d(biy), i0, j0, ncx, g.nx, g.ny)
+    return alpha
+
+
+def iter_lhs1(g, dt, nu, T, S, alpha, uB0, vB0, bb):
+    """The embedded LHS1 (luo_iter::intermediate_velocity_size_lhs/_calculate_lhs) on zeroed
+    arrays: unsorted COO, ns_rhs and interp_rhs.  S: the velocity stencils of the step."""
+    nh = int((T.hybridTagsUV > 0).sum())
+    nnz = _plain_nnz(g, 1) + nh
+    row, col, val = np.zeros(nnz, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+    ns, interp, count = np.zeros(g.nUV), np.zeros(g.nUV), np.zeros(g.nUV, np.int32)
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    ix = [np.ascontiguousarray(S.index[k]) for k in range(4)]
+    cf = [np.ascontiguousarray(S.coef[k]) for k in range(4)]
+    qs = [np.ascontiguousarray(S.q[k]) for k in range(4)]
+    got = _sig("or_iter_lhs1", _ip, _ip, _dp, INT, _dp, _dp, D, D, INT, INT, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _ip,
+               _ip, _dp, D, D, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, restype=INT)(
+        _i(row), _i(col), _d(val), nnz, _d(g.dx), _d(g.dy), dt, nu, g.nx, g.ny, _i(T.hybridTagsUV),
+        _i(T.ghostTagsUV), _d(ns), _d(interp), _i(count), *(_i(a) for a in ix), _d(f64(alpha)), uB0, vB0,
+        *(_d(a) for a in cf), *(_d(a) for a in qs), i0, j0, ncx, ncy)
+    if got != nnz:
+        raise RuntimeError("or_iter_lhs1: %d entries, expected %d" % (got, nnz))
+    return row, col, val, ns, interp
+
+
+def iter_update_rhs1(rhs1, ns, interp, g):
+    r = f64(rhs1).copy()
+    _sig("or_iter_update_rhs1", _dp, _dp, _dp, INT, INT)(_d(r), _d(f64(ns)), _d(f64(interp)), g.nx, g.ny)
+    return r
+
+
+def iter_lhs2(g, dt, T, S, alpha, bb):
+    """The embedded LHS2 (luo_iter::poisson_size_lhs/_calculate_lhs) on zeroed arrays:
+    unsorted COO, ns_rhs and interp_rhs.  S: the pressure stencils of the step (dpdn too)."""
+    nh = int((T.hybridTagsP > 0).sum())
+    nnz = _plain_nnz(g, 2) + nh
+    row, col, val = np.zeros(nnz, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+    ns, interp, count = np.zeros(g.nP), np.zeros(g.nP), np.zeros(g.nP, np.int32)
+    i0, j0, ncx, ncy = (int(v) for v in bb)
+    ix = [np.ascontiguousarray(S.index[k]) for k in range(4)]
+    cf = [np.ascontiguousarray(S.coef[k]) for k in range(4)]
+    qs = [np.ascontiguousarray(S.q[k]) for k in range(4)]
+    got = _sig("or_iter_lhs2", _ip, _ip, _dp, INT, _dp, _dp, INT, INT, D, _ip, _dp, _dp, _ip, _ip, _dp, _dp, _ip, _ip,
+               _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, restype=INT)(
+        _i(row), _i(col), _d(val), nnz, _d(g.dx), _d(g.dy), g.nx, g.ny, dt, _i(count), _d(ns), _d(interp),
+        _i(T.hybridTagsP), _i(T.ghostTagsP), _d(f64(alpha)), _d(S.dpdn), *(_i(a) for a in ix),
+        *(_d(a) for a in cf), *(_d(a) for a in qs), i0, j0, ncx, ncy)
+    if got != nnz:
+        raise RuntimeError("or_iter_lhs2: %d entries, expected %d" % (got, nnz))
+    return row, col, val, ns, interp
+
+
+def iter_update_rhs2(rhs2, ns, interp, g):
+    r = f64(rhs2).copy()
+    _sig("or_iter_update_rhs2", _dp, _dp, _dp, INT, INT)(_d(r), _d(f64(ns)), _d(f64(interp)), g.nx, g.ny)
+    return r
+
+
+def ghost_velocity(direc, u, T, uB0, g, bb, set_=True, S=None):
     u = f64(u).copy()
-    S = Stencils(g.nUV)
+    S = Stencils(g.nUV) if S is None else S
     cs = S.c()
     xc, yc = (g.xu, g.yu) if direc == 0 else (g.xv, g.yv)
     i0, j0, ncx, ncy = (int(v) for v in bb)
@@ -434,9 +513,9 @@ def ghost_velocity(direc, u, T, uB0, g, bb, set_=True):
     return u, S
 
 
-def hybrid_velocity(direc, u, ustar, T, uB0, g, bb):
+def hybrid_velocity(direc, u, ustar, T, uB0, g, bb, S=None):
     ustar = f64(ustar).copy()
-    S = Stencils(g.nUV)
+    S = Stencils(g.nUV) if S is None else S
     cs = S.c()
     xc, yc = (g.xu, g.yu) if direc == 0 else (g.xv, g.yv)
     i0, j0, ncx, ncy = (int(v) for v in bb)
@@ -447,9 +526,9 @@ def hybrid_velocity(direc, u, ustar, T, uB0, g, bb):
     return ustar, S
 
 
-def hybrid_pressure(p, T, dudt, dvdt, g, bb):
+def hybrid_pressure(p, T, dudt, dvdt, g, bb, S=None):
     pstar = np.zeros(g.nP)
-    S = Stencils(g.nP)
+    S = Stencils(g.nP) if S is None else S
     cs = S.c()
     i0, j0, ncx, ncy = (int(v) for v in bb)
     _sig("or_hybrid_pressure", _dp, _dp, _ip, D, D, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,
@@ -459,9 +538,9 @@ def hybrid_pressure(p, T, dudt, dvdt, g, bb):
     return pstar, S
 
 
-def ghost_pressure(p, T, dudt, dvdt, g, bb, set_=True):
+def ghost_pressure(p, T, dudt, dvdt, g, bb, set_=True, S=None):
     p = f64(p).copy()
-    S = Stencils(g.nP)
+    S = Stencils(g.nP) if S is None else S
     cs = S.c()
     i0, j0, ncx, ncy = (int(v) for v in bb)
     _sig("or_ghost_pressure", _dp, INT, _ip, D, D, _dp, _dp, _dp, _dp, _dp, _dp, INT, INT, INT, INT, INT, INT,

@@ -415,10 +415,11 @@ static void weights_at(const double b[16], double det, double px, double py, dou
     for (int c = 0; c < 4; ++c) w[c] = (b[c] + b[4 + c] * px + b[8 + c] * py + b[12 + c] * px * py) / det;
 }
 
-static void store_stencil(or_interp *R, int n, const int idx[4], const double w[4])
+static void store_stencil(or_interp *R, int n, const int idx[4], const double w[4], const double q[4])
 {
     R->index1[n] = idx[0]; R->index2[n] = idx[1]; R->index3[n] = idx[2]; R->index4[n] = idx[3];
     R->q1coef[n] = w[0]; R->q2coef[n] = w[1]; R->q3coef[n] = w[2]; R->q4coef[n] = w[3];
+    if (R->q1) { R->q1[n] = q[0]; R->q2[n] = q[1]; R->q3[n] = q[2]; R->q4[n] = q[3]; }
 }
 
 static int threads_for(int width, int height) { return ((int)((double)width * height - 0.5) / 256 + 1) * 256; }
@@ -473,7 +474,7 @@ void or_ghost_velocity(int dir, double *u, int set, const int *ghostTagsUV, doub
         double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
         double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
         weights_at(b, det, ip_x[n], ip_y[n], w);
-        store_stencil(R, n, id, w);
+        store_stencil(R, n, id, w, q);
         double val = a0 + a1 * ip_x[n] + a2 * ip_y[n] + a3 * ip_x[n] * ip_y[n];
         R->value[n] = val;
         if (set) u[n] = 2 * uB0 - val;
@@ -517,7 +518,7 @@ void or_hybrid_velocity(int dir, const double *u, double *ustar, const int *hybr
         double a2 = (b[8] * q[0] + b[9] * q[1] + b[10] * q[2] + b[11] * q[3]) / det;
         double a3 = (b[12] * q[0] + b[13] * q[1] + b[14] * q[2] + b[15] * q[3]) / det;
         weights_at(b, det, xc[I], yc[J], w);
-        store_stencil(R, n, id, w);
+        store_stencil(R, n, id, w, q);
         ustar[n] = a0 + a1 * xc[I] + a2 * yc[J] + a3 * yc[J] * xc[I];
         R->value[n] = a0 + a1 * ip_x[n] + a2 * ip_y[n] + a3 * ip_x[n] * ip_y[n];
     }
@@ -560,7 +561,7 @@ void or_hybrid_pressure(const double *p, double *pstar, const int *hybridTagsP, 
         double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
         double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
         weights_at(b, det, xv[I], yu[J], w);
-        store_stencil(R, ip, id, w);
+        store_stencil(R, ip, id, w, q);
         pstar[ip] = a0 + a1 * xv[I] + a2 * yu[J] + a3 * xv[I] * yu[J];
     }
 }
@@ -618,7 +619,7 @@ void or_ghost_pressure(double *p, int set, const int *ghostTagsP, double dudt_u,
         double a2 = b[8] / det * q[0] + b[9] / det * q[1] + b[10] / det * q[2] + b[11] / det * q[3];
         double a3 = b[12] / det * q[0] + b[13] / det * q[1] + b[14] / det * q[2] + b[15] / det * q[3];
         weights_at(b, det, ipp_x[ip], ipp_y[ip], w);
-        store_stencil(R, ip, id, w);
+        store_stencil(R, ip, id, w, q);
         double ipv = a0 + a1 * ipp_x[ip] + a2 * ipp_y[ip] + a3 * ipp_y[ip] * ipp_x[ip];
         R->value[ip] = a0 + a1 * bip_x[ip] + a2 * bip_y[ip] + a3 * bip_x[ip] * bip_y[ip];
         R->dpdn[ip] = sqrt(pow(ipp_x[ip] - xv[I], 2) + pow(ipp_y[ip] - yu[J], 2)) * matD;

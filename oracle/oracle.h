@@ -83,6 +83,7 @@ typedef struct {
     double *q1coef, *q2coef, *q3coef, *q4coef;
     double *value; /* image_point_u (velocity) or body_intercept_p (pressure ghost) */
     double *dpdn;  /* pressure ghost only */
+    double *q1, *q2, *q3, *q4; /* the corner values the fit used (field or substituted body values) */
 } or_interp;
 
 void or_tagPoints(or_tags *T, const double *bx, const double *by, const double *uB, const double *vB,
@@ -127,6 +128,24 @@ void or_fadlun_rhs2(double *rhs2, const double *uhat, const int *ghostP, const i
                     const double *dx, const double *dy, int nx, int ny);
 void or_fadlun_project(double *u, const double *uhat, const double *p, const int *ghostP, const double *dx,
                        const double *dy, double dt, int nx, int ny);
+
+/* ---- embedded.c : luo_iter kernels (embedded method, SolverType OSC_CYLINDER) ---- */
+void or_iter_alpha(int kind, double *alpha, const int *ghost, const int *hybrid, const double *yc, const double *xc,
+                   const double *bix, const double *biy, int i_start, int j_start, int width, int nx, int ny);
+int or_iter_lhs1(int *row, int *col, double *val, int nnz, const double *dx, const double *dy, double dt, double nu,
+                 int nx, int ny, const int *hyb, const int *ghost, double *ns_rhs, double *interp_rhs, int *count,
+                 const int *i1, const int *i2, const int *i3, const int *i4, const double *alpha, double uB0,
+                 double vB0, const double *c1, const double *c2, const double *c3, const double *c4,
+                 const double *q1, const double *q2, const double *q3, const double *q4, int i_start, int j_start,
+                 int width, int height);
+void or_iter_update_rhs1(double *rhs1, const double *ns_rhs, const double *interp_rhs, int nx, int ny);
+int or_iter_lhs2(int *row, int *col, double *val, int nnz, const double *dx, const double *dy, int nx, int ny,
+                 double dt, int *count, double *ns_rhs, double *interp_rhs, const int *hyb, const int *ghost,
+                 const double *alpha, const double *dpdn, const int *i1, const int *i2, const int *i3, const int *i4,
+                 const double *c1, const double *c2, const double *c3, const double *c4, const double *q1,
+                 const double *q2, const double *q3, const double *q4, int i_start, int j_start, int width,
+                 int height);
+void or_iter_update_rhs2(double *rhs2, const double *ns_rhs, const double *interp_rhs, int nx, int ny);
 
 #ifdef __cplusplus
 }

@@ -49,6 +49,11 @@ thread_local ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
 #include "solvers/NavierStokes/FadlunModified/kernels/LHS2.h"
 #include "solvers/NavierStokes/FadlunModified/kernels/intermediatePressure.h"
 #include "solvers/NavierStokes/FadlunModified/kernels/projectVelocity.h"
+#include "solvers/NavierStokes/luo_iter/kernels/LHS1.h"
+#include "solvers/NavierStokes/luo_iter/kernels/LHS2.h"
+#include "solvers/NavierStokes/luo_iter/kernels/intermediateVelocity.h"
+#include "solvers/NavierStokes/luo_iter/kernels/pressure.h"
+#include "solvers/NavierStokes/luo_iter/kernels/weight.h"
 
 namespace {
 const int BS = 256;
@@ -500,6 +505,97 @@ void ref_fadlun_project(double *u, double *uhat, double *uold, double *p, int *g
     int gU = grid_for((nx - 1) * ny), gV = grid_for(nx * (ny - 1));
     launch(gU, BS, [&] { kernels::project_velocity_X(u, uhat, uold, p, ghostTagsP, dx, dt, nx, ny); });
     launch(gV, BS, [&] { kernels::project_velocity_Y(u, uhat, uold, p, ghostTagsP, dy, dt, nx, ny); });
+}
+
+// ---- embedded method (luo_iter.cu, luo_iter/*.cu) -------------------------------------
+// alpha_u (kind 0), alpha_v (1), alpha_p (2) on the reference's grid, running only the
+// threads whose node lies in the grid (the others read past the arrays)
+void ref_iter_alpha(int kind, double *alpha, int *ghost, int *hybrid, double *yc, double *xc, double *bix,
+                    double *biy, double *ipx, double *ipy, int i_start, int j_start, int width, int nx, int ny)
+{
+    const int nU = (nx - 1) * ny;
+    const int g = grid_for(kind == 2 ? nx * ny : nU);
+    blockDim = {(unsigned)BS, 1, 1};
+    gridDim = {(unsigned)g, 1, 1};
+    for (int b = 0; b < g; ++b)
+        for (int t = 0; t < BS; ++t) {
+            const int idx = b * BS + t, I = i_start + idx % width, J = j_start + idx / width;
+            if (kind == 0 && (J >= ny || I >= nx - 1)) continue;
+            if (kind == 1 && (J * nx + I > nx * (ny - 1) || J >= ny - 1)) continue;
+            if (kind == 2 && (J * nx + I > nx * ny || J >= ny)) continue;
+            blockIdx = {(unsigned)b, 0, 0};
+            threadIdx = {(unsigned)t, 0, 0};
+            if (kind == 0)
+                kernels::alpha_u(alpha, ghost, hybrid, yc, xc, bix, biy, ipx, ipy, &i_start, &j_start, width, nx, ny);
+            else if (kind == 1)
+                kernels::alpha_v(alpha, ghost, hybrid, yc, xc, bix, biy, ipx, ipy, &i_start, &j_start, width, nx, ny);
+            else
+                kernels::alpha_p(alpha, ghost, hybrid, yc, xc, bix, biy, ipx, ipy, &i_start, &j_start, width, nx, ny);
+        }
+}
+
+// intermediate_velocity_size_lhs + intermediate_velocity_calculate_lhs on zeroed arrays of nnz
+// entries; returns the reference's nnz (plain + max count)
+int ref_iter_lhs1(int *row, int *col, double *val, int nnz, double *dx, double *dy, double dt, double nu, int nx,
+                  int ny, int *hyb, int *ghost, double *ns_rhs, double *interp_rhs, int *count, int *i1, int *i2,
+                  int *i3, int *i4, double *xu, double *yu, double *xv, double *yv, double *alpha, double *uB,
+                  double *vB, double *c1, double *c2, double *c3, double *c4, double *q1, double *q2, double *q3,
+                  double *q4, int i_start, int j_start, int width, int height)
+{
+    const int nUV = (nx - 1) * ny + nx * (ny - 1);
+    for (int k = 0; k < nUV; ++k) count[k] = 0;
+    launch(1, 1, [&] { kernels::size_LHS1(hyb, count, &i_start, &j_start, width, height, nx, ny); });
+    int mx = 0;
+    for (int k = 0; k < nUV; ++k) mx = count[k] > mx ? count[k] : mx;
+    const int need = (nx - 1) * ny * 5 - 2 * (nx - 1) - ny * 2 + nx * (ny - 1) * 5 - 2 * nx - 2 * (ny - 1) + mx;
+    if (need > nnz) return -need;
+    for (int k = 0; k < need; ++k) row[k] = col[k] = 0, val[k] = 0;
+    int gU = grid_for((nx - 1) * ny), gV = grid_for(nx * (ny - 1));
+    launch(gU, BS, [&] { kernels::LHS1_mid_iter_X(row, col, val, dx, dy, dt, nu, nx, ny, hyb, ghost, ns_rhs,
+                                                  interp_rhs, count, i1, i2, i3, i4, xu, yu, alpha, uB, c1, c2, c3,
+                                                  c4, q1, q2, q3, q4); });
+    launch(gV, BS, [&] { kernels::LHS1_mid_iter_Y(row, col, val, dx, dy, dt, nu, nx, ny, hyb, ghost, ns_rhs,
+                                                  interp_rhs, count, i1, i2, i3, i4, xv, yv, alpha, vB, c1, c2, c3,
+                                                  c4, q1, q2, q3, q4); });
+    launch(gU, BS, [&] { kernels::LHS_BC_X(row, col, val, dx, dy, dt, nu, nx, ny); });
+    launch(gV, BS, [&] { kernels::LHS_BC_Y(row, col, val, dx, dy, dt, nu, nx, ny); });
+    return need;
+}
+
+// intermediate_velocity_update_rhs (both kernels on the u grid)
+void ref_iter_update_rhs1(double *rhs1, double *ns_rhs, double *interp_rhs, int nx, int ny)
+{
+    int gU = grid_for((nx - 1) * ny);
+    launch(gU, BS, [&] { kernels::update_rhs1_x(rhs1, ns_rhs, interp_rhs, nx, ny); });
+    launch(gU, BS, [&] { kernels::update_rhs1_y(rhs1, ns_rhs, interp_rhs, nx, ny); });
+}
+
+// poisson_size_lhs + poisson_calculate_lhs
+int ref_iter_lhs2(int *row, int *col, double *val, int nnz, double *dx, double *dy, int nx, int ny, double dt,
+                  int *count, double *ns_rhs, double *interp_rhs, int *hyb, int *ghost, double *alpha, double *dpdn,
+                  int *i1, int *i2, int *i3, int *i4, double *c1, double *c2, double *c3, double *c4, double *q1,
+                  double *q2, double *q3, double *q4, int i_start, int j_start, int width, int height)
+{
+    for (int k = 0; k < nx * ny; ++k) count[k] = 0;
+    launch(1, 1, [&] { kernels::size_LHS2(hyb, count, &i_start, &j_start, width, height, nx, ny); });
+    int mx = 0;
+    for (int k = 0; k < nx * ny; ++k) mx = count[k] > mx ? count[k] : mx;
+    const int need = nx * ny * 5 - 2 * nx - ny * 2 + mx;
+    if (need > nnz) return -need;
+    for (int k = 0; k < need; ++k) row[k] = col[k] = 0, val[k] = 0;
+    int g = grid_for(nx * ny);
+    launch(g, BS, [&] { kernels::LHS2_mid_iter(row, col, val, dx, dy, nx, ny, dt, count, ns_rhs, interp_rhs, hyb,
+                                               ghost, alpha, dpdn, i1, i2, i3, i4, c1, c2, c3, c4, q1, q2, q3, q4,
+                                               1); });
+    launch(g, BS, [&] { kernels::LHS2_BC(row, col, val, dx, dy, nx, ny, dt); });
+    return need;
+}
+
+// poisson_update_rhs
+void ref_iter_update_rhs2(double *rhs2, double *ns_rhs, double *interp_rhs, int nx, int ny)
+{
+    int g = grid_for(nx * ny);
+    launch(g, BS, [&] { kernels::update_rhs2(rhs2, ns_rhs, interp_rhs, nx, ny); });
 }
 
 }  // extern "C"

@@ -416,10 +416,154 @@ def fadlun_case(K, IO, name, folder, rng, nu, dt, scale=2.0):
         nx, ny, (gU > 0).sum(), (hU > 0).sum(), (gP > 0).sum(), (hP > 0).sum()))
 
 
+def iter_case(K, IO, name, folder, rng, nu, dt, uB0=0.25, vB0=-0.15, uBk=0.2, vBk=-0.1, scale=2.0):
+    """The embedded method's per-step kernels (luo_iter/*.cu) on the tags of a circle:
+    alpha, the velocity and pressure stencils of the set = false interpolations, LHS1
+    and LHS2 on zeroed arrays (unsorted), ns_rhs, interp_rhs and the rhs updates.  The
+    body velocity differs from its previous value so that the dp/dn terms are pinned."""
+    nx, ny, G = ref_grid(IO, folder)
+    nU, nV = (nx - 1) * ny, nx * (ny - 1)
+    nUV, nP = nU + nV, nx * ny
+    X, Y, _ = ref_body(IO, folder)
+    n = len(X)
+    mx = 0.0
+    my = 0.0
+    for v in X:
+        mx += v
+    for v in Y:
+        my += v
+    mx /= n
+    my /= n
+    i0, j0, ncx, ncy = bounding_box(X, Y, G["x"], G["y"], scale)
+    bx = np.array([0.0 + (v - mx) for v in X])
+    by = Y.copy()
+    uB, vB = np.full(n, uB0), np.full(n, vB0)
+    p_sized = {"ghostTagsP", "hybridTagsP", "distance_from_u_to_body", "distance_from_v_to_body",
+               "body_intercept_p_x", "body_intercept_p_y", "image_point_p_x", "image_point_p_y",
+               "x1_p", "y1_p", "x2_p", "y2_p"}
+    arr = {}
+    for f, _ in RefTagArrays._fields_:
+        size = nP if f in p_sized else nUV
+        arr[f] = np.zeros(size + 2 * max(nx, ny), np.int32 if "Tags" in f else np.float64)[:size].copy()
+    ta = RefTagArrays(**{f: (i(arr[f]) if "Tags" in f else d(arr[f])) for f, _ in RefTagArrays._fields_})
+    K.ref_tagPoints.argtypes = [ctypes.POINTER(RefTagArrays)] + [_dp] * 8 + [ctypes.c_int] * 7 + \
+        [ctypes.c_double, ctypes.c_double]
+    K.ref_tagPoints(ctypes.byref(ta), d(bx), d(by), d(uB), d(vB), d(G["xu"]), d(G["yu"]), d(G["xv"]), d(G["yv"]),
+                    i0, j0, ncx, ncy, nx, ny, n, 0.0, my)
+    out = {"nx": np.int32(nx), "ny": np.int32(ny), "nu": np.float64(nu), "dt": np.float64(dt),
+           "bb": np.array([i0, j0, ncx, ncy], np.int32), "bx": bx, "by": by, "uB": uB, "vB": vB,
+           "uBk": np.float64(uBk), "vBk": np.float64(vBk), "midY": np.float64(my)}
+    out.update({"grid_" + k: v for k, v in G.items()})
+    gU, hU, gP, hP = (arr[k] for k in ("ghostTagsUV", "hybridTagsUV", "ghostTagsP", "hybridTagsP"))
+    bix, biy, ipx, ipy = (arr[k] for k in ("body_intercept_x", "body_intercept_y", "image_point_x", "image_point_y"))
+    bpx, bpy, ppx, ppy = (arr[k] for k in ("body_intercept_p_x", "body_intercept_p_y", "image_point_p_x",
+                                           "image_point_p_y"))
+    for f in ("ghostTagsUV", "ghostTagsP", "hybridTagsUV", "hybridTagsP"):
+        out["tag_" + f] = arr[f].copy()
+
+    def interp_arrays(size):
+        a = {f: np.zeros(size, np.int32 if f.startswith("index") else np.float64) for f, _ in RefInterpArrays._fields_}
+        r = RefInterpArrays(**{f: (i(a[f]) if f.startswith("index") else d(a[f])) for f, _ in RefInterpArrays._fields_})
+        return a, r
+
+    stencil = ("index1", "index2", "index3", "index4", "q1coef", "q2coef", "q3coef", "q4coef", "q1", "q2", "q3", "q4")
+    u = 1.0 + 0.2 * rng.standard_normal(nUV)
+    out["u_in"] = u.copy()
+    # luo_iter::intermediate_velocity_interpolation_setup: four set = false launches
+    # into one set of stencil arrays
+    a, r = interp_arrays(nUV)
+    K.ref_interpolateVelocityToGhostNode.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip] + [_dp] * 9 + \
+        [ctypes.c_int] * 6 + [ctypes.POINTER(RefInterpArrays)]
+    K.ref_interpolateVelocityToHybridNode.argtypes = [ctypes.c_int, _dp, _dp, _ip] + [_dp] * 9 + \
+        [ctypes.c_int] * 6 + [ctypes.POINTER(RefInterpArrays)]
+    for direc, (xc, yc, vel) in enumerate(((G["xu"], G["yu"], uB), (G["xv"], G["yv"], vB))):
+        K.ref_interpolateVelocityToGhostNode(direc, d(u), 0, i(gU), d(bx), d(by), d(vel), d(yc), d(xc), d(bix),
+                                             d(biy), d(ipx), d(ipy), i0, j0, ncx, ncy, nx, ny, ctypes.byref(r))
+    ustar = np.zeros(nUV)
+    for direc, (xc, yc, vel) in enumerate(((G["xu"], G["yu"], uB), (G["xv"], G["yv"], vB))):
+        K.ref_interpolateVelocityToHybridNode(direc, d(u), d(ustar), i(hU), d(bx), d(by), d(vel), d(yc), d(xc),
+                                              d(bix), d(biy), d(ipx), d(ipy), i0, j0, ncx, ncy, nx, ny,
+                                              ctypes.byref(r))
+    for f in stencil:
+        out["vel_" + f] = a[f].copy()
+    K.ref_iter_alpha.argtypes = [ctypes.c_int, _dp, _ip, _ip] + [_dp] * 6 + [ctypes.c_int] * 5
+    alpha = np.zeros(nUV)
+    K.ref_iter_alpha(0, d(alpha), i(gU), i(hU), d(G["yu"]), d(G["xu"]), d(bix), d(biy), d(ipx), d(ipy), i0, j0, ncx,
+                     nx, ny)
+    K.ref_iter_alpha(1, d(alpha), i(gU), i(hU), d(G["yv"]), d(G["xv"]), d(bix), d(biy), d(ipx), d(ipy), i0, j0, ncx,
+                     nx, ny)
+    out["alpha_uv"] = alpha.copy()
+    nnz1 = (nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + nx * (ny - 1) * 5 - 2 * nx - 2 * (ny - 1) + int((hU > 0).sum())
+    r1, c1, v1 = np.zeros(nnz1, np.int32), np.zeros(nnz1, np.int32), np.zeros(nnz1)
+    ns1, in1, cnt1 = np.zeros(nUV), np.zeros(nUV), np.zeros(nUV, np.int32)
+    K.ref_iter_lhs1.argtypes = [_ip, _ip, _dp, ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _ip, _ip] + \
+        [_dp] * 15 + [ctypes.c_int] * 4
+    K.ref_iter_lhs1.restype = ctypes.c_int
+    got = K.ref_iter_lhs1(i(r1), i(c1), d(v1), nnz1, d(G["dx"]), d(G["dy"]), dt, nu, nx, ny, i(hU), i(gU), d(ns1),
+                          d(in1), i(cnt1), i(a["index1"]), i(a["index2"]), i(a["index3"]), i(a["index4"]),
+                          d(G["xu"]), d(G["yu"]), d(G["xv"]), d(G["yv"]), d(alpha), d(uB), d(vB), d(a["q1coef"]),
+                          d(a["q2coef"]), d(a["q3coef"]), d(a["q4coef"]), d(a["q1"]), d(a["q2"]), d(a["q3"]),
+                          d(a["q4"]), i0, j0, ncx, ncy)
+    assert got == nnz1, (got, nnz1)
+    out.update({"lhs1_row": r1, "lhs1_col": c1, "lhs1_val": v1, "ns_rhs1": ns1, "interp_rhs1": in1})
+    rhs1 = rng.standard_normal(nUV)
+    out["rhs1_in"] = rhs1.copy()
+    K.ref_iter_update_rhs1.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int]
+    K.ref_iter_update_rhs1(d(rhs1), d(ns1), d(in1), nx, ny)
+    out["rhs1_out"] = rhs1
+    # luo_iter::poisson_interpolation_setup: stencil arrays zeroed, then the ghost
+    # (set = false, dp/dn) and hybrid pressure launches
+    p = 0.1 * rng.standard_normal(nP)
+    out["p_in"] = p.copy()
+    uBk_a, vBk_a = np.full(n, uBk), np.full(n, vBk)
+    a, r = interp_arrays(nUV)
+    dpdn, bip = np.zeros(nP), np.zeros(nP)
+    K.ref_interpolatePressureToGhostNode.argtypes = [_dp, ctypes.c_int, _dp, _ip, _dp, _dp, _dp] + [_dp] * 12 + \
+        [_dp] + [ctypes.c_int] * 6 + [ctypes.c_double, ctypes.POINTER(RefInterpArrays)]
+    K.ref_interpolatePressureToGhostNode(d(p), 0, d(u), i(gP), d(bx), d(by), d(dpdn), d(uB), d(uBk_a), d(vB),
+                                         d(vBk_a), d(G["yu"]), d(G["yv"]), d(G["xu"]), d(G["xv"]), d(bpx), d(bpy),
+                                         d(ppx), d(ppy), d(bip), i0, j0, ncx, ncy, nx, ny, dt, ctypes.byref(r))
+    K.ref_interpolatePressureToHybridNode.argtypes = [_dp, _dp, _dp, _ip] + [_dp] * 14 + [ctypes.c_int] * 6 + \
+        [ctypes.c_double, ctypes.POINTER(RefInterpArrays)]
+    pstar = np.zeros(nP)
+    K.ref_interpolatePressureToHybridNode(d(p), d(pstar), d(u), i(hP), d(bx), d(by), d(uB), d(uBk_a), d(vB),
+                                          d(vBk_a), d(G["yu"]), d(G["yv"]), d(G["xu"]), d(G["xv"]), d(bpx), d(bpy),
+                                          d(ppx), d(ppy), i0, j0, ncx, ncy, nx, ny, dt, ctypes.byref(r))
+    for f in stencil:
+        out["p_" + f] = a[f][:nP].copy()
+    out["dpdn"] = dpdn.copy()
+    alpha_p = np.zeros(nP)
+    K.ref_iter_alpha(2, d(alpha_p), i(gP), i(hP), d(G["yu"]), d(G["xv"]), d(bpx), d(bpy), d(ppx), d(ppy), i0, j0,
+                     ncx, nx, ny)
+    out["alpha_p"] = alpha_p.copy()
+    nnz2 = nx * ny * 5 - 2 * nx - 2 * ny + int((hP > 0).sum())
+    r2, c2, v2 = np.zeros(nnz2, np.int32), np.zeros(nnz2, np.int32), np.zeros(nnz2)
+    ns2, in2, cnt2 = np.zeros(nP), np.zeros(nP), np.zeros(nP, np.int32)
+    K.ref_iter_lhs2.argtypes = [_ip, _ip, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                _ip, _dp, _dp, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _ip] + [_dp] * 8 + \
+        [ctypes.c_int] * 4
+    K.ref_iter_lhs2.restype = ctypes.c_int
+    got = K.ref_iter_lhs2(i(r2), i(c2), d(v2), nnz2, d(G["dx"]), d(G["dy"]), nx, ny, dt, i(cnt2), d(ns2), d(in2),
+                          i(hP), i(gP), d(alpha_p), d(dpdn), i(a["index1"]), i(a["index2"]), i(a["index3"]),
+                          i(a["index4"]), d(a["q1coef"]), d(a["q2coef"]), d(a["q3coef"]), d(a["q4coef"]), d(a["q1"]),
+                          d(a["q2"]), d(a["q3"]), d(a["q4"]), i0, j0, ncx, ncy)
+    assert got == nnz2, (got, nnz2)
+    out.update({"lhs2_row": r2, "lhs2_col": c2, "lhs2_val": v2, "ns_rhs2": ns2, "interp_rhs2": in2})
+    rhs2 = rng.standard_normal(nP)
+    out["rhs2_in"] = rhs2.copy()
+    K.ref_iter_update_rhs2.argtypes = [_dp, _dp, _dp, ctypes.c_int, ctypes.c_int]
+    K.ref_iter_update_rhs2(d(rhs2), d(ns2), d(in2), nx, ny)
+    out["rhs2_out"] = rhs2
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "nx=%d ny=%d ghostUV=%d hybridUV=%d ghostP=%d hybridP=%d" % (
+        nx, ny, (gU > 0).sum(), (hU > 0).sum(), (gP > 0).sum(), (hP > 0).sum()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
-    ap.add_argument("--only", default=None, help="generate one group: fadlun")
+    ap.add_argument("--only", default=None, help="generate one group: fadlun, iter")
     a = ap.parse_args()
     K, IO = ref_libs(a.ref)
     if a.only == "fadlun":
@@ -432,6 +576,17 @@ def main():
             cases.cylinder(f, h=0.025, ratio=1.08, extent=2.5, core=0.7, points=101, nu=0.02, dt=0.005, nt=1,
                            radius=0.43)
             fadlun_case(K, IO, "fadlun_circle101", f, rng, nu=0.02, dt=0.005)
+        return
+    if a.only == "iter":
+        with tempfile.TemporaryDirectory() as tmp:
+            rng = np.random.default_rng(20261205)
+            f = os.path.join(tmp, "it1")
+            cases.cylinder(f, h=0.05, ratio=1.1, extent=2.0, core=0.6, points=48, nu=0.02, dt=0.01, nt=1)
+            iter_case(K, IO, "iter_circle48", f, rng, nu=0.02, dt=0.01)
+            f = os.path.join(tmp, "it2")
+            cases.cylinder(f, h=0.025, ratio=1.08, extent=2.5, core=0.7, points=101, nu=0.02, dt=0.005, nt=1,
+                           radius=0.43)
+            iter_case(K, IO, "iter_circle101", f, rng, nu=0.02, dt=0.005, uB0=0.1, vB0=0.05, uBk=0.1, vBk=0.05)
         return
     rng = np.random.default_rng(20261203)
     with tempfile.TemporaryDirectory() as tmp:
