@@ -34,6 +34,7 @@ UNITS = {
     "amg.cu": [],
     "fused_solve.cu": [],
     "fadlun.cu": ["-fmad=false"],
+    "embedded.cu": ["-fmad=false"],
     "ib_kernels.cu": ["-fmad=false"],
 }
 

@@ -133,7 +133,8 @@ struct PhaseTimer {
 // ---- phases ---------------------------------------------------------------------
 static bool is_luo(const Context &c) { return c.P.solverType == ST_LUO && c.has_body; }
 static bool is_fadlun(const Context &c) { return c.P.solverType == ST_FADLUN && c.has_body; }
-static bool is_ib(const Context &c) { return is_luo(c) || is_fadlun(c); }
+static bool is_embedded(const Context &c) { return c.P.solverType == ST_OSC && c.has_body; }
+static bool is_ib(const Context &c) { return is_luo(c) || is_fadlun(c) || is_embedded(c); }
 
 static void phase_generate_rhs1(Context &c)
 {
@@ -141,7 +142,8 @@ static void phase_generate_rhs1(Context &c)
     // updateRobinBoundary, rhs1GNInterpolation, zeroVelocity, rhs1HNInterpolation
     if (is_luo(c)) launch_ib_rhs1(c);
     if (is_fadlun(c)) launch_robin(c);
-    launch_rhs1(c, false);
+    if (is_embedded(c)) launch_ib_robin_inside(c);  // updateRobinBoundary, setInsideVelocity
+    launch_rhs1(c, false);  // with the embedded method's update_rhs1_x/y
     if (is_fadlun(c)) launch_fadlun_rhs1(c);  // updateRHS1forIBX/Y
 }
 
@@ -174,7 +176,7 @@ static void phase_project(Context &c)
         return;
     }
     launch_project(c);
-    if (is_luo(c)) launch_ib_after_projection(c);  // ghost u, zeroVelocity
+    if (is_luo(c) || is_embedded(c)) launch_ib_after_projection(c);  // ghost u, inside velocity
 }
 
 static void phase_update_body(Context &c)
@@ -311,10 +313,13 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         g.nUV = g.nU + g.nV;
         g.nP = g.nx * g.ny;
         c.has_body = c.body.total > 0 && c.P.solverType != ST_NAVIERSTOKES;
-        if (c.P.solverType == ST_OSC)
-            throw InputError("SolverType OSC_CYLINDER is not implemented by this build yet");
-        if (c.P.solverType == ST_FADLUN && (c.P.krylovVelocity == KRYLOV_CG || c.P.krylovPoisson == KRYLOV_CG))
-            throw InputError("the Fadlun operators are not symmetric: use BICGSTAB (krylov: CG is for the other methods)");
+        if ((c.P.solverType == ST_FADLUN || c.P.solverType == ST_OSC) &&
+            (c.P.krylovVelocity == KRYLOV_CG || c.P.krylovPoisson == KRYLOV_CG))
+            throw InputError("the Fadlun and embedded operators are not symmetric: use BICGSTAB (krylov: CG is for "
+                             "the other methods)");
+        if (c.has_body && c.P.VIV != 0)
+            throw InputError("simulation VIV (flow-induced body motion) is not implemented by this build; "
+                             "prescribed motion (VIV: 0) is");
         if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
             throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
         if (c.has_body) {
@@ -357,6 +362,14 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
             initialise_body(c);
             launch_tag_points(c);
             setup_fadlun(c);
+        }
+        if (c.P.solverType == ST_OSC && c.has_body) {
+            // the embedded operators' rows of the initial tags, before the solvers (and the
+            // SA hierarchy, built from these rows) are set up
+            setup_embedded(c);
+            c.timeStep = c.P.startStep;
+            initialise_body(c);
+            launch_tag_points(c);
         }
         setup_system(c, c.sys1);
         setup_system(c, c.sys2);
@@ -490,6 +503,17 @@ int cuibm_get_info(const cuibm_ctx *h, cuibm_info *info)
     if (is_fadlun(c)) {
         info->nnz_lhs1 = c.fadlun.nnz1;
         info->nnz_lhs2 = c.fadlun.nnz2;
+    }
+    if (is_embedded(c)) {  // size_LHS1 / size_LHS2: one extra slot per hybrid node
+        // the plan's node counts live on the device: read them on the context's stream
+        Context &cm = const_cast<Context &>(c);
+        try {
+            info->nnz_lhs1 += embedded_hybrid_count(cm, 1);
+            info->nnz_lhs2 += embedded_hybrid_count(cm, 2);
+        } catch (const CudaError &e) {
+            cm.err = e.msg;
+            return CUIBM_ERR_CUDA;
+        }
     }
     info->velocity_precond = c.P.velocity.precond;
     info->poisson_precond = c.P.poisson.precond;

@@ -104,20 +104,24 @@ struct Op1D {
             }
         }
         const int wu = g.nx - 1;
-        double y = diag[i] * xi;
+        // embedded method: the off-diagonal part is scaled by rscale (diag[i] carries it
+        // already); the other methods sum the row in the order of lhs1_row_f
+        const double *rs = c.rscale;
+        double o = rs ? 0.0 : diag[i] * xi;
         if (i < g.nU) {
             const int I = i % wu, J = i / wu;
-            if (I != g.nx - 2) y -= c.uE[I] * x(i + 1);
-            if (I != 0) y -= c.uW[I] * x(i - 1);
-            if (J != g.ny - 1) y -= c.uN[J] * x(i + wu);
-            if (J != 0) y -= c.uS[J] * x(i - wu);
+            if (I != g.nx - 2) o -= c.uE[I] * x(i + 1);
+            if (I != 0) o -= c.uW[I] * x(i - 1);
+            if (J != g.ny - 1) o -= c.uN[J] * x(i + wu);
+            if (J != 0) o -= c.uS[J] * x(i - wu);
         } else {
             const int k = i - g.nU, I = k % g.nx, J = k / g.nx;
-            if (I != g.nx - 1) y -= c.vE[I] * x(i + 1);
-            if (I != 0) y -= c.vW[I] * x(i - 1);
-            if (J != g.ny - 2) y -= c.vN[J] * x(i + g.nx);
-            if (J != 0) y -= c.vS[J] * x(i - g.nx);
+            if (I != g.nx - 1) o -= c.vE[I] * x(i + 1);
+            if (I != 0) o -= c.vW[I] * x(i - 1);
+            if (J != g.ny - 2) o -= c.vN[J] * x(i + g.nx);
+            if (J != 0) o -= c.vS[J] * x(i - g.nx);
         }
+        const double y = rs ? diag[i] * xi + o * rs[i] : o;
         return w ? w[i] * y : y;
     }
 };
@@ -910,6 +914,17 @@ struct Op2Plain {
     }
 };
 
+// the operator diagonal the persistent solver's rows use (rows may change when a body moves)
+void refresh_fused_diag(Context &c, LinearSystem &S)
+{
+    if (!S.diag) return;
+    if (S.which == 1)
+        k_fused_diag<<<blocks_for(S.n), kBlock, 0, c.stream>>>(Op1Plain{c.l1, c.g}, S.n, S.diag);
+    else
+        k_fused_diag<<<blocks_for(S.n), kBlock, 0, c.stream>>>(Op2Plain{c.l2, c.g}, S.n, S.diag);
+    CUIBM_TRY(cudaGetLastError());
+}
+
 template <class Op>
 static void *pick_kernel(int precond, int krylov)
 {
@@ -1071,11 +1086,7 @@ void setup_fused(Context &c, LinearSystem &S)
     S.fsync = c.carve<FusedSyncState>(1);
     S.diag = c.carve<double>(n);
     CUIBM_TRY(cudaMemsetAsync(S.fsync, 0, sizeof(FusedSyncState), c.stream));
-    if (S.which == 1)
-        k_fused_diag<<<blocks_for(n), kBlock, 0, c.stream>>>(Op1Plain{c.l1, c.g}, n, S.diag);
-    else
-        k_fused_diag<<<blocks_for(n), kBlock, 0, c.stream>>>(Op2Plain{c.l2, c.g}, n, S.diag);
-    CUIBM_TRY(cudaGetLastError());
+    refresh_fused_diag(c, S);
     S.winv = nullptr;
     if (S.w) {
         std::vector<double> w(n), wi(n);

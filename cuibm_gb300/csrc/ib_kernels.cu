@@ -27,6 +27,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ib_plan.h"
 #include "solver.h"
 
 namespace cuibm {
@@ -563,30 +564,6 @@ __device__ __forceinline__ void neumann_row(double px, double py, double bx_, do
 }
 
 // ---- interpolation plan ---------------------------------------------------------------
-// The ghost and hybrid interpolations are linear in the field: the value at a
-// node is sum_l w_l q_l over the four corners of the image point's cell, where
-// q_l is the field at the corner or, for corners replaced by the body, the body
-// velocity (velocity) or -(n . dU/dt) (pressure Neumann rows).  Which corners
-// are replaced, the corner indices and the weights w_l (the rows of the inverse
-// 4x4 bilinear fit evaluated at the point) depend only on the tags and the body
-// geometry, so they are computed once per tagging (luo_base::tagPoints) into a
-// plan of compact node lists; each step then only gathers.  The weights are the
-// reference's own q*coef of its biLinearInterpolation kernels, so the values
-// agree with its a0 + a1 x + a2 y + a3 x y to rounding.
-struct IbPlan {
-    int *count;  // [0] ghost velocity, [1] hybrid velocity, [2] ghost pressure, [3] hybrid pressure, [4] inside
-    int cap_v, cap_p, cap_in;
-    int *gvNode, *gvIdx, *gvMask;  // mask bit l: corner l takes the body value
-    double *gvW;
-    int *hvNode, *hvIdx, *hvMask;
-    double *hvW, *hvWi, *hvAlpha;  // weights at the node and at its image point; blend factor
-    int *gpNode, *gpIdx, *gpMask;  // mask bit l: corner l is a Neumann row
-    double *gpN, *gpW, *gpWb, *gpCn, *gpDist;  // corner normals; weights at image point and intercept;
-                                               // normal and distance of the dp/dn correction
-    int *hpNode, *hpIdx, *hpMask;
-    double *hpN, *hpW, *hpAlpha;
-    int *inNode;  // nodes inside the body (tag 0)
-};
 
 // weights of the fit at (px, py): coefficient c of store_dev
 __device__ __forceinline__ void fit_weights(const double b[16], double det, double px, double py, double *w)
@@ -1210,6 +1187,8 @@ static std::vector<IbHost> g_ib_host;  // one per context (indexed by Context::i
 
 static IbHost &hostside(Context &c) { return g_ib_host[c.ib_slot]; }
 
+IbPlan &ib_plan(Context &c) { return hostside(c).plan; }
+
 void setup_ib(Context &c)
 {
     IbArrays &b = c.ib;
@@ -1418,6 +1397,8 @@ void launch_tag_points(Context &c)
                 b.gpCoef, b.hpCoef};
     k_plan_build<<<dim3(blocks_for(P.cap_v), 4), kBlock, 0, c.stream>>>(G2, P);
     CUIBM_TRY(cudaGetLastError());
+    // the embedded method's operator rows follow the tags
+    launch_embedded_rows(c);
 }
 
 // one block runs the phases in k_ib_step's order on the plan of the current tags
@@ -1445,6 +1426,7 @@ void launch_ib_rhs1(Context &c) { launch_ib(c, PH_ROBIN | PH_GHOST_U | PH_INSIDE
 void launch_ib_after_velocity(Context &c) { launch_ib(c, PH_WEIGHT_U | PH_GHOST_U, c.uhat); }
 void launch_ib_after_poisson(Context &c) { launch_ib(c, PH_HYBRID_P | PH_WEIGHT_P | PH_GHOST_P, c.u); }
 void launch_ib_after_projection(Context &c) { launch_ib(c, PH_GHOST_U | PH_INSIDE, c.u); }
+void launch_ib_robin_inside(Context &c) { launch_ib(c, PH_ROBIN | PH_INSIDE, c.u); }
 
 void launch_force(Context &c)
 {

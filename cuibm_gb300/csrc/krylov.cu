@@ -25,6 +25,7 @@
 #include <cmath>
 #include <vector>
 
+#include "amg.h"
 #include "operators.cuh"
 #include "solver.h"
 
@@ -473,6 +474,37 @@ void setup_system(Context &c, LinearSystem &S)
     CUIBM_TRY(cudaGetLastError());
     if (S.precond == PC_SMOOTHED_AGGREGATION) build_sa_hierarchy(c, S);
     setup_fused(c, S);
+}
+
+// level 0 of the SA hierarchy: Jacobi smoother tables from the operator's new diagonal
+// (the hierarchy below keeps the operator it was built from)
+__global__ void k_sa_level0_tables(int n, const double *__restrict__ dinv, double omega, double *__restrict__ l0dinv,
+                                   double *__restrict__ l0wd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    l0dinv[i] = dinv[i];
+    if (l0wd) l0wd[i] = omega * dinv[i];
+}
+
+// The operator's rows changed (the embedded method's rows after a body moved): the
+// Jacobi table, the persistent solver's diagonal and the SA smoother's level-0 tables
+// follow.  The reference rebuilds its whole preconditioner each step instead; the
+// coarser SA levels here keep the operator of the initial tags.
+void refresh_system_diagonals(Context &c, LinearSystem &S)
+{
+    const int n = S.n;
+    if (S.which == 1)
+        k_dinv<<<blocks_for(n), kBlock, 0, c.stream>>>(op1(c, S.w), n, S.dinv);
+    else
+        k_dinv<<<blocks_for(n), kBlock, 0, c.stream>>>(op2(c, S.w), n, S.dinv);
+    CUIBM_TRY(cudaGetLastError());
+    refresh_fused_diag(c, S);
+    if (!S.amg.empty() && S.amg[0]->n == n) {
+        SaLevel *L = S.amg[0];
+        k_sa_level0_tables<<<blocks_for(n), kBlock, 0, c.stream>>>(n, S.dinv, L->omega, L->dinv, L->wd);
+        CUIBM_TRY(cudaGetLastError());
+    }
 }
 
 struct SolveLauncher {

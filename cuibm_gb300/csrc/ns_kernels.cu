@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "ib_plan.h"
 #include "operators.cuh"
 #include "solver.h"
 
@@ -44,13 +45,44 @@ struct BcPtrs {
     const double *xm, *xp, *ym, *yp;
 };
 
+// The embedded method's update of rhs1 (luo_iter/kernels/intermediateVelocity.cu
+// update_rhs1_x/y with the ns_rhs and interp_rhs of LHS1_mid_iter_X/Y): interior rows
+// without a patch are divided by their diagonal (rhs * rscale); a hybrid row becomes
+// rhs * pns + pint; a ghost row becomes its interp_rhs 2 u_B - sum_l w_l q_l over the
+// interpolation corners that are ghost nodes, q_l the body velocity where the
+// interpolation substituted the corner, else the field there.  pid is null for the
+// other methods.
+struct EmbRhs1 {
+    const int *pid;
+    const double *rscale, *pns, *pint;
+    int cap;  // slots below cap are ghost rows
+    const int *gin, *gIdx, *gMask;
+    const double *gW, *uB, *vB;
+};
+
+__device__ __forceinline__ double emb_rhs1(const EmbRhs1 &e, int t, int nU, double r, const double *__restrict__ u)
+{
+    const int k = e.pid[t];
+    if (k < 0) return r * e.rscale[t];
+    if (k >= e.cap) return __dadd_rn(__dmul_rn(r, e.pns[k]), e.pint[k]);
+    const double qb = t >= nU ? e.vB[0] : e.uB[0];
+    const int in = e.gin[k], m = e.gMask[k];
+    double temp = 0;
+    for (int l = 0; l < 4; ++l)
+        if (in >> l & 1) {
+            const double q = (m >> l & 1) ? qb : u[e.gIdx[4 * k + l]];
+            temp = __dsub_rn(temp, __dmul_rn(e.gW[4 * k + l], q));
+        }
+    return __dadd_rn(2 * qb, temp);
+}
+
 // SHIFT: the step's form: N of the previous step moves to Nold while the new N is
 // written (the reference's "Nold = N" copy).  DEBUG: also store L and bc1.
 template <bool SHIFT, bool DEBUG>
 __global__ void __launch_bounds__(256) k_rhs1(RhsCoef c, Grid g, BcPtrs b, const double *__restrict__ u,
                                               double *__restrict__ N, double *__restrict__ Nold,
                                               double *__restrict__ rhs, double *__restrict__ Lout,
-                                              double *__restrict__ bc1out, double nu, double dt)
+                                              double *__restrict__ bc1out, double nu, double dt, EmbRhs1 e)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.nUV) return;
@@ -108,16 +140,28 @@ __global__ void __launch_bounds__(256) k_rhs1(RhsCoef c, Grid g, BcPtrs b, const
     const double Nprev = SHIFT ? N[t] : Nold[t];
     if (SHIFT) Nold[t] = Nprev;
     N[t] = Nn;
-    rhs[t] = uc + dt * (0.5 * Nprev - 1.5 * Nn + 0.5 * Ln) + B1;
+    const double r = uc + dt * (0.5 * Nprev - 1.5 * Nn + 0.5 * Ln) + B1;
+    rhs[t] = e.pid ? emb_rhs1(e, t, nU, r, u) : r;
     if (DEBUG) {
         Lout[t] = Ln;
         bc1out[t] = B1;
     }
 }
 
+// The embedded method's update of rhs2 (luo_iter/kernels/pressure.cu update_rhs2, whose
+// threads stop at (nx-1)*ny): a patched row becomes rhs * pns + interp_rhs, where
+// interp_rhs (the dp/dn and Neumann-corner terms of LHS2_mid_iter) is linear in the
+// body acceleration (uB - uBk)/dt; the other rows keep rhs (ns_rhs 1, interp_rhs 0).
+struct EmbRhs2 {
+    const int *pid;
+    const double *pns, *pAu, *pAv;
+    const double *uB, *uBk, *vB, *vBk;
+    double dt;
+};
+
 // rhs2 = -D uhat with boundary velocities on the domain edges
 __global__ void k_rhs2(Grid g, BcPtrs b, const double *__restrict__ dx, const double *__restrict__ dy,
-                       const double *__restrict__ uh, double *__restrict__ rhs2)
+                       const double *__restrict__ uh, double *__restrict__ rhs2, EmbRhs2 e)
 {
     const int ip = blockIdx.x * blockDim.x + threadIdx.x;
     if (ip >= g.nP) return;
@@ -127,7 +171,16 @@ __global__ void k_rhs2(Grid g, BcPtrs b, const double *__restrict__ dx, const do
     const double uw = (I != 0) ? uh[iu - 1] : b.xm[J];
     const double vn = (J != ny - 1) ? uh[iv] : b.yp[nx - 1 + I];
     const double vs = (J != 0) ? uh[iv - nx] : b.ym[nx - 1 + I];
-    rhs2[ip] = (((0 - ue / dx[I]) + uw / dx[I]) - vn / dy[J]) + vs / dy[J];
+    double r = (((0 - ue / dx[I]) + uw / dx[I]) - vn / dy[J]) + vs / dy[J];
+    if (e.pid && ip < (nx - 1) * ny) {
+        const int k = e.pid[ip];
+        if (k >= 0) {
+            const double dudt = (e.uB[0] - e.uBk[0]) / e.dt, dvdt = (e.vB[0] - e.vBk[0]) / e.dt;
+            const double in = __dadd_rn(__dmul_rn(dudt, e.pAu[k]), __dmul_rn(dvdt, e.pAv[k]));
+            r = __dadd_rn(__dmul_rn(r, e.pns[k]), in);
+        }
+    }
+    rhs2[ip] = r;
 }
 
 // u = uhat - dt G p ; uold = u
@@ -302,8 +355,8 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
         col.push_back(cc);
         val.push_back(v);
     };
-    // a patched row of the modified Fadlun method: its entries in column order (the
-    // reference sorts its Fadlun matrices by row and column; zero entries dropped)
+    // a patched row (modified Fadlun or embedded method): its entries in column order
+    // (the reference sorts these matrices by row and column; zero entries dropped)
     auto patched = [&](int i, const std::vector<int> &pid, const std::vector<int> &pcol,
                        const std::vector<double> &pval, const std::vector<double> &pdiag) {
         if (pid.empty() || pid[i] < 0) return false;
@@ -318,13 +371,60 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
         for (auto &q : e) push(i, q.first, q.second);
         return true;
     };
-    const auto &F = c.fadlun;
+    // the embedded method's patched rows live on the device (rebuilt at every tagging)
+    Context::FadlunRows F = c.fadlun;
+    const bool emb = c.emb.pid1 != nullptr;
+    if (emb) {
+        auto down = [&](auto &v, const auto *src, size_t n) {
+            v.resize(n);
+            CUIBM_TRY(cudaMemcpyAsync(v.data(), src, n * sizeof(v[0]), cudaMemcpyDeviceToHost, c.stream));
+        };
+        const size_t s1 = 2 * (size_t)c.emb.cap1, s2 = 2 * (size_t)c.emb.cap2;
+        down(F.pid1, c.emb.pid1, c.g.nUV);
+        down(F.pcol1, c.emb.pcol1, 5 * s1);
+        down(F.pval1, c.emb.pval1, 5 * s1);
+        down(F.pdiag1, c.emb.pdiag1, s1);
+        down(F.pid2, c.emb.pid2, c.g.nP);
+        down(F.pcol2, c.emb.pcol2, 5 * s2);
+        down(F.pval2, c.emb.pval2, 5 * s2);
+        down(F.pdiag2, c.emb.pdiag2, s2);
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    }
+    const double *dx = c.gx.width.data(), *dy = c.gy.width.data(), dt = c.P.dt, nu = c.P.nu;
+    // an interior row of the embedded LHS1 without a patch: the momentum row over its
+    // diagonal (LHS1_mid_iter_X/Y, luo_iter/kernels/LHS1.cu), entries E, W, N, S, centre
+    auto scaled_u = [&](int i, int I, int J) {
+        const double temp = 1 + 0.5 * dt * nu * (1 / (dx[I + 1] * (dx[I + 1] + dx[I]) * 0.5)) +
+                            0.5 * dt * nu * (1 / (dx[I] * (dx[I + 1] + dx[I]) * 0.5)) +
+                            0.5 * dt * nu * (1 / (dy[J] * (dy[J + 1] + dy[J]) * 0.5)) +
+                            0.5 * dt * nu * (1 / (dy[J] * (dy[J - 1] + dy[J]) * 0.5));
+        push(i, i + 1, -0.5 * dt * nu * (1 / (dx[I + 1] * (dx[I + 1] + dx[I]) * 0.5)) / temp);
+        push(i, i - 1, -0.5 * dt * nu * (1 / (dx[I] * (dx[I + 1] + dx[I]) * 0.5)) / temp);
+        push(i, i + (nx - 1), -0.5 * dt * nu * (1 / (dy[J] * (dy[J + 1] + dy[J]) * 0.5)) / temp);
+        push(i, i - (nx - 1), -0.5 * dt * nu * (1 / (dy[J] * (dy[J - 1] + dy[J]) * 0.5)) / temp);
+        push(i, i, 1);
+    };
+    auto scaled_v = [&](int i, int I, int J) {
+        const double temp = 1 + 0.5 * dt * nu * (1 / (dx[I] * (dx[I] + dx[I + 1]) * 0.5)) +
+                            0.5 * dt * nu * (1 / (dx[I] * (dx[I] + dx[I - 1]) * 0.5)) +
+                            0.5 * dt * nu * (1 / (dy[J + 1] * (dy[J] + dy[J + 1]) * 0.5)) +
+                            0.5 * dt * nu * (1 / (dy[J] * (dy[J] + dy[J + 1]) * 0.5));
+        push(i, i + 1, -0.5 * dt * nu * (1 / (dx[I] * (dx[I] + dx[I + 1]) * 0.5)) / temp);
+        push(i, i - 1, -0.5 * dt * nu * (1 / (dx[I] * (dx[I] + dx[I - 1]) * 0.5)) / temp);
+        push(i, i + nx, -0.5 * dt * nu * (1 / (dy[J + 1] * (dy[J] + dy[J + 1]) * 0.5)) / temp);
+        push(i, i - nx, -0.5 * dt * nu * (1 / (dy[J] * (dy[J] + dy[J + 1]) * 0.5)) / temp);
+        push(i, i, 1);
+    };
     if (which == 1) {
         const double *E = T("1uE"), *W = T("1uW"), *Nn = T("1uN"), *S = T("1uS");
         for (int J = 0; J < ny; ++J)
             for (int I = 0; I < nx - 1; ++I) {
                 int i = J * (nx - 1) + I;
                 if (patched(i, F.pid1, F.pcol1, F.pval1, F.pdiag1)) continue;
+                if (emb && I != 0 && I != nx - 2 && J != 0 && J != ny - 1) {
+                    scaled_u(i, I, J);
+                    continue;
+                }
                 if (I != nx - 2) push(i, i + 1, -E[I]);
                 if (I != 0) push(i, i - 1, -W[I]);
                 if (J != ny - 1) push(i, i + nx - 1, -Nn[J]);
@@ -336,6 +436,10 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
             for (int I = 0; I < nx; ++I) {
                 int i = c.g.nU + J * nx + I;
                 if (patched(i, F.pid1, F.pcol1, F.pval1, F.pdiag1)) continue;
+                if (emb && I != 0 && I != nx - 1 && J != 0 && J != ny - 2) {
+                    scaled_v(i, I, J);
+                    continue;
+                }
                 if (I != nx - 1) push(i, i + 1, -vE[I]);
                 if (I != 0) push(i, i - 1, -vW[I]);
                 if (J != ny - 2) push(i, i + nx, -vN[J]);
@@ -357,6 +461,32 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
                 push(i, i, d);
             }
     }
+    if (emb) {
+        // the embedded matrices as the reference leaves them after its per-step sort: rows
+        // and columns ascending, and as many entries as it sized them (the plain operator's
+        // plus one per hybrid node); the positions its kernels leave unwritten hold zero
+        // entries at (0, 0), which sort first
+        std::vector<size_t> order(row.size());
+        for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            return row[a] != row[b] ? row[a] < row[b] : col[a] < col[b];
+        });
+        const size_t plain = which == 1 ? (size_t)(nx - 1) * ny * 5 - 2 * ny - 2 * (nx - 1) + (size_t)nx * (ny - 1) * 5 -
+                                              2 * nx - 2 * (ny - 1)
+                                        : (size_t)nx * ny * 5 - 2 * nx - 2 * ny;
+        const size_t want = plain + embedded_hybrid_count(c, which);
+        const size_t pad = want > row.size() ? want - row.size() : 0;
+        std::vector<int> r2(pad, 0), c2(pad, 0);
+        std::vector<double> v2(pad, 0.0);
+        for (size_t k : order) {
+            r2.push_back(row[k]);
+            c2.push_back(col[k]);
+            v2.push_back(val[k]);
+        }
+        row.swap(r2);
+        col.swap(c2);
+        val.swap(v2);
+    }
 }
 
 // CSR of the operator the solver iterates on (row weights w applied when given)
@@ -375,21 +505,33 @@ void host_operator_csr(Context &c, int which, const double *w, std::vector<int> 
 
 static BcPtrs bc_ptrs(Context &c) { return BcPtrs{c.bc[XMINUS], c.bc[XPLUS], c.bc[YMINUS], c.bc[YPLUS]}; }
 
+static EmbRhs1 emb_rhs1_args(Context &c)
+{
+    const auto &E = c.emb;
+    if (!E.pid1) return EmbRhs1{};
+    const IbPlan &P = ib_plan(c);
+    return EmbRhs1{E.pid1, E.rscale1, E.pns1, E.pint1, E.cap1, E.gin, P.gvIdx, P.gvMask, P.gvW, c.ib.uB, c.ib.vB};
+}
+
 void launch_rhs1(Context &c, bool debug_terms)
 {
     int nb = blocks_for(c.g.nUV);
+    const EmbRhs1 e = debug_terms ? EmbRhs1{} : emb_rhs1_args(c);
     if (debug_terms)
         k_rhs1<false, true><<<nb, kBlock, 0, c.stream>>>(c.rc, c.g, bc_ptrs(c), c.u, c.N, c.Nold, c.rhs1, c.L, c.bc1,
-                                                         c.P.nu, c.P.dt);
+                                                         c.P.nu, c.P.dt, e);
     else
         k_rhs1<true, false><<<nb, kBlock, 0, c.stream>>>(c.rc, c.g, bc_ptrs(c), c.u, c.N, c.Nold, c.rhs1, nullptr,
-                                                         nullptr, c.P.nu, c.P.dt);
+                                                         nullptr, c.P.nu, c.P.dt, e);
     CUIBM_TRY(cudaGetLastError());
 }
 
 void launch_rhs2(Context &c, const double *uh)
 {
-    k_rhs2<<<blocks_for(c.g.nP), kBlock, 0, c.stream>>>(c.g, bc_ptrs(c), c.dx, c.dy, uh, c.rhs2);
+    const auto &E = c.emb;
+    const EmbRhs2 e = E.pid2 ? EmbRhs2{E.pid2, E.pns2, E.pAu2, E.pAv2, c.ib.uB, c.ib.uBk, c.ib.vB, c.ib.vBk, c.P.dt}
+                             : EmbRhs2{};
+    k_rhs2<<<blocks_for(c.g.nP), kBlock, 0, c.stream>>>(c.g, bc_ptrs(c), c.dx, c.dy, uh, c.rhs2, e);
     CUIBM_TRY(cudaGetLastError());
 }
 

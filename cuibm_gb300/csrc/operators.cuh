@@ -40,7 +40,7 @@ __device__ __forceinline__ double lhs1_row_f(const Lhs1Coef &c, const Grid &g, i
         if (I != 0) y -= c.uW[I] * x(i - 1);
         if (J != g.ny - 1) y -= c.uN[J] * x(i + w);
         if (J != 0) y -= c.uS[J] * x(i - w);
-        return y;
+        return c.rscale ? y * c.rscale[i] : y;
     }
     int k = i - g.nU, I = k % g.nx, J = k / g.nx;
     double d = (((1 + c.vE[I]) + c.vW[I]) + c.vN[J]) + c.vS[J];
@@ -49,7 +49,7 @@ __device__ __forceinline__ double lhs1_row_f(const Lhs1Coef &c, const Grid &g, i
     if (I != 0) y -= c.vW[I] * x(i - 1);
     if (J != g.ny - 2) y -= c.vN[J] * x(i + g.nx);
     if (J != 0) y -= c.vS[J] * x(i - g.nx);
-    return y;
+    return c.rscale ? y * c.rscale[i] : y;
 }
 
 template <class X>

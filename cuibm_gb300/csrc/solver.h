@@ -48,6 +48,9 @@ struct Lhs1Coef {
     // v rows: E/W on I (0..nx-1), N/S on J (0..ny-2)
     const double *vE, *vW, *vN, *vS;
     RowPatch patch;
+    // embedded method: rows without a patch are scaled by rscale[i] (1 / diagonal on the
+    // interior rows, 1 on the boundary rows); null for the other methods
+    const double *rscale;
 };
 struct Lhs2Coef {
     const double *E, *W;  // on I (0..nx-1), zero where the neighbour is missing
@@ -209,6 +212,19 @@ struct Context {
         int nnz1 = 0, nnz2 = 0;  // entries of the matrices cuibm_get_matrix returns
     } fadlun;
 
+    // embedded method (OSC_CYLINDER): the patched rows of the tagged nodes, rebuilt at
+    // every tagging.  Velocity slots: ghost nodes [0, cap1), hybrid nodes [cap1, 2 cap1);
+    // pressure slots: ghost [0, cap2), hybrid [cap2, 2 cap2)
+    struct EmbeddedRows {
+        int cap1 = 0, cap2 = 0;
+        int *pid1 = nullptr, *pcol1 = nullptr, *pid2 = nullptr, *pcol2 = nullptr;
+        double *pval1 = nullptr, *pdiag1 = nullptr, *pval2 = nullptr, *pdiag2 = nullptr;
+        double *pns1 = nullptr, *pint1 = nullptr;  // rhs1 = rhs1 pns + pint (hybrid slots)
+        int *gin = nullptr;                        // ghost slots: corners that are ghost nodes
+        double *pns2 = nullptr, *pAu2 = nullptr, *pAv2 = nullptr;  // rhs2 = rhs2 pns + dudt pAu + dvdt pAv
+        double *rscale1 = nullptr;                 // numUV
+    } emb;
+
     // output files
     FILE *iterationsFile = nullptr, *forceFile = nullptr, *midPositionFile = nullptr;
 
@@ -243,18 +259,25 @@ void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool 
 int read_solve_status(Context &c, LinearSystem &S, int *iterations);
 int read_body_runs(Context &c, LinearSystem &S);
 int count_kernel_nodes(cudaGraph_t g);
+void refresh_system_diagonals(Context &c, LinearSystem &S);  // after the operator's rows changed
 
 // fused_solve.cu
 void setup_fused(Context &c, LinearSystem &S);
 void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x);
 void set_fused_trace(Context &c, LinearSystem &S, bool on);
 double solve_bytes(const LinearSystem &S, int iterations);
+void refresh_fused_diag(Context &c, LinearSystem &S);
 
 // fadlun.cu
 void setup_fadlun(Context &c);
 void launch_fadlun_rhs1(Context &c);
 void launch_fadlun_rhs2(Context &c);
 void launch_fadlun_project(Context &c);
+
+// embedded.cu
+void setup_embedded(Context &c);
+void launch_embedded_rows(Context &c);  // after each tagging: the patched rows of the new tags
+int embedded_hybrid_count(Context &c, int system);
 
 // amg.cu
 void build_sa_hierarchy(Context &c, LinearSystem &S);
@@ -278,6 +301,7 @@ void launch_ib_rhs1(Context &c);             // Robin, ghost u, inside, hybrid u
 void launch_ib_after_velocity(Context &c);   // weight uhat, ghost uhat
 void launch_ib_after_poisson(Context &c);    // hybrid p, weight p, ghost p
 void launch_ib_after_projection(Context &c); // ghost u, inside
+void launch_ib_robin_inside(Context &c);     // Robin, inside (embedded rhs1)
 void launch_force(Context &c);
 void launch_body_motion(Context &c, double t);
 void launch_body_pre_step(Context &c);

@@ -851,3 +851,104 @@ class FadlunSolver(LuoSolver):
         self._update_solver()
         self.iters = (it1, it2)
         self.timeStep += 1
+
+
+class EmbeddedSolver(LuoSolver):
+    """The embedded method (SolverType OSC_CYLINDER) on the CPU: luo_base::stepTime
+    (luo_base.cu:208-233) with luo_iter's phases - intermediate_velocity_setup
+    (luo_iter/intermediateVelocity.cu:17-80: Robin outflow, inside velocity, explicit
+    terms, alpha, the set = false stencils, LHS1 rebuilt, rhs1 updated), the velocity
+    solve, poisson_setup (luo_iter/poisson.cu:15-58: rhs2, alpha, pressure stencils,
+    LHS2 rebuilt, rhs2 updated), the Poisson solve, luo_base::_project_velocity
+    (luo_base/projectVelocity.cu:11-53) and the body update (force, motion, tags).
+
+    The operators are rebuilt every step on zeroed arrays (the reference's first step;
+    later steps of the reference reuse its previous sorted COO arrays without clearing
+    the LHS1 values, which this restatement does not reproduce)."""
+
+    def __init__(self, folder, solve="direct"):
+        super().__init__(folder, solve="none")
+        g = self.g
+        # luo_iter::initialise (luo_base::initialise) does not set the inside velocity
+        f0 = load_case(folder)[1][0]
+        ip = f0.get("initialPerturbation", [0.0, 0.0])
+        self.u = initial_velocity(g, float(f0["initialVelocity"][0]), float(f0["initialVelocity"][1]),
+                                  float(ip[0]), float(ip[1]))
+        self.uhat = self.u.copy()
+        self.solve = solve
+        self._fact = {1: (None, None), 2: (None, None)}
+        if solve != "direct":
+            ls = {s["system"]: s for s in self.sim.get("linearSolvers", [])}
+            self.cfg = {k: (float(ls[k].get("tolerance", 1e-5)), int(ls[k].get("maxIterations", 10000)),
+                            _PC.get(ls[k].get("preconditioner", "DIAGONAL"), 1)) for k in ("velocity", "Poisson")}
+
+    def _solve(self, which, b, x0):
+        A = self.A1 if which == 1 else self.A2
+        key, fact = self._fact[which]
+        same = key is not None and all(np.array_equal(a, k) for a, k in zip((A.ptr, A.col, A.val), key))
+        if self.solve == "direct":
+            if not same:
+                import scipy.sparse.linalg as spla
+                fact = spla.splu(A.scipy().tocsc())
+                self._fact[which] = ((A.ptr.copy(), A.col.copy(), A.val.copy()), fact)
+            return fact.solve(b), 0
+        tol, mx, pc = self.cfg["velocity" if which == 1 else "Poisson"]
+        if pc == 2 and not same:
+            fact = Amg(A)
+            self._fact[which] = ((A.ptr.copy(), A.col.copy(), A.val.copy()), fact)
+        x, it, ok = bicgstab_pc(A, b, x0, tol, mx, pc, fact if pc == 2 else None)
+        if not ok:
+            raise RuntimeError("oracle %s solve did not converge" % ("velocity" if which == 1 else "Poisson"))
+        return x, it
+
+    def step(self):
+        g, T, bb, dt = self.g, self.T, self.bb, self.dt
+        xm, xp, ym, yp = self.bc
+        ub, vb = float(self.uB[0]), float(self.vB[0])
+        # _pre_step
+        self.uold = self.u.copy()
+        self.uBk = self.uB.copy()
+        Nold = self.N
+        # intermediate_velocity_setup: u = uold, Robin outflow, inside velocity, explicit terms
+        xp[:] = robin(self.u, xp, g, dt)
+        u = set_inside(self.u, T, ub, vb, g)
+        bc = (xm, xp, ym, yp)
+        self.N = generate_N(u, g, bc)
+        L = generate_L(u, g, bc, self.nu)
+        b1 = generate_bc1(u, g, bc, self.nu, dt)
+        rhs1 = generate_rhs(L, Nold, self.N, u, b1, dt)
+        alpha = iter_alpha(0, T, g, bb)
+        iter_alpha(1, T, g, bb, alpha)
+        S = Stencils(g.nUV)
+        ghost_velocity(0, u, T, ub, g, bb, set_=False, S=S)
+        ghost_velocity(1, u, T, vb, g, bb, set_=False, S=S)
+        ustar, _ = hybrid_velocity(0, u, np.zeros(g.nUV), T, ub, g, bb, S=S)
+        hybrid_velocity(1, u, ustar, T, vb, g, bb, S=S)
+        row, col, val, ns, interp = iter_lhs1(g, dt, self.nu, T, S, alpha, ub, vb, bb)
+        self.A1 = csr_from_coo_summed(g.nUV, row, col, val)
+        rhs1 = iter_update_rhs1(rhs1, ns, interp, g)
+        self.uhat, it1 = self._solve(1, rhs1, self.uhat)
+        # poisson_setup
+        rhs2 = generate_rhs2(self.uhat, g, bc)
+        dudt = (float(self.uB[0]) - float(self.uBk[0])) / dt  # zero: _pre_step set uBk = uB
+        Sp = Stencils(g.nP)
+        ghost_pressure(self.p, T, dudt, 0.0, g, bb, set_=False, S=Sp)
+        hybrid_pressure(self.p, T, dudt, 0.0, g, bb, S=Sp)
+        row, col, val, ns, interp = iter_lhs2(g, dt, T, Sp, iter_alpha(2, T, g, bb), bb)
+        self.A2 = csr_from_coo_summed(g.nP, row, col, val)
+        rhs2 = iter_update_rhs2(rhs2, ns, interp, g)
+        self.p, it2 = self._solve(2, rhs2, self.p)
+        # luo_base::_project_velocity: projection, ghost nodes (set), inside velocity
+        u, self.uold = project(u, self.uhat, self.p, g, dt)
+        u, _ = ghost_velocity(0, u, T, ub, g, bb)
+        u, _ = ghost_velocity(1, u, T, vb, g, bb)
+        self.u = set_inside(u, T, ub, vb, g)
+        # body update: control-volume force, then the prescribed motion at t = dt * timeStep
+        self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
+        xnew, unew = self.motion(self.timeStep)
+        self.bx = np.array([xnew + v for v in self.bdx])
+        self.uB = np.full(len(self.bx), unew)
+        self.midX = xnew
+        self._update_solver()
+        self.iters = (it1, it2)
+        self.timeStep += 1

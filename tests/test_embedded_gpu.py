@@ -1,0 +1,201 @@
+"""GPU parity of the embedded ghost-node method (SolverType OSC_CYLINDER, the
+reference's luo_iter) against the oracle, through the C ABI: the per-step LHS1 and
+LHS2 entry by entry (the interior momentum rows over their diagonal bit for bit,
+the rows of tagged nodes to the interpolation weights' rounding), the fused
+right-hand-side updates, and tightly solved steps of the impulsively started
+cylinder, fixed and oscillating (fields to 1e-9 relative L2, drag and lift to 1e-6)."""
+import numpy as np
+import pytest
+
+import oracle
+
+cb = pytest.importorskip("cuibm_gb300")
+from cuibm_gb300 import cases  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+RTOL_W = 1e-10       # rows of tagged nodes: CUDA acos/sin/tan vs the C library in the intercepts
+RTOL_KERNEL = 1e-12  # explicit terms use precomputed metric tables (rounding order differs)
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def rel_max(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def emb_case(path, **kw):
+    args = dict(h=0.05, ratio=1.1, extent=3.0, core=0.6, points=48, nu=0.025, dt=0.01, nt=50, vel_tol=1e-12,
+                pois_tol=1e-12, pois_pc="SMOOTHED_AGGREGATION", method="OSC_CYLINDER")
+    args.update(kw)
+    return cases.cylinder(path, **args)
+
+
+@pytest.fixture(params=[(48, 0.5, 0.05), (101, 0.43, 0.025)])
+def emb(request, tmp_path):
+    pts, r, h = request.param
+    f = emb_case(str(tmp_path / "c"), points=pts, radius=r, h=h)
+    s = cb.NavierStokesSolver(f)
+    s.set_option("write_output", 0)
+    s.initialise()
+    yield s
+    s.close()
+
+
+def oracle_state(s):
+    g = oracle.Grid.from_arrays(s.get("x"), s.get("dx"), s.get("xu"), s.get("y"), s.get("dy"), s.get("yv"))
+    i = s.info
+    bb = (i.bb_start_i, i.bb_start_j, i.bb_ncx, i.bb_ncy)
+    by = s.get("body_y")
+    T = oracle.tag_points(g, s.get("body_x"), by, s.get("body_uB"), s.get("body_vB"), bb, 0.0,
+                          sum(float(v) for v in by) / len(by))
+    return g, bb, T
+
+
+def oracle_velocity_rows(g, bb, T, u, dt, nu, ub=0.0, vb=0.0):
+    S = oracle.Stencils(g.nUV)
+    oracle.ghost_velocity(0, u, T, ub, g, bb, set_=False, S=S)
+    oracle.ghost_velocity(1, u, T, vb, g, bb, set_=False, S=S)
+    ustar, _ = oracle.hybrid_velocity(0, u, np.zeros(g.nUV), T, ub, g, bb, S=S)
+    oracle.hybrid_velocity(1, u, ustar, T, vb, g, bb, S=S)
+    a = oracle.iter_alpha(0, T, g, bb)
+    oracle.iter_alpha(1, T, g, bb, a)
+    return oracle.iter_lhs1(g, dt, nu, T, S, a, ub, vb, bb)
+
+
+def oracle_pressure_rows(g, bb, T, p, dt):
+    S = oracle.Stencils(g.nP)
+    oracle.ghost_pressure(p, T, 0.0, 0.0, g, bb, set_=False, S=S)
+    oracle.hybrid_pressure(p, T, 0.0, 0.0, g, bb, S=S)
+    return oracle.iter_lhs2(g, dt, T, S, oracle.iter_alpha(2, T, g, bb), bb)
+
+
+def gpu_csr(s, system, n):
+    import scipy.sparse as sp
+    r, c, v = s.matrix(system)
+    A = sp.coo_matrix((v, (r, c)), shape=(n, n)).tocsr()
+    A.sort_indices()
+    A.eliminate_zeros()
+    return A
+
+
+def test_tags_bit_exact(emb):
+    g, bb, T = oracle_state(emb)
+    for mine, ref in (("ghost_tags_uv", T.ghostTagsUV), ("hybrid_tags_uv", T.hybridTagsUV),
+                      ("ghost_tags_p", T.ghostTagsP), ("hybrid_tags_p", T.hybridTagsP)):
+        assert np.array_equal(emb.get(mine), ref), mine
+    assert (T.hybridTagsUV > 0).sum() > 20
+
+
+@pytest.mark.parametrize("system", [1, 2])
+def test_matrices_match_oracle(emb, system):
+    """The reference's per-step matrix (summed, zeros dropped) entry by entry."""
+    g, bb, T = oracle_state(emb)
+    i = emb.info
+    if system == 1:
+        r, c, v, _, _ = oracle_velocity_rows(g, bb, T, emb.get("u"), i.dt, i.nu)
+        n, tagged = g.nUV, (T.ghostTagsUV > 0) | (T.hybridTagsUV > 0)
+        assert i.nnz_lhs1 == len(r)
+    else:
+        r, c, v, _, _ = oracle_pressure_rows(g, bb, T, emb.get("p"), i.dt)
+        n, tagged = g.nP, (T.ghostTagsP > 0) | (T.hybridTagsP > 0)
+        assert i.nnz_lhs2 == len(r)
+    ref = oracle.csr_from_coo_summed(n, r, c, v)
+    gr, gc, _ = emb.matrix(system)  # sorted by row, then column, as the reference sorts it
+    assert len(gr) == len(r) and np.all((np.diff(gr) > 0) | ((np.diff(gr) == 0) & (np.diff(gc) >= 0)))
+    A = gpu_csr(emb, system, n)
+    assert np.array_equal(A.indptr, ref.ptr) and np.array_equal(A.indices, ref.col)
+    rows = np.repeat(np.arange(n), np.diff(ref.ptr))
+    plain = ~tagged[rows]
+    assert np.array_equal(A.data[plain].view(np.uint64), ref.val[plain].view(np.uint64))
+    assert np.max(np.abs(A.data[~plain] - ref.val[~plain])) < RTOL_W
+    # the matrix-free operator applies the same matrix
+    rng = np.random.default_rng(system)
+    x = rng.standard_normal(n)
+    emb.set("work_x", np.concatenate([x, np.zeros(max(g.nUV, g.nP) - n)]))
+    emb.run("apply_lhs1" if system == 1 else "apply_lhs2")
+    y = emb.get("work_y")[:n]
+    assert rel_max(y, ref.matvec(x)) < RTOL_W
+
+
+def test_rhs_updates_match_oracle(emb):
+    g, bb, T = oracle_state(emb)
+    i = emb.info
+    rng = np.random.default_rng(5)
+    u = 1.0 + 0.2 * rng.standard_normal(g.nUV)
+    emb.set("u", u)
+    bc = [emb.get(k).copy() for k in ("bc_xminus", "bc_xplus", "bc_yminus", "bc_yplus")]
+    emb.run("generate_rhs1")  # Robin outflow, inside velocity, explicit terms, update_rhs1
+    xm, xp, ym, yp = bc
+    xp = oracle.robin(u, xp, g, i.dt)
+    ui = oracle.set_inside(u, T, 0.0, 0.0, g)
+    assert np.array_equal(emb.get("u"), ui)
+    b = (xm, xp, ym, yp)
+    N = oracle.generate_N(ui, g, b)
+    L = oracle.generate_L(ui, g, b, i.nu)
+    b1 = oracle.generate_bc1(ui, g, b, i.nu, i.dt)
+    rhs = oracle.generate_rhs(L, np.zeros(g.nUV), N, ui, b1, i.dt)
+    _, _, _, ns, interp = oracle_velocity_rows(g, bb, T, ui, i.dt, i.nu)
+    ref1, got1 = oracle.iter_update_rhs1(rhs, ns, interp, g), emb.get("rhs1")
+    tagged = (T.ghostTagsUV > 0) | (T.hybridTagsUV > 0)
+    scale = np.max(np.abs(ref1))
+    assert np.max(np.abs(got1 - ref1)[~tagged]) / scale < RTOL_KERNEL
+    assert np.max(np.abs(got1 - ref1)[tagged]) / scale < RTOL_W  # interpolation weights
+    uhat = 1.0 + 0.2 * rng.standard_normal(g.nUV)
+    emb.set("uhat", uhat)
+    emb.run("rhs2")
+    _, _, _, ns2, interp2 = oracle_pressure_rows(g, bb, T, emb.get("p"), i.dt)
+    ref2 = oracle.iter_update_rhs2(oracle.generate_rhs2(uhat, g, b), ns2, interp2, g)
+    assert rel_max(emb.get("rhs2"), ref2) < 1e-15
+
+
+@pytest.mark.parametrize("graph,fused", [(1, 1), (0, 1), (1, 0)])
+def test_cylinder_steps_match_oracle(tmp_path, graph, fused):
+    """Impulsively started cylinder, embedded method: 30 tightly solved steps."""
+    f = emb_case(str(tmp_path / "c"), nt=30)
+    ref = oracle.EmbeddedSolver(f, solve="direct")
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.set_option("use_graph", graph)
+        s.set_option("fused_solve", fused)
+        s.initialise()
+        forces = []
+        for k in range(30):
+            s.stepTime(1)
+            ref.step()
+            forces.append((s.forces(), (ref.fx, ref.fy)))
+        assert rel_l2(s.get("u"), ref.u) < 1e-9
+        assert rel_l2(s.get("p"), ref.p) < 1e-8
+        for (fx, fy), (ox, oy) in forces:
+            assert abs(2 * fx - 2 * ox) < 1e-6 and abs(2 * fy - 2 * oy) < 1e-6
+
+
+def test_cg_is_rejected(tmp_path):
+    f = emb_case(str(tmp_path / "c"), pois_krylov="CG")
+    with pytest.raises(cb.CuibmError) as e:
+        cb.NavierStokesSolver(f)
+    assert "BICGSTAB" in str(e.value)
+
+
+@pytest.mark.parametrize("graph", [1, 0])
+def test_oscillating_cylinder_steps_match_oracle(tmp_path, graph):
+    """A prescribed oscillation: the tags, the interpolation plan and the operator rows
+    follow the body every step (the reference rebuilds its matrices each step too)."""
+    motion = {"xCoefficient": 0.05, "uCoefficient": 0.05 * 2 * np.pi, "xfrequency": 1.0, "xPhase": 0.0,
+              "uPhase": 0.0}
+    f = emb_case(str(tmp_path / "c"), nt=30, motion=motion)
+    ref = oracle.EmbeddedSolver(f, solve="direct")
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.set_option("use_graph", graph)
+        s.initialise()
+        for k in range(20):
+            s.stepTime(1)
+            ref.step()
+            assert abs(2 * s.forces()[0] - 2 * ref.fx) < 1e-6, k
+        assert np.array_equal(s.get("ghost_tags_uv"), ref.T.ghostTagsUV)
+        assert np.array_equal(s.get("hybrid_tags_p"), ref.T.hybridTagsP)
+        assert rel_l2(s.get("u"), ref.u) < 1e-9
+        assert rel_l2(s.get("p"), ref.p) < 1e-8
