@@ -40,18 +40,30 @@ METRIC = "Mcell-steps/s"
 # reference's; CG (on the symmetrised operators, same stopping rule) for study -
 # on this stretched grid it needs about three times as many V-cycles.
 KRYLOV = os.environ.get("CUIBM_BENCH_KRYLOV", "BICGSTAB")
+# Precision of both solves: FP64 (the reference's) or MIXED (FP32 multigrid cycles or
+# inner solves under FP64 Krylov iterations, the same FP64 stopping rule).
+PRECISION = os.environ.get("CUIBM_BENCH_PRECISION", "FP64")
 
 
-def make_case(workload, folder, tight=False):
+def make_case(workload, folder, tight=False, precision=None):
     from cuibm_gb300 import cases
+    prec = precision or PRECISION
+    prec = None if prec == "FP64" else prec
     if workload == "cavity64":
         return cases.cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000000, vel_tol=1e-8, pois_tol=1e-8,
-                            pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG"), 64 * 64
+                            pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG", precision=prec), 64 * 64
     if workload == "cylinder_re40":
         k = KRYLOV
         f = cases.cylinder(folder, h=0.02, ratio=1.03, points=157, nu=1.0 / 40, dt=0.01, nt=1000000,
-                           vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k)
+                           vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k,
+                           precision=prec)
         return f, 270 * 270
+    if workload == "cylinder_re550":
+        k = KRYLOV
+        f = cases.cylinder(folder, h=0.005, ratio=1.01, points=629, nu=1.0 / 550, dt=0.002, nt=1000000,
+                           vel_tol=1e-5, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k,
+                           precision=prec)
+        return f, 922 * 922
     raise SystemExit("unknown workload " + workload)
 
 

@@ -69,7 +69,8 @@ class Info(ctypes.Structure):
                [("dt", ctypes.c_double), ("nu", ctypes.c_double)] + \
                [(n, ctypes.c_int) for n in ("total_points", "bb_start_i", "bb_start_j", "bb_ncx", "bb_ncy",
                                             "nnz_lhs1", "nnz_lhs2", "velocity_precond", "poisson_precond",
-                                            "velocity_krylov", "poisson_krylov", "amg_levels")]
+                                            "velocity_krylov", "poisson_krylov", "amg_levels",
+                                            "velocity_precision", "poisson_precision")]
 
 
 _lib = None

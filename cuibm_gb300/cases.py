@@ -63,7 +63,10 @@ def write_case(folder, sim, flow, domain, bodies):
 
 
 def solvers(vel_pc="DIAGONAL", vel_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", pois_tol=1e-5, vel_krylov=None,
-            pois_krylov=None, vel_maxit=10000, pois_maxit=20000):
+            pois_krylov=None, vel_maxit=10000, pois_maxit=20000, precision=None):
+    """The linearSolvers entries; precision "MIXED" runs both solves' multigrid cycles
+    (or, without one, inner solves) in FP32 under FP64 Krylov iterations (an extension
+    of the reference's schema)."""
     v = {"system": "velocity", "solver": "CG", "preconditioner": vel_pc, "tolerance": vel_tol,
          "maxIterations": vel_maxit}
     p = {"system": "Poisson", "solver": "CG", "preconditioner": pois_pc, "tolerance": pois_tol,
@@ -72,6 +75,8 @@ def solvers(vel_pc="DIAGONAL", vel_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", poi
         v["krylov"] = vel_krylov
     if pois_krylov:
         p["krylov"] = pois_krylov
+    if precision:
+        v["precision"] = p["precision"] = precision
     return [v, p]
 
 
@@ -91,11 +96,13 @@ def axis(direction, start, mid_h, subs):
 
 
 def cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000, nsave=None, lid=1.0, vel_tol=1e-8, pois_tol=1e-8,
-           pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG", vel_pc="DIAGONAL", vel_krylov=None, extra=None):
+           pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG", vel_pc="DIAGONAL", vel_krylov=None, extra=None,
+           precision=None):
     """Lid-driven cavity on [0,1]^2, uniform n x n cells, fluid at rest."""
     sim = {"type": "simulation", "dt": float(dt), "nt": int(nt), "nsave": int(nsave or nt),
            "SolverType": "NAVIER_STOKES_SOLVER",
-           "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov)}
+           "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov,
+                                    precision=precision)}
     if extra:
         sim.update(extra)
     flow = [{"type": "flow", "nu": float(nu), "initialVelocity": [0.0, 0.0], "initialPerturbation": [0.0, 0.0],
@@ -108,10 +115,11 @@ def cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000, nsave=None, lid=1.0, vel_tol
 def cylinder(folder, h=0.02, ratio=1.03, extent=15.0, core=0.6, points=157, nu=1.0 / 40, dt=0.01, nt=2000,
              nsave=None, method="LUO", vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION",
              pois_krylov=None, vel_krylov=None, vel_pc="DIAGONAL", radius=0.5, scaleCV=None, motion=None,
-             uinf=1.0, quiescent=False):
+             uinf=1.0, quiescent=False, precision=None):
     """Circle of diameter 2*radius at the origin in [-extent, extent]^2."""
     sim = {"type": "simulation", "dt": float(dt), "nt": int(nt), "nsave": int(nsave or nt), "SolverType": method,
-           "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov)}
+           "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov,
+                                    precision=precision)}
     if scaleCV is not None:
         sim["scaleCV"] = float(scaleCV)
     u0 = 0.0 if quiescent else float(uinf)

@@ -297,6 +297,12 @@ std::string parse_simulation(const Node *doc, Params &P)
                 ls.precond = precond_from(precond);
                 ls.tolerance = tol;
                 ls.maxIterations = maxIter;
+                if (s->get("precision")) {
+                    const std::string &pv = s->get("precision")->text;
+                    if (pv == "MIXED") ls.precision = PRECISION_MIXED;
+                    else if (pv == "DOUBLE" || pv == "FP64") ls.precision = PRECISION_FP64;
+                    else return "simParams.yaml: precision must be DOUBLE (or FP64) or MIXED";
+                }
                 int kry = KRYLOV_BICGSTAB;
                 if (s->get("krylov")) {
                     const std::string &kv = s->get("krylov")->text;

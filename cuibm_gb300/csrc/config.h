@@ -13,6 +13,7 @@ enum Boundary { XMINUS = 0, XPLUS = 1, YMINUS = 2, YPLUS = 3 };
 enum BcType { DIRICHLET = 0, NEUMANN, CONVECTIVE, PERIODIC, SPECIAL };
 enum Precond { PC_NONE = 0, PC_DIAGONAL = 1, PC_SMOOTHED_AGGREGATION = 2, PC_AINV = 3 };
 enum Krylov { KRYLOV_BICGSTAB = 0, KRYLOV_CG = 1 };
+enum Precision { PRECISION_FP64 = 0, PRECISION_MIXED = 1 };
 enum SolverType { ST_NAVIERSTOKES = 0, ST_FADLUN = 1, ST_OSC = 2, ST_FSI = 3, ST_LUO = 4 };
 
 struct LinearSolve {
@@ -20,6 +21,7 @@ struct LinearSolve {
     int precond = PC_DIAGONAL;
     double tolerance = 1e-5;
     int maxIterations = 10000;
+    int precision = PRECISION_FP64;  // `precision: MIXED`: FP32 multigrid cycles / inner solves, FP64 Krylov
 };
 
 struct AxisDesc {

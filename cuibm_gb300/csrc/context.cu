@@ -519,6 +519,8 @@ int cuibm_get_info(const cuibm_ctx *h, cuibm_info *info)
     info->poisson_precond = c.P.poisson.precond;
     info->velocity_krylov = c.P.krylovVelocity;
     info->poisson_krylov = c.P.krylovPoisson;
+    info->velocity_precision = c.P.velocity.precision;
+    info->poisson_precision = c.P.poisson.precision;
     info->amg_levels = (int)c.sys2.amg.size();
     return CUIBM_OK;
 }
@@ -871,6 +873,8 @@ int cuibm_case_info(const char *folder, int argc, const char **argv, cuibm_info 
     info->poisson_precond = hc.P.poisson.precond;
     info->velocity_krylov = hc.P.krylovVelocity;
     info->poisson_krylov = hc.P.krylovPoisson;
+    info->velocity_precision = hc.P.velocity.precision;
+    info->poisson_precision = hc.P.poisson.precision;
     return CUIBM_OK;
 }
 
@@ -911,6 +915,8 @@ void cuibm_destroy(cuibm_ctx *h)
     if (c.step_graph) cudaGraphDestroy(c.step_graph);
     free_sa_hierarchy(c.sys1);
     free_sa_hierarchy(c.sys2);
+    free_fused(c.sys1);
+    free_fused(c.sys2);
     if (c.arena) cudaFree(c.arena);
     if (c.h_scalars) cudaFreeHost(c.h_scalars);
     if (c.ev0) cudaEventDestroy(c.ev0);

@@ -34,6 +34,25 @@
 // count are those of the stepwise kernels in krylov.cu; results agree with them
 // to rounding.
 //
+// Mixed precision (a linear solver's `precision: MIXED`).  The Krylov code is also
+// instantiated for float vectors, operator tables and multigrid levels (dot products
+// still reduce in double), in two arrangements:
+//  * with the SA preconditioner (k_fused_mixed): an FP64 BiCGSTAB - residuals, dot
+//    products, updates and the stopping rule in FP64 - whose V-cycles run in FP32
+//    except the coarsest dense solve.  The pressure operator is nearly singular (its
+//    near-null space is the constant, pinned at one cell), and FP32 rounding inside
+//    the cycle leaves a spurious constant in its output; each preconditioned vector z
+//    therefore gets its constant component re-solved in FP64, z = y + c e with
+//    c = (e.r - w.y) / E, w = A^T e, E = e^T A e - the coarse correction of the
+//    constant mode, which makes e^T (A z - r) = 0 whatever y's constant;
+//  * otherwise (k_fused_ir): iterative refinement around FP32 Krylov solves - the
+//    residual r = b - A x, its norm and the stopping test in FP64, an FP32 solve of
+//    A d = r to a relative tolerance of max(tol / (2 ||r||), 1e-3) in at most 100
+//    iterations, x += d in FP64 - until the FP64 residual meets the tolerance.
+// The FP64 work moves out of the preconditioner (most of an SA iteration) or out of
+// the whole iteration (refinement), and FP32 vectors and matrix values take half the
+// bytes; GB300's FP32 rate is about fifty times its FP64 rate.
+//
 // Barrier waits are bounded: a block that waits more than kBarrierTimeoutNs
 // sets the abort word and returns, every other block leaves at its next
 // barrier, and the host reports the failure.  Vectors written inside the
@@ -57,21 +76,30 @@ constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 constexpr int kGroupR = 8;  // lanes per restriction row (15-30 entries)
 constexpr int kGroupA = 4;  // lanes per coarse-operator row (9-25 entries)
 
+template <class T>
+struct CsrV {
+    int n, nnz;
+    const int *ptr, *col;
+    const T *val;
+};
+
+template <class T>
 struct FLevel {
     int n;
-    DevCsr A, P, R, AP;
-    const double *wd;  // omega D^-1
-    double *x, *b, *r, *t;
-    const double *inv;  // coarsest level: dense inverse
+    CsrV<T> A, P, R, AP;
+    const T *wd;  // omega D^-1
+    T *x, *b, *r, *t;
+    const double *inv;  // coarsest level: dense inverse, FP64 in every precision (dense_solve)
 };
 
 // Everything a solve needs except its right-hand side and solution, built once
 // per system and kept in device memory (the kernel reads it through a pointer:
 // a struct this size indexed by level would otherwise be copied to local memory).
+template <class T>
 struct FArgs {
     int n;
-    double *r, *rs, *p, *p2, *Mp, *AMp, *AMp2, *s, *Ms, *AMs, *z, *q;
-    const double *dinv, *w, *winv, *diag;
+    T *r, *rs, *p, *p2, *Mp, *AMp, *AMp2, *s, *Ms, *AMs, *z, *q;
+    const T *dinv, *w, *winv, *diag;
     double *partials;  // 2 x gridDim x 4
     FusedSyncState *sync;
     unsigned long long *trace;  // [count, stamps...] of kTraceLen, or null
@@ -79,35 +107,77 @@ struct FArgs {
     int *err;
     int which;
     int nlev;
-    FLevel lev[kMaxLevels];
+    FLevel<T> lev[kMaxLevels];
+    // mixed precision, float side: the FP32 cycle's input (SA) or the inner system's
+    // right-hand side and solution (refinement)
+    T *bin, *xin;
+    // mixed precision with SA, FP64 side: the FP32 cycle's output and the constant-mode
+    // correction (wdef = A^T e, Edef = e^T A e; wdef null: no correction)
+    double *ym;
+    const double *wdef;
+    double Edef;
 };
 
+// coefficient tables of the structured operators in the solver's precision
+template <class T>
+struct Lhs1T {
+    const T *uE, *uW, *uN, *uS, *vE, *vW, *vN, *vS;
+    RowPatch patch;
+    const T *rscale;
+};
+template <class T>
+struct Lhs2T {
+    const T *E, *W, *N, *S;
+    int pin0, pinc;
+    RowPatch patch;
+};
+
+static Lhs1T<double> tab64(const Lhs1Coef &c)
+{
+    return Lhs1T<double>{c.uE, c.uW, c.uN, c.uS, c.vE, c.vW, c.vN, c.vS, c.patch, c.rscale};
+}
+static Lhs2T<double> tab64(const Lhs2Coef &c) { return Lhs2T<double>{c.E, c.W, c.N, c.S, c.pin0, c.pinc, c.patch}; }
+
+// a patched row (FP64 entries, applied in T)
+template <class T, class X>
+__device__ __forceinline__ T patch_row_t(const RowPatch &P, int k, T xi, const X &x)
+{
+    T y = (T)P.pdiag[k] * xi;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        const int j = P.pcol[5 * k + m];
+        if (j >= 0) y += (T)P.pval[5 * k + m] * x(j);
+    }
+    return y;
+}
+
 // ---- operators with a precomputed diagonal ---------------------------------------
+template <class T>
 struct Op1D {
-    Lhs1Coef c;
+    Lhs1T<T> c;
     Grid g;
-    const double *diag, *w;
+    const T *diag, *w;
     template <class X>
-    __device__ __forceinline__ double row(int i, const X &x) const
+    __device__ __forceinline__ T row(int i, const X &x) const
     {
         return row_x(i, x(i), x);
     }
     // the row with the own value given (it is often at hand already)
     template <class X>
-    __device__ __forceinline__ double row_x(int i, double xi, const X &x) const
+    __device__ __forceinline__ T row_x(int i, T xi, const X &x) const
     {
         if (c.patch.pid) {
             const int k = c.patch.pid[i];
             if (k >= 0) {
-                const double y = patch_row(c.patch, k, xi, x);
+                const T y = patch_row_t<T>(c.patch, k, xi, x);
                 return w ? w[i] * y : y;
             }
         }
         const int wu = g.nx - 1;
         // embedded method: the off-diagonal part is scaled by rscale (diag[i] carries it
         // already); the other methods sum the row in the order of lhs1_row_f
-        const double *rs = c.rscale;
-        double o = rs ? 0.0 : diag[i] * xi;
+        const T *rs = c.rscale;
+        T o = rs ? T(0) : diag[i] * xi;
         if (i < g.nU) {
             const int I = i % wu, J = i / wu;
             if (I != g.nx - 2) o -= c.uE[I] * x(i + 1);
@@ -121,31 +191,32 @@ struct Op1D {
             if (J != g.ny - 2) o -= c.vN[J] * x(i + g.nx);
             if (J != 0) o -= c.vS[J] * x(i - g.nx);
         }
-        const double y = rs ? diag[i] * xi + o * rs[i] : o;
+        const T y = rs ? diag[i] * xi + o * rs[i] : o;
         return w ? w[i] * y : y;
     }
 };
+template <class T>
 struct Op2D {
-    Lhs2Coef c;
+    Lhs2T<T> c;
     Grid g;
-    const double *diag, *w;
+    const T *diag, *w;
     template <class X>
-    __device__ __forceinline__ double row(int i, const X &x) const
+    __device__ __forceinline__ T row(int i, const X &x) const
     {
         return row_x(i, x(i), x);
     }
     template <class X>
-    __device__ __forceinline__ double row_x(int i, double xi, const X &x) const
+    __device__ __forceinline__ T row_x(int i, T xi, const X &x) const
     {
         if (c.patch.pid) {
             const int k = c.patch.pid[i];
             if (k >= 0) {
-                const double y = patch_row(c.patch, k, xi, x);
+                const T y = patch_row_t<T>(c.patch, k, xi, x);
                 return w ? w[i] * y : y;
             }
         }
         const int I = i % g.nx, J = i / g.nx;
-        double y = diag[i] * xi;
+        T y = diag[i] * xi;
         if (I != g.nx - 1) y -= c.E[I] * x(i + 1);
         if (I != 0) y -= c.W[I] * x(i - 1);
         if (J != g.ny - 1) y -= c.N[J] * x(i + g.nx);
@@ -155,39 +226,58 @@ struct Op2D {
 };
 
 // ---- vector access inside the persistent kernel ----------------------------------
+template <class T>
 struct LdAcc {
-    const double *p;
-    __device__ __forceinline__ double operator()(int j) const { return __ldcg(p + j); }
+    const T *p;
+    __device__ __forceinline__ T operator()(int j) const { return __ldcg(p + j); }
 };
-template <class F>
+template <class T>
+__device__ __forceinline__ LdAcc<T> acc(const T *p)
+{
+    return LdAcc<T>{p};
+}
+struct LdShift {  // y + c (the FP32 cycle's output with its constant re-solved)
+    const double *y;
+    double c;
+    __device__ __forceinline__ double operator()(int j) const { return __ldcg(y + j) + c; }
+};
+template <class F, class T>
 struct LdScale {  // f .* d (right Jacobi, or the first damped-Jacobi sweep with d = omega D^-1)
     F f;
-    const double *d;
-    __device__ __forceinline__ double operator()(int j) const { return d[j] * f(j); }
+    const T *d;
+    __device__ __forceinline__ T operator()(int j) const { return d[j] * f(j); }
 };
+template <class F, class T>
+__device__ __forceinline__ LdScale<F, T> scaled(const F &f, const T *d)
+{
+    return LdScale<F, T>{f, d};
+}
+template <class T>
 struct LdPnew {  // CG direction z + beta p
-    const double *z, *p;
-    double beta;
-    __device__ __forceinline__ double operator()(int j) const { return __ldcg(z + j) + beta * __ldcg(p + j); }
+    const T *z, *p;
+    T beta;
+    __device__ __forceinline__ T operator()(int j) const { return __ldcg(z + j) + beta * __ldcg(p + j); }
 };
+template <class T>
 struct LdAxpy {  // u - a v: the CG residual r - alpha q, the BiCGSTAB half step r - alpha A M p
-    const double *u, *v;
-    double a;
-    __device__ __forceinline__ double operator()(int j) const { return __ldcg(u + j) - a * __ldcg(v + j); }
+    const T *u, *v;
+    T a;
+    __device__ __forceinline__ T operator()(int j) const { return __ldcg(u + j) - a * __ldcg(v + j); }
 };
+template <class T>
 struct LdBicgDir {  // BiCGSTAB direction r + beta (p - omega A M p)
-    const double *r, *p, *AMp;
-    double beta, omega;
-    __device__ __forceinline__ double operator()(int j) const
+    const T *r, *p, *AMp;
+    T beta, omega;
+    __device__ __forceinline__ T operator()(int j) const
     {
         return __ldcg(r + j) + beta * (__ldcg(p + j) - omega * __ldcg(AMp + j));
     }
 };
 
-template <class X>
-__device__ __forceinline__ double csr_row(const DevCsr &M, int i, const X &x)
+template <class T, class X>
+__device__ __forceinline__ T csr_row(const CsrV<T> &M, int i, const X &x)
 {
-    double s = 0;
+    T s = 0;
     const int k1 = M.ptr[i + 1];
 #pragma unroll 4
     for (int k = M.ptr[i]; k < k1; ++k) s += M.val[k] * x(M.col[k]);
@@ -201,11 +291,11 @@ __device__ __forceinline__ unsigned group_mask()
 }
 
 // one CSR row split over G lanes; every lane of the group gets the sum
-template <int G, class X>
-__device__ __forceinline__ double csr_row_g(const DevCsr &M, int i, const X &x)
+template <int G, class T, class X>
+__device__ __forceinline__ T csr_row_g(const CsrV<T> &M, int i, const X &x)
 {
     const int sub = threadIdx.x & (G - 1);
-    double s = 0;
+    T s = 0;
     const int k1 = M.ptr[i + 1];
     for (int k = M.ptr[i] + sub; k < k1; k += G) s += M.val[k] * x(M.col[k]);
 #pragma unroll
@@ -279,9 +369,10 @@ __device__ bool grid_sync(FusedSyncState *st, unsigned long long *trace)
 // totals into NO scalars with fn - the same arithmetic in every block, so every
 // block takes the same decisions - and the block reads them from shared memory
 // (the square roots and divisions of the recurrences run once per block, not
-// once per thread: FP64 issue is the scarce resource).
-template <int NV, int NO, class Fn>
-__device__ bool grid_reduce(const double (&v)[NV], const FArgs &a, int &parity, const Fn &fn, double (&o)[NO])
+// once per thread: FP64 issue is the scarce resource).  The per-thread values
+// are summed in double whatever the vectors' precision.
+template <int NV, int NO, class A, class Fn>
+__device__ bool grid_reduce(const double (&v)[NV], const A &a, int &parity, const Fn &fn, double (&o)[NO])
 {
     __shared__ double sh[NV][32];
     __shared__ double res[NO];
@@ -326,13 +417,22 @@ __device__ bool grid_reduce(const double (&v)[NV], const FArgs &a, int &parity, 
     return true;
 }
 
-template <int NV>
-__device__ __forceinline__ bool grid_sum(const double (&v)[NV], double (&tot)[NV], const FArgs &a, int &parity)
+// per-thread partial sums kept in T, handed to the reduction in double
+template <class T, int N>
+__device__ __forceinline__ void to_double(const T (&v)[N], double (&d)[N])
 {
-    return grid_reduce<NV, NV>(v, a, parity, [](const double (&t)[NV], double (&o)[NV]) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) o[k] = t[k];
-    }, tot);
+    for (int k = 0; k < N; ++k) d[k] = (double)v[k];
+}
+
+// An FP32 inner solve (refinement) stops at a breakdown - a non-finite or zero
+// recurrence scalar - keeping the iterate it has; the FP64 refinement around it
+// measures the true residual and goes on.  FP64 solves keep the reference's
+// behaviour (the non-finite residual is reported).
+template <class T>
+__device__ __forceinline__ bool inner_breakdown(double v)
+{
+    return sizeof(T) == 4 && !(isfinite(v) && v != 0.0);
 }
 
 __device__ __forceinline__ int solve_state(double rnorm, double tol, int it, int maxit)
@@ -350,22 +450,25 @@ __device__ __forceinline__ int solve_state(double rnorm, double tol, int it, int
 
 // First phase on level 0 for one row, with the input given by an accessor:
 // r_0 = b - A (w D^-1 b).  The caller adds its own per-row work and the barrier.
-template <class Op, class B>
-__device__ __forceinline__ void vcycle_residual0_row(const Op &A, const FLevel &V, int i, const B &b, double bi)
+template <class Op, class T, class B>
+__device__ __forceinline__ void vcycle_residual0_row(const Op &A, const FLevel<T> &V, int i, const B &b, T bi)
 {
-    V.r[i] = bi - A.row_x(i, V.wd[i] * bi, LdScale<B>{b, V.wd});
+    V.r[i] = bi - A.row_x(i, V.wd[i] * bi, scaled(b, V.wd));
 }
 
 // Coarsest level: x = A^-1 b with the dense inverse.  Each block stages b in
 // shared memory; a warp per row then streams the row of the inverse with many
-// loads in flight (they do not depend on one another).
+// loads in flight (they do not depend on one another).  The product runs in FP64
+// for the FP32 cycle too: the coarse pressure operator is nearly singular, its
+// inverse has entries of order 1/lambda_min, and an FP32 product of it is noise.
 constexpr int kDenseMax = 1536;  // the coarsest level's size limit (kCoarse in amg.cu is below it)
 
-__device__ __forceinline__ void dense_solve(const FLevel &C, const double *b, double *x)
+template <class T>
+__device__ __forceinline__ void dense_solve(const FLevel<T> &C, const T *b, T *x)
 {
     __shared__ double sb[kDenseMax];
     const int n = C.n;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = __ldcg(b + k);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = (double)__ldcg(b + k);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -379,76 +482,86 @@ __device__ __forceinline__ void dense_solve(const FLevel &C, const double *b, do
             acc1 += a[k + 32] * sb[k + 32];
         }
         if (k < n) acc0 += a[k] * sb[k];
-        double acc = acc0 + acc1;
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) x[row] = acc;
+        double s = acc0 + acc1;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) x[row] = (T)s;
     }
 }
 
 // The cycle after its first phase (r_0 written, barrier passed).  b0 is the
-// cycle's input (stored).  With dot, returns b0 . z.
-template <class Op>
-__device__ __forceinline__ bool vcycle_rest(const Op &A, const FArgs &a, const double *b0, double *zout, bool dot,
-                                            double rho_prev, double &rz, double &beta, int &parity)
+// cycle's input (stored); the output zout may have another precision.  With dot,
+// returns b0 . z; with wdot (and no dot), returns wdot . z in *wz.
+template <class Op, class T, class TO>
+__device__ __forceinline__ bool vcycle_rest(const Op &A, const FArgs<T> &a, const T *b0, TO *zout, bool dot,
+                                            double rho_prev, double &rz, double &beta, int &parity,
+                                            const double *wdot = nullptr, double *wz = nullptr)
 {
     const int L = a.nlev;
     for (int l = 0; l < L - 1; ++l) {
-        const FLevel &V = a.lev[l];
-        const FLevel &C = a.lev[l + 1];
+        const FLevel<T> &V = a.lev[l];
+        const FLevel<T> &C = a.lev[l + 1];
         if (l > 0) {
             FOR_GROUP_ROWS(kGroupA, i, V.n)
             {
-                const double ax = csr_row_g<kGroupA>(V.A, i, LdScale<LdAcc>{LdAcc{V.b}, V.wd});
+                const T ax = csr_row_g<kGroupA>(V.A, i, scaled(acc(V.b), V.wd));
                 if ((threadIdx.x & (kGroupA - 1)) == 0) V.r[i] = __ldcg(V.b + i) - ax;
             }
             if (!grid_sync(a.sync, a.trace)) return false;
         }
         FOR_GROUP_ROWS(kGroupR, i, C.n)
         {
-            const double bi = csr_row_g<kGroupR>(V.R, i, LdAcc{V.r});
+            const T bi = csr_row_g<kGroupR>(V.R, i, acc(V.r));
             if ((threadIdx.x & (kGroupR - 1)) == 0) C.b[i] = bi;
         }
         if (!grid_sync(a.sync, a.trace)) return false;
     }
-    const FLevel &C = a.lev[L - 1];
+    const FLevel<T> &C = a.lev[L - 1];
     dense_solve(C, C.b, C.x);
     if (!grid_sync(a.sync, a.trace)) return false;
-    const double *xc = C.x;
+    const T *xc = C.x;
     for (int l = L - 2; l >= 0; --l) {
-        const FLevel &V = a.lev[l];
-        const double *bb = l == 0 ? b0 : V.b;
-        double *out = l == 0 ? zout : V.t;
-        double v[1] = {0};
+        const FLevel<T> &V = a.lev[l];
+        const T *bb = l == 0 ? b0 : V.b;
+        T *out = V.t;  // levels above 0 (level 0 writes zout, in the output's precision)
+        T v[1] = {0};
+        double vw = 0;
         if (l == 0) {
             FOR_ROWS(i, V.n)
             {
-                const double wdi = V.wd[i];
-                const double xi = wdi * __ldcg(bb + i) + csr_row(V.P, i, LdAcc{xc});
-                const double o = xi + wdi * (__ldcg(V.r + i) - csr_row(V.AP, i, LdAcc{xc}));
-                out[i] = o;
+                const T wdi = V.wd[i];
+                const T xi = wdi * __ldcg(bb + i) + csr_row(V.P, i, acc(xc));
+                const T o = xi + wdi * (__ldcg(V.r + i) - csr_row(V.AP, i, acc(xc)));
+                zout[i] = (TO)o;
                 if (dot) v[0] += __ldcg(b0 + i) * o;
+                if (wdot) vw += wdot[i] * (double)o;
             }
         } else {
             FOR_GROUP_ROWS(kGroupA, i, V.n)
             {
-                const double px = csr_row_g<kGroupA>(V.P, i, LdAcc{xc});
-                const double apx = csr_row_g<kGroupA>(V.AP, i, LdAcc{xc});
+                const T px = csr_row_g<kGroupA>(V.P, i, acc(xc));
+                const T apx = csr_row_g<kGroupA>(V.AP, i, acc(xc));
                 if ((threadIdx.x & (kGroupA - 1)) == 0) {
-                    const double wdi = V.wd[i];
-                    const double xi = wdi * __ldcg(bb + i) + px;
+                    const T wdi = V.wd[i];
+                    const T xi = wdi * __ldcg(bb + i) + px;
                     out[i] = xi + wdi * (__ldcg(V.r + i) - apx);
                 }
             }
         }
         if (dot && l == 0) {
-            double q[2];
-            if (!grid_reduce<1, 2>(v, a, parity, [&](const double (&t)[1], double (&o)[2]) {
+            double vd[1], q[2];
+            to_double(v, vd);
+            if (!grid_reduce<1, 2>(vd, a, parity, [&](const double (&t)[1], double (&o)[2]) {
                     o[0] = t[0];
                     o[1] = t[0] / rho_prev;
                 }, q))
                 return false;
             rz = q[0];
             beta = q[1];
+        } else if (wdot && l == 0) {
+            double vd[1] = {vw}, q[1];
+            if (!grid_reduce<1, 1>(vd, a, parity, [&](const double (&t)[1], double (&o)[1]) { o[0] = t[0]; }, q))
+                return false;
+            *wz = q[0];
         } else if (!grid_sync(a.sync, a.trace)) {
             return false;
         }
@@ -459,17 +572,19 @@ __device__ __forceinline__ bool vcycle_rest(const Op &A, const FArgs &a, const d
 
 // z = V(b) for a stored input; with dot also rz = b . z and beta = rz / rho_prev.
 // A one-level hierarchy is the dense solve alone.
-template <class Op>
-__device__ __forceinline__ bool vcycle(const Op &A, const FArgs &a, const double *b, double *zout, bool dot,
+template <class Op, class T>
+__device__ __forceinline__ bool vcycle(const Op &A, const FArgs<T> &a, const T *b, T *zout, bool dot,
                                        double rho_prev, double &rz, double &beta, int &parity)
 {
     if (a.nlev == 1) {
         dense_solve(a.lev[0], b, zout);
         if (!grid_sync(a.sync, a.trace)) return false;
         if (!dot) return true;
-        double v[1] = {0}, q[2];
+        T v[1] = {0};
+        double vd[1], q[2];
         FOR_ROWS(i, a.lev[0].n) v[0] += __ldcg(b + i) * __ldcg(zout + i);
-        if (!grid_reduce<1, 2>(v, a, parity, [&](const double (&t)[1], double (&o)[2]) {
+        to_double(v, vd);
+        if (!grid_reduce<1, 2>(vd, a, parity, [&](const double (&t)[1], double (&o)[2]) {
                 o[0] = t[0];
                 o[1] = t[0] / rho_prev;
             }, q))
@@ -478,39 +593,54 @@ __device__ __forceinline__ bool vcycle(const Op &A, const FArgs &a, const double
         beta = q[1];
         return true;
     }
-    FOR_ROWS(i, a.lev[0].n) vcycle_residual0_row(A, a.lev[0], i, LdAcc{b}, __ldcg(b + i));
+    FOR_ROWS(i, a.lev[0].n) vcycle_residual0_row(A, a.lev[0], i, acc(b), __ldcg(b + i));
     if (!grid_sync(a.sync, a.trace)) return false;
     return vcycle_rest(A, a, b, zout, dot, rho_prev, rz, beta, parity);
+}
+
+// Mixed precision with SA: y = V(b32) in FP32 from b32, the float copy of an FP64
+// vector b that the caller wrote (with eb = e . b reduced) before its barrier; y goes
+// to the FP64 vector y.  The preconditioned vector is z = y + c e: with wdef set,
+// c = (e . b - wdef . y) / Edef re-solves its constant component in FP64.
+template <class Op32>
+__device__ __forceinline__ bool vcycle_mixed(const Op32 &A32, const FArgs<float> &f, const float *b32, double *y,
+                                             const double *wdef, double Edef, double eb, double &c, int &parity)
+{
+    FOR_ROWS(i, f.lev[0].n) vcycle_residual0_row(A32, f.lev[0], i, acc(b32), __ldcg(b32 + i));
+    if (!grid_sync(f.sync, f.trace)) return false;
+    double d0 = 0, d1 = 0, wy = 0;
+    if (!vcycle_rest(A32, f, b32, y, false, 1.0, d0, d1, parity, wdef, &wy)) return false;
+    c = wdef ? (eb - wy) / Edef : 0.0;
+    return true;
 }
 
 // ---- CG on the symmetrised system (W A) x = W b ---------------------------------------
 // With the SA preconditioner the update x += alpha p, r -= alpha q runs in the
 // same phase as the V-cycle's first sweep (which forms r - alpha q at its stencil
 // points; the residual is double-buffered).
-template <class Op, int PC>
-__device__ __forceinline__ bool cg_solve(const Op &A, const FArgs &a, const double *b, double *x, double (&out)[4],
-                                         int &it_out, int &status_out)
+template <class Op, int PC, class T>
+__device__ __forceinline__ bool cg_solve(const Op &A, const FArgs<T> &a, const T *b, T *x, double rtol, int maxit,
+                                         int &parity, double (&out)[4], int &it_out, int &status_out)
 {
-    int parity = 0;
-    const double rtol = a.ks->rtol;
-    const int maxit = a.ks->maxit;
     const bool merge = PC == 2 && a.nlev >= 2;
-    double v[3] = {0, 0, 0}, o[5];
+    T v[3] = {0, 0, 0};
+    double vd[3], o[5];
     FOR_ROWS(i, a.n)
     {
-        const double bi = b[i];
-        const double ri = a.w[i] * bi - A.row(i, LdAcc{x});
+        const T bi = b[i];
+        const T ri = a.w[i] * bi - A.row(i, acc(x));
         a.r[i] = ri;
-        const double ro = ri * a.winv[i];
+        const T ro = ri * a.winv[i];
         v[0] += ro * ro;
         v[1] += bi * bi;
         if (PC != 2) {
-            const double zi = PC == 1 ? ri * a.dinv[i] : ri;
+            const T zi = PC == 1 ? ri * a.dinv[i] : ri;
             a.z[i] = zi;
             v[2] += ri * zi;
         }
     }
-    if (!grid_reduce<3, 5>(v, a, parity, [&](const double (&t)[3], double (&q)[5]) {
+    to_double(v, vd);
+    if (!grid_reduce<3, 5>(vd, a, parity, [&](const double (&t)[3], double (&q)[5]) {
             q[0] = sqrt(t[0]);
             q[1] = sqrt(t[1]);
             q[2] = rtol * q[1];
@@ -523,56 +653,67 @@ __device__ __forceinline__ bool cg_solve(const Op &A, const FArgs &a, const doub
     double rho = o[3], beta = 0;
     int it = 0;
     int status = (int)o[4];
-    double *r = a.r, *rn = a.rs;
-    if (status == KS_RUNNING && PC == 2 && !vcycle(A, a, r, a.z, true, 1.0, rho, beta, parity)) return false;
-    double *p = a.p, *pn = a.p2;
+    T *r = a.r, *rn = a.rs;
+    if (status == KS_RUNNING && PC == 2 && !vcycle(A, a, (const T *)r, a.z, true, 1.0, rho, beta, parity))
+        return false;
+    T *p = a.p, *pn = a.p2;
     bool first = true;
     while (status == KS_RUNNING) {
         // direction pn = z + beta p, q = A pn, pn . q
-        double v1[1] = {0}, o1[1];
+        const T bt = (T)beta;
+        T v1[1] = {0};
+        double v1d[1], o1[1];
         FOR_ROWS(i, a.n)
         {
-            const double zi = __ldcg(a.z + i);
-            double pi, qi;
+            const T zi = __ldcg(a.z + i);
+            T pi, qi;
             if (first) {
                 pi = zi;
-                qi = A.row_x(i, pi, LdAcc{a.z});
+                qi = A.row_x(i, pi, acc((const T *)a.z));
             } else {
-                pi = zi + beta * __ldcg(p + i);
-                qi = A.row_x(i, pi, LdPnew{a.z, p, beta});
+                pi = zi + bt * __ldcg(p + i);
+                qi = A.row_x(i, pi, LdPnew<T>{a.z, p, bt});
             }
             pn[i] = pi;
             a.q[i] = qi;
             v1[0] += pi * qi;
         }
-        if (!grid_reduce<1, 1>(v1, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = rho / t[0]; }, o1))
+        to_double(v1, v1d);
+        if (!grid_reduce<1, 1>(v1d, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = rho / t[0]; }, o1))
             return false;
         const double alpha = o1[0];
+        if (inner_breakdown<T>(alpha)) {
+            status = KS_STALLED;
+            break;
+        }
+        const T at = (T)alpha;
         {
-            double *tmp = p;
+            T *tmp = p;
             p = pn;
             pn = tmp;
         }
         first = false;
         if (merge) {
-            const LdAxpy rnew{r, a.q, alpha};
-            double v2[1] = {0}, o2[2];
+            const LdAxpy<T> rnew{r, a.q, at};
+            T v2[1] = {0};
+            double v2d[1], o2[2];
             FOR_ROWS(i, a.n)
             {
-                x[i] = __ldcg(x + i) + alpha * __ldcg(p + i);
-                const double ri = rnew(i);
+                x[i] = __ldcg(x + i) + at * __ldcg(p + i);
+                const T ri = rnew(i);
                 rn[i] = ri;
-                const double ro = ri * a.winv[i];
+                const T ro = ri * a.winv[i];
                 v2[0] += ro * ro;
                 vcycle_residual0_row(A, a.lev[0], i, rnew, ri);
             }
-            if (!grid_reduce<1, 2>(v2, a, parity, [&](const double (&t)[1], double (&q)[2]) {
+            to_double(v2, v2d);
+            if (!grid_reduce<1, 2>(v2d, a, parity, [&](const double (&t)[1], double (&q)[2]) {
                     q[0] = sqrt(t[0]);
                     q[1] = solve_state(q[0], tol, it + 1, maxit);
                 }, o2))
                 return false;
             {
-                double *tmp = r;
+                T *tmp = r;
                 r = rn;
                 rn = tmp;
             }
@@ -581,25 +722,31 @@ __device__ __forceinline__ bool cg_solve(const Op &A, const FArgs &a, const doub
             status = (int)o2[1];
             if (status != KS_RUNNING) break;
             double rz = 0;
-            if (!vcycle_rest(A, a, r, a.z, true, rho, rz, beta, parity)) return false;
+            if (!vcycle_rest(A, a, (const T *)r, a.z, true, rho, rz, beta, parity)) return false;
             rho = rz;
+            if (inner_breakdown<T>(beta)) {
+                status = KS_STALLED;
+                break;
+            }
             continue;
         }
-        double v2[2] = {0, 0}, o2[4];
+        T v2[2] = {0, 0};
+        double v2d[2], o2[4];
         FOR_ROWS(i, a.n)
         {
-            x[i] = __ldcg(x + i) + alpha * __ldcg(p + i);
-            const double ri = __ldcg(r + i) - alpha * __ldcg(a.q + i);
+            x[i] = __ldcg(x + i) + at * __ldcg(p + i);
+            const T ri = __ldcg(r + i) - at * __ldcg(a.q + i);
             r[i] = ri;
-            const double ro = ri * a.winv[i];
+            const T ro = ri * a.winv[i];
             v2[0] += ro * ro;
             if (PC != 2) {
-                const double zi = PC == 1 ? ri * a.dinv[i] : ri;
+                const T zi = PC == 1 ? ri * a.dinv[i] : ri;
                 a.z[i] = zi;
                 v2[1] += ri * zi;
             }
         }
-        if (!grid_reduce<2, 4>(v2, a, parity, [&](const double (&t)[2], double (&q)[4]) {
+        to_double(v2, v2d);
+        if (!grid_reduce<2, 4>(v2d, a, parity, [&](const double (&t)[2], double (&q)[4]) {
                 q[0] = sqrt(t[0]);
                 q[1] = solve_state(q[0], tol, it + 1, maxit);
                 q[2] = PC != 2 ? t[1] / rho : 0.0;
@@ -616,8 +763,12 @@ __device__ __forceinline__ bool cg_solve(const Op &A, const FArgs &a, const doub
         if (status != KS_RUNNING) break;
         if (PC == 2) {
             double rz = 0;
-            if (!vcycle(A, a, r, a.z, true, rho, rz, beta, parity)) return false;
+            if (!vcycle(A, a, (const T *)r, a.z, true, rho, rz, beta, parity)) return false;
             rho = rz;
+        }
+        if (inner_breakdown<T>(beta)) {
+            status = KS_STALLED;
+            break;
         }
     }
     out[0] = rnorm;
@@ -637,26 +788,29 @@ __device__ __forceinline__ bool cg_solve(const Op &A, const FArgs &a, const doub
 // Phases per iteration: Jacobi or none - 3 (the direction update rides on the
 // next A M p, the half step on A M s); SA - 2 V-cycles + 3 (the direction
 // update rides on the first V-cycle sweep, the half step on the second).
-template <class Op, int PC>
-__device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs &a, const double *b, double *x,
-                                           double (&out)[4], int &it_out, int &status_out)
+// MX (mixed precision with SA, T = double): the V-cycles run in FP32 (A32, f) on
+// float copies written in the direction and half-step phases, their outputs get the
+// constant-mode correction, and M p, M s are written in the phases that apply A.
+template <class Op, int PC, class T, bool MX = false, class Op32 = Op>
+__device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const T *b, T *x, double rtol, int maxit,
+                                           int &parity, double (&out)[4], int &it_out, int &status_out,
+                                           const Op32 *A32 = nullptr, const FArgs<float> *f = nullptr)
 {
-    int parity = 0;
-    const double rtol = a.ks->rtol;
-    const int maxit = a.ks->maxit;
     const bool sa_multi = PC == 2 && a.nlev >= 2;
-    double v[2] = {0, 0}, o[5];
+    T v[2] = {0, 0};
+    double vd[2], o[5];
     FOR_ROWS(i, a.n)
     {
-        const double bi = b[i];
-        const double ri = bi - A.row(i, LdAcc{x});
+        const T bi = b[i];
+        const T ri = bi - A.row(i, acc(x));
         a.r[i] = ri;
         a.rs[i] = ri;
         a.p[i] = ri;
         v[0] += ri * ri;
         v[1] += bi * bi;
     }
-    if (!grid_reduce<2, 5>(v, a, parity, [&](const double (&t)[2], double (&q)[5]) {
+    to_double(v, vd);
+    if (!grid_reduce<2, 5>(vd, a, parity, [&](const double (&t)[2], double (&q)[5]) {
             q[0] = t[0];
             q[1] = sqrt(t[0]);
             q[2] = sqrt(t[1]);
@@ -670,87 +824,133 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs &a, const do
     int status = (int)o[4];
     // p and A M p are double-buffered: the direction update reads the old ones
     // at the stencil points of the phase that writes the new ones
-    double *p = a.p, *pn = a.p2, *amp = a.AMp, *ampn = a.AMp2;
+    T *p = a.p, *pn = a.p2, *amp = a.AMp, *ampn = a.AMp2;
     double beta = 0, omega = 1;
     bool first = true;
-    double dummy = 0, dummy2 = 0;
+    double dummy = 0, dummy2 = 0, cmx = 0;
     while (status == KS_RUNNING) {
         // ---- new direction (folded), Mp = M p, A Mp, rs . A Mp
-        const LdBicgDir dir{a.r, p, amp, beta, omega};
+        const LdBicgDir<T> dir{a.r, p, amp, (T)beta, (T)omega};
         if (PC == 2) {
-            if (sa_multi) {
+            if (MX) {
+                T ve[1] = {0};
+                FOR_ROWS(i, a.n)
+                {
+                    T pi;
+                    if (first) {
+                        pi = __ldcg(p + i);
+                    } else {
+                        pi = dir(i);
+                        pn[i] = pi;
+                    }
+                    f->bin[i] = (float)pi;
+                    ve[0] += pi;
+                }
+                double ved[1], eb[1];
+                to_double(ve, ved);
+                if (!grid_reduce<1, 1>(ved, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = t[0]; },
+                                       eb))
+                    return false;
+                if (!first) {
+                    T *tmp = p;
+                    p = pn;
+                    pn = tmp;
+                }
+                if (!vcycle_mixed(*A32, *f, f->bin, a.ym, a.wdef, a.Edef, eb[0], cmx, parity)) return false;
+            } else if (sa_multi) {
                 FOR_ROWS(i, a.n)
                 {
                     if (first) {
-                        vcycle_residual0_row(A, a.lev[0], i, LdAcc{p}, __ldcg(p + i));
+                        vcycle_residual0_row(A, a.lev[0], i, acc((const T *)p), __ldcg(p + i));
                     } else {
-                        const double pi = dir(i);
+                        const T pi = dir(i);
                         pn[i] = pi;
                         vcycle_residual0_row(A, a.lev[0], i, dir, pi);
                     }
                 }
                 if (!grid_sync(a.sync, a.trace)) return false;
                 if (!first) {
-                    double *tmp = p;
+                    T *tmp = p;
                     p = pn;
                     pn = tmp;
                 }
-                if (!vcycle_rest(A, a, p, a.Mp, false, 1.0, dummy, dummy2, parity)) return false;
+                if (!vcycle_rest(A, a, (const T *)p, a.Mp, false, 1.0, dummy, dummy2, parity)) return false;
             } else {
                 if (!first) {
                     FOR_ROWS(i, a.n) pn[i] = dir(i);
                     if (!grid_sync(a.sync, a.trace)) return false;
-                    double *tmp = p;
+                    T *tmp = p;
                     p = pn;
                     pn = tmp;
                 }
-                if (!vcycle(A, a, p, a.Mp, false, 1.0, dummy, dummy2, parity)) return false;
+                if (!vcycle(A, a, (const T *)p, a.Mp, false, 1.0, dummy, dummy2, parity)) return false;
             }
         }
-        double v1[1] = {0}, o1[1];
+        T v1[1] = {0};
+        double v1d[1], o1[1];
         FOR_ROWS(i, a.n)
         {
-            double ai;
-            if (PC == 2) {
-                ai = A.row(i, LdAcc{a.Mp});
+            T ai;
+            if (PC == 2 && MX) {
+                const double mi = __ldcg(a.ym + i) + cmx;
+                a.Mp[i] = (T)mi;
+                ai = A.row_x(i, (T)mi, LdShift{a.ym, cmx});
+            } else if (PC == 2) {
+                ai = A.row(i, acc((const T *)a.Mp));
             } else if (first) {
-                const double pi = __ldcg(p + i);
-                const double mpi = PC == 1 ? a.dinv[i] * pi : pi;
+                const T pi = __ldcg(p + i);
+                const T mpi = PC == 1 ? a.dinv[i] * pi : pi;
                 a.Mp[i] = mpi;
-                ai = PC == 1 ? A.row_x(i, mpi, LdScale<LdAcc>{LdAcc{p}, a.dinv}) : A.row_x(i, mpi, LdAcc{p});
+                ai = PC == 1 ? A.row_x(i, mpi, scaled(acc((const T *)p), a.dinv)) : A.row_x(i, mpi, acc((const T *)p));
             } else {
-                const double pi = dir(i);
+                const T pi = dir(i);
                 pn[i] = pi;
-                const double mpi = PC == 1 ? a.dinv[i] * pi : pi;
+                const T mpi = PC == 1 ? a.dinv[i] * pi : pi;
                 a.Mp[i] = mpi;
-                ai = PC == 1 ? A.row_x(i, mpi, LdScale<LdBicgDir>{dir, a.dinv}) : A.row_x(i, mpi, dir);
+                ai = PC == 1 ? A.row_x(i, mpi, scaled(dir, a.dinv)) : A.row_x(i, mpi, dir);
             }
             ampn[i] = ai;
             v1[0] += __ldcg(a.rs + i) * ai;
         }
-        if (!grid_reduce<1, 1>(v1, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = rho / t[0]; }, o1))
+        to_double(v1, v1d);
+        if (!grid_reduce<1, 1>(v1d, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = rho / t[0]; }, o1))
             return false;
         if (PC != 2 && !first) {
-            double *tmp = p;
+            T *tmp = p;
             p = pn;
             pn = tmp;
         }
         {
-            double *tmp = amp;
+            T *tmp = amp;
             amp = ampn;
             ampn = tmp;
         }
         first = false;
         const double alpha = o1[0];
+        if (inner_breakdown<T>(alpha)) {
+            status = KS_STALLED;
+            break;
+        }
+        const T at = (T)alpha;
         // ---- half step s = r - alpha A Mp (folded into the application of M and A to s)
-        const LdAxpy snew{a.r, amp, alpha};
+        const LdAxpy<T> snew{a.r, amp, at};
         double o3[3];  // snorm, half-step convergence, omega
         if (PC == 2) {
-            double v2[1] = {0};
-            if (sa_multi) {
+            T v2[2] = {0, 0};
+            double v2d[2], o2[2];
+            if (MX) {
                 FOR_ROWS(i, a.n)
                 {
-                    const double si = snew(i);
+                    const T si = snew(i);
+                    a.s[i] = si;
+                    v2[0] += si * si;
+                    v2[1] += si;
+                    f->bin[i] = (float)si;
+                }
+            } else if (sa_multi) {
+                FOR_ROWS(i, a.n)
+                {
+                    const T si = snew(i);
                     a.s[i] = si;
                     v2[0] += si * si;
                     vcycle_residual0_row(A, a.lev[0], i, snew, si);
@@ -758,80 +958,103 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs &a, const do
             } else {
                 FOR_ROWS(i, a.n)
                 {
-                    const double si = snew(i);
+                    const T si = snew(i);
                     a.s[i] = si;
                     v2[0] += si * si;
                 }
             }
-            if (!grid_reduce<1, 3>(v2, a, parity, [&](const double (&t)[1], double (&q)[3]) {
+            to_double(v2, v2d);
+            if (!grid_reduce<2, 2>(v2d, a, parity, [&](const double (&t)[2], double (&q)[2]) {
                     q[0] = sqrt(t[0]);
-                    q[1] = q[0] <= tol;
-                    q[2] = 0;
-                }, o3))
+                    q[1] = t[1];
+                }, o2))
                 return false;
+            o3[0] = o2[0];
+            o3[1] = o2[0] <= tol;
             if (o3[1] != 0) {
-                FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + alpha * __ldcg(a.Mp + i);
+                FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + at * __ldcg(a.Mp + i);
                 rnorm = o3[0];
                 status = KS_CONVERGED;
                 break;
             }
-            if (sa_multi) {
-                if (!vcycle_rest(A, a, a.s, a.Ms, false, 1.0, dummy, dummy2, parity)) return false;
-            } else if (!vcycle(A, a, a.s, a.Ms, false, 1.0, dummy, dummy2, parity)) {
+            if (MX) {
+                if (!vcycle_mixed(*A32, *f, f->bin, a.ym, a.wdef, a.Edef, o2[1], cmx, parity)) return false;
+            } else if (sa_multi) {
+                if (!vcycle_rest(A, a, (const T *)a.s, a.Ms, false, 1.0, dummy, dummy2, parity)) return false;
+            } else if (!vcycle(A, a, (const T *)a.s, a.Ms, false, 1.0, dummy, dummy2, parity)) {
                 return false;
             }
-            double v3[2] = {0, 0}, o4[1];
+            T v3[2] = {0, 0};
+            double v3d[2], o4[1];
             FOR_ROWS(i, a.n)
             {
-                const double ai = A.row(i, LdAcc{a.Ms});
+                T ai;
+                if (MX) {
+                    const double mi = __ldcg(a.ym + i) + cmx;
+                    a.Ms[i] = (T)mi;
+                    ai = A.row_x(i, (T)mi, LdShift{a.ym, cmx});
+                } else {
+                    ai = A.row(i, acc((const T *)a.Ms));
+                }
                 a.AMs[i] = ai;
-                const double si = __ldcg(a.s + i);
+                const T si = __ldcg(a.s + i);
                 v3[0] += ai * si;
                 v3[1] += ai * ai;
             }
-            if (!grid_reduce<2, 1>(v3, a, parity, [&](const double (&t)[2], double (&q)[1]) { q[0] = t[0] / t[1]; },
+            to_double(v3, v3d);
+            if (!grid_reduce<2, 1>(v3d, a, parity, [&](const double (&t)[2], double (&q)[1]) { q[0] = t[0] / t[1]; },
                                    o4))
                 return false;
             o3[2] = o4[0];
         } else {
-            double v3[3] = {0, 0, 0};
+            T v3[3] = {0, 0, 0};
+            double v3d[3];
             FOR_ROWS(i, a.n)
             {
-                const double si = snew(i);
+                const T si = snew(i);
                 a.s[i] = si;
-                const double msi = PC == 1 ? a.dinv[i] * si : si;
+                const T msi = PC == 1 ? a.dinv[i] * si : si;
                 a.Ms[i] = msi;
-                const double ai = PC == 1 ? A.row_x(i, msi, LdScale<LdAxpy>{snew, a.dinv}) : A.row_x(i, msi, snew);
+                const T ai = PC == 1 ? A.row_x(i, msi, scaled(snew, a.dinv)) : A.row_x(i, msi, snew);
                 a.AMs[i] = ai;
                 v3[0] += ai * si;
                 v3[1] += ai * ai;
                 v3[2] += si * si;
             }
-            if (!grid_reduce<3, 3>(v3, a, parity, [&](const double (&t)[3], double (&q)[3]) {
+            to_double(v3, v3d);
+            if (!grid_reduce<3, 3>(v3d, a, parity, [&](const double (&t)[3], double (&q)[3]) {
                     q[0] = sqrt(t[2]);
                     q[1] = q[0] <= tol;
                     q[2] = t[0] / t[1];
                 }, o3))
                 return false;
             if (o3[1] != 0) {
-                FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + alpha * __ldcg(a.Mp + i);
+                FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + at * __ldcg(a.Mp + i);
                 rnorm = o3[0];
                 status = KS_CONVERGED;
                 break;
             }
         }
         omega = o3[2];
+        if (inner_breakdown<T>(omega)) {  // keep the half step
+            FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + at * __ldcg(a.Mp + i);
+            status = KS_STALLED;
+            break;
+        }
+        const T ot = (T)omega;
         // ---- x, r and the dots that give beta
-        double v4[2] = {0, 0}, o5[4];
+        T v4[2] = {0, 0};
+        double v4d[2], o5[4];
         FOR_ROWS(i, a.n)
         {
-            x[i] = __ldcg(x + i) + (alpha * __ldcg(a.Mp + i) + omega * __ldcg(a.Ms + i));
-            const double ri = __ldcg(a.s + i) - omega * __ldcg(a.AMs + i);
+            x[i] = __ldcg(x + i) + (at * __ldcg(a.Mp + i) + ot * __ldcg(a.Ms + i));
+            const T ri = __ldcg(a.s + i) - ot * __ldcg(a.AMs + i);
             a.r[i] = ri;
             v4[0] += __ldcg(a.rs + i) * ri;
             v4[1] += ri * ri;
         }
-        if (!grid_reduce<2, 4>(v4, a, parity, [&](const double (&t)[2], double (&q)[4]) {
+        to_double(v4, v4d);
+        if (!grid_reduce<2, 4>(v4d, a, parity, [&](const double (&t)[2], double (&q)[4]) {
                 q[0] = (t[0] / rho) * (alpha / omega);
                 q[1] = t[0];
                 q[2] = sqrt(t[1]);
@@ -843,6 +1066,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs &a, const do
         ++it;
         rnorm = o5[2];
         status = (int)o5[3];
+        if (status == KS_RUNNING && inner_breakdown<T>(beta)) status = KS_STALLED;
     }
     out[0] = rnorm;
     out[1] = bnorm;
@@ -854,17 +1078,19 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs &a, const do
 }
 
 template <class Op, int PC, int KRY>
-__global__ void __launch_bounds__(kFT, 1) k_fused_solve(Op A, const FArgs *__restrict__ ap, const double *b, double *x)
+__global__ void __launch_bounds__(kFT, 1) k_fused_solve(Op A, const FArgs<double> *__restrict__ ap, const double *b,
+                                                        double *x)
 {
-    const FArgs &a = *ap;
+    const FArgs<double> &a = *ap;
     if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
         a.trace[0] = 1;
         a.trace[1] = global_ns();
     }
     double res[4];
-    int it = 0, status = KS_RUNNING;
-    const bool ok = KRY == KRYLOV_CG ? cg_solve<Op, PC>(A, a, b, x, res, it, status)
-                                     : bicg_solve<Op, PC>(A, a, b, x, res, it, status);
+    int it = 0, status = KS_RUNNING, parity = 0;
+    const bool ok = KRY == KRYLOV_CG
+                        ? cg_solve<Op, PC, double>(A, a, b, x, a.ks->rtol, a.ks->maxit, parity, res, it, status)
+                        : bicg_solve<Op, PC, double>(A, a, b, x, a.ks->rtol, a.ks->maxit, parity, res, it, status);
     trace_stamp(a.trace);
     if (threadIdx.x != 0) return;
     if (!ok) {
@@ -883,6 +1109,122 @@ __global__ void __launch_bounds__(kFT, 1) k_fused_solve(Op A, const FArgs *__res
     if ((status == KS_MAXIT || status == KS_NAN) && a.err) atomicCAS(a.err, 0, a.which * 16 + status);
 }
 
+// Mixed precision with the SA preconditioner: FP64 BiCGSTAB whose two V-cycles per
+// iteration run in FP32 (the constant mode re-solved in FP64).
+template <class Op64, class Op32>
+__global__ void __launch_bounds__(kFT, 1) k_fused_mixed(Op64 A, Op32 A32, const FArgs<double> *__restrict__ ap,
+                                                        const FArgs<float> *__restrict__ fp, const double *b,
+                                                        double *x)
+{
+    const FArgs<double> &a = *ap;
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.trace[0] = 1;
+        a.trace[1] = global_ns();
+    }
+    double res[4];
+    int it = 0, status = KS_RUNNING, parity = 0;
+    const bool ok = bicg_solve<Op64, 2, double, true, Op32>(A, a, b, x, a.ks->rtol, a.ks->maxit, parity, res, it,
+                                                            status, &A32, fp);
+    trace_stamp(a.trace);
+    if (threadIdx.x != 0) return;
+    if (!ok) {
+        atomicCAS(a.err, 0, a.which * 16 + KS_TIMEOUT);
+        return;
+    }
+    if (blockIdx.x != 0) return;
+    KrylovScalars *ks = a.ks;
+    ks->rnorm = res[0];
+    ks->bnorm = res[1];
+    ks->tol = res[2];
+    ks->rho = res[3];
+    ks->it = it;
+    ks->body_runs = it;
+    ks->status = status;
+    if ((status == KS_MAXIT || status == KS_NAN) && a.err) atomicCAS(a.err, 0, a.which * 16 + status);
+}
+
+// Mixed precision without SA: iterative refinement in FP64 around FP32 Krylov solves,
+// in one launch.  A64 is the original (unweighted) operator; A32 the FP32 operator the
+// inner solver iterates on (symmetrised for CG).  The iteration count is the sum of the
+// inner iterations.
+template <class Op64, class Op32, int PC, int KRY>
+__global__ void __launch_bounds__(kFT, 1) k_fused_ir(Op64 A, Op32 A32, const FArgs<double> *__restrict__ ap,
+                                                     const FArgs<float> *__restrict__ fp, const double *b, double *x)
+{
+    const FArgs<double> &a = *ap;
+    const FArgs<float> &f = *fp;
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.trace[0] = 1;
+        a.trace[1] = global_ns();
+    }
+    const double rtol = a.ks->rtol, floor_in = a.ks->inner_rtol;
+    const int maxit = a.ks->maxit, maxit_in = a.ks->inner_maxit;
+    int parity = 0, its = 0, status = KS_RUNNING;
+    double bnorm = 0, tol = 0, rnorm = 0;
+    bool ok = true, first = true;
+    while (ok) {
+        // outer residual of the original system in FP64; the inner right-hand side and
+        // a zero inner start
+        double v[2] = {0, 0}, o[5];
+        FOR_ROWS(i, a.n)
+        {
+            const double bi = b[i];
+            const double ri = bi - A.row(i, acc((const double *)x));
+            f.bin[i] = (float)ri;
+            f.xin[i] = 0.f;
+            v[0] += ri * ri;
+            v[1] += bi * bi;
+        }
+        const double bn0 = bnorm, tl0 = tol;
+        ok = grid_reduce<2, 5>(v, a, parity, [&](const double (&t)[2], double (&q)[5]) {
+            q[0] = sqrt(t[0]);
+            q[1] = first ? sqrt(t[1]) : bn0;
+            q[2] = first ? rtol * q[1] : tl0;
+            q[3] = solve_state(q[0], q[2], its, maxit);
+            q[4] = fmax(0.5 * q[2] / q[0], floor_in);  // the inner solve's relative tolerance
+        }, o);
+        if (!ok) break;
+        rnorm = o[0];
+        bnorm = o[1];
+        tol = o[2];
+        status = (int)o[3];
+        first = false;
+        if (status != KS_RUNNING) break;
+        double res[4];
+        int it_in = 0, st_in = KS_RUNNING;
+        const int cap = min(maxit - its, maxit_in);
+        ok = KRY == KRYLOV_CG ? cg_solve<Op32, PC, float>(A32, f, f.bin, f.xin, o[4], cap, parity, res, it_in, st_in)
+                              : bicg_solve<Op32, PC, float>(A32, f, f.bin, f.xin, o[4], cap, parity, res, it_in, st_in);
+        if (!ok) break;
+        its += it_in > 0 ? it_in : 1;
+        if (st_in == KS_NAN) {
+            status = KS_NAN;
+            break;
+        }
+        if (st_in == KS_STALLED && it_in == 0) {  // a breakdown before any progress: give up
+            status = KS_MAXIT;
+            break;
+        }
+        FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + (double)__ldcg(f.xin + i);
+        ok = grid_sync(a.sync, a.trace);
+    }
+    trace_stamp(a.trace);
+    if (threadIdx.x != 0) return;
+    if (!ok) {
+        atomicCAS(a.err, 0, a.which * 16 + KS_TIMEOUT);
+        return;
+    }
+    if (blockIdx.x != 0) return;
+    KrylovScalars *ks = a.ks;
+    ks->rnorm = rnorm;
+    ks->bnorm = bnorm;
+    ks->tol = tol;
+    ks->it = its;
+    ks->body_runs = its;
+    ks->status = status;
+    if ((status == KS_MAXIT || status == KS_NAN) && a.err) atomicCAS(a.err, 0, a.which * 16 + status);
+}
+
 // unscaled operator diagonal, summed as the stepwise row functions sum it
 template <class Op>
 __global__ void k_fused_diag(Op A, int n, double *diag)
@@ -890,6 +1232,12 @@ __global__ void k_fused_diag(Op A, int n, double *diag)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     diag[i] = A.row(i, [&](int j) { return j == i ? 1.0 : 0.0; });
+}
+
+__global__ void k_to_float(const double *__restrict__ src, float *__restrict__ dst, long n)
+{
+    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -914,7 +1262,38 @@ struct Op2Plain {
     }
 };
 
-// the operator diagonal the persistent solver's rows use (rows may change when a body moves)
+// Float copies of a system's tables for the mixed-precision solve (device memory in
+// the context arena; this host record points at them).
+struct MixedState {
+    Lhs1T<float> l1{};
+    Lhs2T<float> l2{};
+    float *diag = nullptr, *dinv = nullptr, *w = nullptr, *winv = nullptr;
+    float *wd0 = nullptr;        // level 0's omega D^-1 (refreshed with the diagonal)
+    double *ym = nullptr;        // the FP32 cycle's output (SA)
+    double *wdef = nullptr;      // A^T e (SA, Poisson): the constant-mode correction
+    double Edef = 0;             // e^T A e
+    FArgs<float> *dev = nullptr;
+};
+
+static float *to_float(Context &c, const double *src, size_t n)
+{
+    float *dst = c.carve<float>(std::max<size_t>(n, 1));
+    if (n) {
+        k_to_float<<<blocks_for((long)n), kBlock, 0, c.stream>>>(src, dst, (long)n);
+        CUIBM_TRY(cudaGetLastError());
+    }
+    return dst;
+}
+
+static void convert_into(Context &c, const double *src, float *dst, size_t n)
+{
+    if (!src || !dst || !n) return;
+    k_to_float<<<blocks_for((long)n), kBlock, 0, c.stream>>>(src, dst, (long)n);
+    CUIBM_TRY(cudaGetLastError());
+}
+
+// the operator diagonal the persistent solver's rows use (rows may change when a body
+// moves), and its float copies
 void refresh_fused_diag(Context &c, LinearSystem &S)
 {
     if (!S.diag) return;
@@ -923,6 +1302,16 @@ void refresh_fused_diag(Context &c, LinearSystem &S)
     else
         k_fused_diag<<<blocks_for(S.n), kBlock, 0, c.stream>>>(Op2Plain{c.l2, c.g}, S.n, S.diag);
     CUIBM_TRY(cudaGetLastError());
+    if (MixedState *m = static_cast<MixedState *>(S.mixed)) {
+        convert_into(c, S.diag, m->diag, S.n);
+        convert_into(c, S.dinv, m->dinv, S.n);
+    }
+}
+
+void refresh_fused_level0(Context &c, LinearSystem &S)
+{
+    MixedState *m = static_cast<MixedState *>(S.mixed);
+    if (m && m->wd0 && !S.amg.empty()) convert_into(c, S.amg[0]->wd, m->wd0, S.n);
 }
 
 template <class Op>
@@ -938,28 +1327,66 @@ static void *pick_kernel(int precond, int krylov)
     return (void *)k_fused_solve<Op, 0, KRYLOV_BICGSTAB>;
 }
 
-template <class Op>
-static void launch_fused_op(Context &c, LinearSystem &S, Op A, const double *b, double *x)
+// mixed precision: BiCGSTAB with a multilevel SA hierarchy keeps the FP64 Krylov
+// around FP32 V-cycles; everything else is refined around FP32 solves
+static bool mixed_vcycle(const LinearSystem &S)
+{
+    return S.precond == PC_SMOOTHED_AGGREGATION && S.krylov == KRYLOV_BICGSTAB && S.amg.size() >= 2;
+}
+
+template <class Op64, class Op32>
+static void *pick_mixed_kernel(const LinearSystem &S)
+{
+    if (mixed_vcycle(S)) return (void *)k_fused_mixed<Op64, Op32>;
+    if (S.krylov == KRYLOV_CG) {
+        if (S.precond == PC_SMOOTHED_AGGREGATION) return (void *)k_fused_ir<Op64, Op32, 2, KRYLOV_CG>;
+        if (S.precond == PC_DIAGONAL) return (void *)k_fused_ir<Op64, Op32, 1, KRYLOV_CG>;
+        return (void *)k_fused_ir<Op64, Op32, 0, KRYLOV_CG>;
+    }
+    if (S.precond == PC_SMOOTHED_AGGREGATION) return (void *)k_fused_ir<Op64, Op32, 2, KRYLOV_BICGSTAB>;
+    if (S.precond == PC_DIAGONAL) return (void *)k_fused_ir<Op64, Op32, 1, KRYLOV_BICGSTAB>;
+    return (void *)k_fused_ir<Op64, Op32, 0, KRYLOV_BICGSTAB>;
+}
+
+static cudaLaunchConfig_t coop_config(Context &c, LinearSystem &S, cudaLaunchAttribute *attr)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(S.fused_grid);
     cfg.blockDim = dim3(kFT);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = c.stream;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    using Fn = void (*)(Op, const FArgs *, const double *, double *);
-    const FArgs *args = static_cast<const FArgs *>(S.fargs);
+    return cfg;
+}
+
+template <class Op>
+static void launch_fused_op(Context &c, LinearSystem &S, Op A, const double *b, double *x)
+{
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = coop_config(c, S, attr);
+    using Fn = void (*)(Op, const FArgs<double> *, const double *, double *);
+    const FArgs<double> *args = static_cast<const FArgs<double> *>(S.fargs);
     CUIBM_TRY(cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(S.fused_fn), A, args, b, x));
+}
+
+template <class Op64, class Op32>
+static void launch_fused_mixed(Context &c, LinearSystem &S, Op64 A, Op32 A32, const double *b, double *x)
+{
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = coop_config(c, S, attr);
+    using Fn = void (*)(Op64, Op32, const FArgs<double> *, const FArgs<float> *, const double *, double *);
+    const FArgs<double> *args = static_cast<const FArgs<double> *>(S.fargs);
+    const FArgs<float> *fargs = static_cast<MixedState *>(S.mixed)->dev;
+    CUIBM_TRY(cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(S.fused_fn), A, A32, args, fargs, b, x));
 }
 
 // Upload the solver's arguments (after the SA hierarchy exists).
 static void upload_fargs(Context &c, LinearSystem &S)
 {
-    FArgs a = {};
+    FArgs<double> a = {};
     a.n = S.n;
     a.r = S.r;
     a.rs = S.rs;
@@ -986,12 +1413,13 @@ static void upload_fargs(Context &c, LinearSystem &S)
     a.nlev = (int)S.amg.size();
     for (int l = 0; l < a.nlev; ++l) {
         const SaLevel *L = S.amg[l];
-        FLevel &F = a.lev[l];
+        FLevel<double> &F = a.lev[l];
+        auto view = [](const DevCsr &M) { return CsrV<double>{M.n, M.nnz, M.ptr, M.col, M.val}; };
         F.n = L->n;
-        F.A = L->A;
-        F.P = L->P;
-        F.R = L->R;
-        F.AP = L->AP;
+        F.A = view(L->A);
+        F.P = view(L->P);
+        F.R = view(L->R);
+        F.AP = view(L->AP);
         F.wd = L->wd;
         F.x = L->x;
         F.b = L->b;
@@ -999,19 +1427,133 @@ static void upload_fargs(Context &c, LinearSystem &S)
         F.t = L->t;
         F.inv = L->coarse_inv;
     }
-    FArgs *d = S.fargs ? static_cast<FArgs *>(S.fargs) : c.carve<FArgs>(1);
-    CUIBM_TRY(cudaMemcpyAsync(d, &a, sizeof(FArgs), cudaMemcpyHostToDevice, c.stream));
+    MixedState *m = static_cast<MixedState *>(S.mixed);
+    if (m) {
+        a.ym = m->ym;
+        a.wdef = m->wdef;
+        a.Edef = m->Edef;
+    }
+    FArgs<double> *d = S.fargs ? static_cast<FArgs<double> *>(S.fargs) : c.carve<FArgs<double>>(1);
+    CUIBM_TRY(cudaMemcpyAsync(d, &a, sizeof(a), cudaMemcpyHostToDevice, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
     S.fargs = d;
+    if (m) {
+        // the float solver shares the reduction buffers, the barrier and the trace
+        FArgs<float> fa = {};
+        CUIBM_TRY(cudaMemcpy(&fa, m->dev, sizeof(fa), cudaMemcpyDeviceToHost));
+        fa.partials = S.fpartials;
+        fa.sync = S.fsync;
+        fa.trace = a.trace;
+        fa.ks = S.ks;
+        fa.err = c.err_word;
+        CUIBM_TRY(cudaMemcpy(m->dev, &fa, sizeof(fa), cudaMemcpyHostToDevice));
+    }
+}
+
+// The float side of a mixed-precision system: vectors, operator tables, Jacobi and
+// symmetrisation tables and the SA hierarchy's matrices and smoother weights (index
+// arrays and the coarsest dense inverse are shared with the FP64 copies); for the
+// Poisson system with SA also A^T e and e^T A e for the constant-mode correction.
+static void setup_mixed(Context &c, LinearSystem &S)
+{
+    MixedState *m = new MixedState();
+    S.mixed = m;
+    const int n = S.n, nx = c.g.nx, ny = c.g.ny;
+    if (S.which == 1) {
+        const Lhs1Coef &t = c.l1;
+        m->l1 = Lhs1T<float>{to_float(c, t.uE, nx - 1), to_float(c, t.uW, nx - 1), to_float(c, t.uN, ny),
+                             to_float(c, t.uS, ny),     to_float(c, t.vE, nx),     to_float(c, t.vW, nx),
+                             to_float(c, t.vN, ny - 1), to_float(c, t.vS, ny - 1), t.patch,
+                             t.rscale ? to_float(c, t.rscale, c.g.nUV) : nullptr};
+    } else {
+        const Lhs2Coef &t = c.l2;
+        m->l2 = Lhs2T<float>{to_float(c, t.E, nx), to_float(c, t.W, nx), to_float(c, t.N, ny), to_float(c, t.S, ny),
+                             t.pin0, t.pinc, t.patch};
+    }
+    m->diag = to_float(c, S.diag, n);
+    m->dinv = to_float(c, S.dinv, n);
+    if (S.w) {
+        m->w = to_float(c, S.w, n);
+        m->winv = to_float(c, S.winv, n);
+    }
+    if (mixed_vcycle(S)) {
+        m->ym = c.carve<double>(n);
+        if (S.which == 2) {
+            // w = A^T e (column sums) and E = e^T A e of the operator the solver iterates on
+            std::vector<int> ptr, col;
+            std::vector<double> val, w(n, 0.0);
+            host_operator_csr(c, 2, nullptr, ptr, col, val);
+            for (size_t k = 0; k < col.size(); ++k) w[col[k]] += val[k];
+            double E = 0;
+            for (double v : w) E += v;
+            if (E != 0) {
+                m->wdef = c.carve<double>(n);
+                m->Edef = E;
+                CUIBM_TRY(cudaMemcpyAsync(m->wdef, w.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+                CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            }
+        }
+    }
+    FArgs<float> f = {};
+    f.n = n;
+    float **vecs[] = {&f.r, &f.rs, &f.p, &f.p2, &f.Mp, &f.AMp, &f.AMp2, &f.s, &f.Ms, &f.AMs, &f.bin, &f.xin};
+    for (float **v : vecs) *v = c.carve<float>(n);
+    f.z = f.Ms;  // as in the FP64 layout: CG's z and q reuse BiCGSTAB's Ms and AMs
+    f.q = f.AMs;
+    f.dinv = m->dinv;
+    f.w = m->w;
+    f.winv = m->winv;
+    f.diag = m->diag;
+    f.which = S.which;
+    f.nlev = (int)S.amg.size();
+    for (int l = 0; l < f.nlev; ++l) {
+        const SaLevel *L = S.amg[l];
+        FLevel<float> &F = f.lev[l];
+        auto view = [&](const DevCsr &M) {
+            return CsrV<float>{M.n, M.nnz, M.ptr, M.col, M.val ? to_float(c, M.val, M.nnz) : nullptr};
+        };
+        F.n = L->n;
+        F.A = view(L->A);
+        F.P = view(L->P);
+        F.R = view(L->R);
+        F.AP = view(L->AP);
+        F.wd = L->wd ? to_float(c, L->wd, L->n) : nullptr;
+        if (l == 0) m->wd0 = const_cast<float *>(F.wd);
+        F.x = c.carve<float>(L->n);
+        F.b = c.carve<float>(L->n);
+        F.r = c.carve<float>(L->n);
+        F.t = c.carve<float>(L->n);
+        F.inv = L->coarse_inv;  // shared: the coarse solve runs in FP64
+    }
+    m->dev = c.carve<FArgs<float>>(1);
+    CUIBM_TRY(cudaMemcpyAsync(m->dev, &f, sizeof(f), cudaMemcpyHostToDevice, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+}
+
+void free_fused(LinearSystem &S)
+{
+    delete static_cast<MixedState *>(S.mixed);
+    S.mixed = nullptr;
 }
 
 void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x)
 {
     CUIBM_TRY(cudaMemsetAsync(S.fsync, 0, sizeof(FusedSyncState), c.stream));
+    if (MixedState *m = static_cast<MixedState *>(S.mixed)) {
+        // the refinement's outer residual is that of the original system (no
+        // symmetrisation weights); the FP32 operator carries them for CG
+        if (S.which == 1)
+            launch_fused_mixed(c, S, Op1D<double>{tab64(c.l1), c.g, S.diag, mixed_vcycle(S) ? S.w : nullptr},
+                               Op1D<float>{m->l1, c.g, m->diag, m->w}, b, x);
+        else
+            launch_fused_mixed(c, S, Op2D<double>{tab64(c.l2), c.g, S.diag, mixed_vcycle(S) ? S.w : nullptr},
+                               Op2D<float>{m->l2, c.g, m->diag, m->w}, b, x);
+        return;
+    }
     if (S.which == 1)
-        launch_fused_op(c, S, Op1D{c.l1, c.g, S.diag, S.w}, b, x);
+        launch_fused_op(c, S, Op1D<double>{tab64(c.l1), c.g, S.diag, S.w}, b, x);
     else
-        launch_fused_op(c, S, Op2D{c.l2, c.g, S.diag, S.w}, b, x);
+        launch_fused_op(c, S, Op2D<double>{tab64(c.l2), c.g, S.diag, S.w}, b, x);
 }
 
 void set_fused_trace(Context &c, LinearSystem &S, bool on)
@@ -1027,22 +1569,26 @@ void set_fused_trace(Context &c, LinearSystem &S, bool on)
 // bound, so this is a floor on traffic, not the bound.
 double solve_bytes(const LinearSystem &S, int it)
 {
-    const double n = S.n, D = 8;
-    auto csr = [](const DevCsr &M) { return 12.0 * M.nnz + 4.0 * (M.n + 1); };
+    // mixed precision: the multigrid levels' vectors and matrix values are float (and,
+    // for refinement, the Krylov vectors too; its FP64 residual phases are left out)
+    const bool mixed = S.precision == PRECISION_MIXED && S.mixed;
+    const bool ir = mixed && !mixed_vcycle(S);
+    const double n = S.n, D = ir ? 4 : 8, DL = mixed ? 4 : 8, E = mixed ? 8 : 12;
+    auto csr = [E](const DevCsr &M) { return E * M.nnz + 4.0 * (M.n + 1); };
     double vc = 0;  // one V-cycle without its first sweep's vector reads
     const int L = (int)S.amg.size();
     if (L == 1) {
-        vc = D * (double)S.amg[0]->n * S.amg[0]->n + 2 * D * S.amg[0]->n;
+        vc = 8.0 * (double)S.amg[0]->n * S.amg[0]->n + 2 * DL * S.amg[0]->n;
     } else if (L > 1) {
-        vc += 2 * D * n;  // first sweep: omega D^-1 and r_0 (its input is counted by the caller)
+        vc += 2 * DL * n;  // first sweep: omega D^-1 and r_0 (its input is counted by the caller)
         for (int l = 0; l < L - 1; ++l) {
             const SaLevel *V = S.amg[l], *C = S.amg[l + 1];
-            if (l > 0) vc += 3 * D * V->n + csr(V->A);
-            vc += D * V->n + csr(V->R) + D * C->n;                           // restriction
-            vc += 4 * D * V->n + csr(V->P) + csr(V->AP) + D * C->n;          // prolongation and sweep
+            if (l > 0) vc += 3 * DL * V->n + csr(V->A);
+            vc += DL * V->n + csr(V->R) + DL * C->n;                           // restriction
+            vc += 4 * DL * V->n + csr(V->P) + csr(V->AP) + DL * C->n;          // prolongation and sweep
         }
         const double nc = S.amg[L - 1]->n;
-        vc += D * nc * nc + 2 * D * nc;
+        vc += 8.0 * nc * nc + 2 * DL * nc;
     }
     double per_it, init;
     if (S.krylov == KRYLOV_CG) {
@@ -1060,7 +1606,8 @@ double solve_bytes(const LinearSystem &S, int it)
 
 // Decide whether the system can use the persistent solver, size its grid (one
 // block per SM unless CUIBM_FUSED_BLOCKS_PER_SM asks for more and the kernel's
-// registers allow it) and build its tables.
+// registers allow it) and build its tables.  A mixed-precision system gets its
+// mixed kernel and the float tables.
 void setup_fused(Context &c, LinearSystem &S)
 {
     S.fused_fn = nullptr;
@@ -1068,7 +1615,12 @@ void setup_fused(Context &c, LinearSystem &S)
     if (S.precond == PC_SMOOTHED_AGGREGATION &&
         (S.amg.empty() || (int)S.amg.size() > kMaxLevels || sa_coarsest_size(S) > kDenseMax))
         return;
-    void *fn = S.which == 1 ? pick_kernel<Op1D>(S.precond, S.krylov) : pick_kernel<Op2D>(S.precond, S.krylov);
+    const bool mixed = S.precision == PRECISION_MIXED;
+    void *fn;
+    if (S.which == 1)
+        fn = mixed ? pick_mixed_kernel<Op1D<double>, Op1D<float>>(S) : pick_kernel<Op1D<double>>(S.precond, S.krylov);
+    else
+        fn = mixed ? pick_mixed_kernel<Op2D<double>, Op2D<float>>(S) : pick_kernel<Op2D<double>>(S.precond, S.krylov);
     int dev = 0, sms = 0, coop = 0, per_sm = 0;
     CUIBM_TRY(cudaGetDevice(&dev));
     CUIBM_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1097,6 +1649,7 @@ void setup_fused(Context &c, LinearSystem &S)
         CUIBM_TRY(cudaMemcpyAsync(S.winv, wi.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
     }
+    if (mixed) setup_mixed(c, S);
     upload_fargs(c, S);
 }
 

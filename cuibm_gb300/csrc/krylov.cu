@@ -438,6 +438,7 @@ void setup_system(Context &c, LinearSystem &S)
     S.precond = L.precond;
     S.rtol = L.tolerance;
     S.maxit = L.maxIterations;
+    S.precision = L.precision;
     if (S.precond == PC_AINV)
         throw InputError("preconditioner AINV is not implemented by this build; use DIAGONAL or SMOOTHED_AGGREGATION");
     const int n = S.n;
@@ -458,6 +459,11 @@ void setup_system(Context &c, LinearSystem &S)
         KrylovScalars hk{};
         hk.rtol = S.rtol;
         hk.maxit = S.maxit;
+        // mixed precision by refinement: each FP32 solve is asked for a 1e-3 reduction at
+        // least and stops after 100 iterations (FP32 recurrences stall near their
+        // attainable accuracy; the FP64 refinement then goes on from a fresh residual)
+        hk.inner_rtol = 1e-3;
+        hk.inner_maxit = 100;
         hk.status = KS_CONVERGED;
         CUIBM_TRY(cudaMemcpy(S.ks, &hk, sizeof(hk), cudaMemcpyHostToDevice));
     }
@@ -504,6 +510,7 @@ void refresh_system_diagonals(Context &c, LinearSystem &S)
         SaLevel *L = S.amg[0];
         k_sa_level0_tables<<<blocks_for(n), kBlock, 0, c.stream>>>(n, S.dinv, L->omega, L->dinv, L->wd);
         CUIBM_TRY(cudaGetLastError());
+        refresh_fused_level0(c, S);
     }
 }
 

@@ -80,13 +80,15 @@ struct RhsCoef {
 };
 
 // ---- Krylov state living in device memory -------------------------------------
-enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3, KS_TIMEOUT = 4 };
+enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3, KS_TIMEOUT = 4,
+               KS_STALLED = 5 };  // KS_STALLED: an FP32 inner solve stopped at a breakdown (refinement goes on)
 struct KrylovScalars {
     double rho, alpha, omega, beta;
     double bnorm, tol, rnorm, snorm;
-    double rtol, pad0;
+    double rtol, inner_rtol;  // inner_rtol: mixed precision, the FP32 solves' relative tolerance floor
     int it, maxit, status, s_done;
-    int body_runs, pad1;  // executions of the iteration body in the last solve
+    int body_runs, inner_maxit;  // executions of the iteration body in the last solve; mixed
+                                 // precision: iterations of one FP32 solve at most
     unsigned int arrive;  // last-block-done counter of the fused reductions
     int pad;
 };
@@ -121,6 +123,8 @@ struct LinearSystem {
     int fused_grid = 0;
     double *p2 = nullptr, *AMp2 = nullptr, *fpartials = nullptr;
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
+    int precision = PRECISION_FP64;
+    void *mixed = nullptr;  // mixed precision: the float tables (fused_solve.cu)
     FusedSyncState *fsync = nullptr;
     void *fargs = nullptr;  // device copy of the solver arguments
 };
@@ -267,6 +271,8 @@ void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x)
 void set_fused_trace(Context &c, LinearSystem &S, bool on);
 double solve_bytes(const LinearSystem &S, int iterations);
 void refresh_fused_diag(Context &c, LinearSystem &S);
+void refresh_fused_level0(Context &c, LinearSystem &S);
+void free_fused(LinearSystem &S);
 
 // fadlun.cu
 void setup_fadlun(Context &c);

@@ -80,6 +80,17 @@ def test_bad_inputs_report_errors(tmp_path):
         cb.case_info(f, ["-nt", "notanumber"])
 
 
+def test_precision_option(tmp_path):
+    f = cases.cavity(str(tmp_path / "m"), n=16, nt=1, precision="MIXED")
+    info = cb.case_info(f)
+    assert info.velocity_precision == 1 and info.poisson_precision == 1
+    info = cb.case_info(cases.cavity(str(tmp_path / "d"), n=16, nt=1))
+    assert info.velocity_precision == 0 and info.poisson_precision == 0
+    with pytest.raises(cb.CuibmError) as e:
+        cb.case_info(cases.cavity(str(tmp_path / "h"), n=16, nt=1, precision="HALF"))
+    assert e.value.status == cb.ERR_BAD_INPUT and "precision" in str(e.value)
+
+
 def test_unknown_solver_type_falls_back_to_navier_stokes(tmp_path):
     f = cases.cavity(str(tmp_path / "c"), n=16, nt=1)
     p = os.path.join(f, "simParams.yaml")
