@@ -17,6 +17,11 @@ stream (outside the events) to flush the 129 MB L2, because the whole working
 set of these grids fits in L2.  --gpus N runs N independent replicas (one per
 GPU, one process each under torchrun); value = total cell-steps / max time.
 
+The line also carries "mixed_precision": the Re 550 cylinder (922 x 922) timed over
+the same steps in plain FP64 and with precision MIXED (FP32 multigrid cycles inside
+FP64 BiCGSTAB, FP32 inner solves under FP64 refinement), with both runs' C_D
+(--no-mixed skips it; single-GPU runs only).
+
 --impl reference times the reference's algorithm on the host CPU cores: the
 oracle port (oracle/, a C restatement of the reference's kernels and of its
 BiCGSTAB / smoothed-aggregation solvers - the reference itself needs CUSP,
@@ -60,8 +65,10 @@ def make_case(workload, folder, tight=False, precision=None):
         return f, 270 * 270
     if workload == "cylinder_re550":
         k = KRYLOV
+        # both solves to 1e-8: C_D then stays within 1e-6 of a tightly solved run (at 1e-5 the
+        # velocity solve stops after one iteration and C_D is off by about 2e-3 at step 40)
         f = cases.cylinder(folder, h=0.005, ratio=1.01, points=629, nu=1.0 / 550, dt=0.002, nt=1000000,
-                           vel_tol=1e-5, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k,
+                           vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k,
                            precision=prec)
         return f, 922 * 922
     raise SystemExit("unknown workload " + workload)
@@ -268,6 +275,46 @@ def run_ours(a, rank, world, local, pg):
             "gpu_launches": launches * a.steps if launches is not None else None}
 
 
+def precision_comparison(local, warm=20, steps=20):
+    """The Re 550 cylinder (922 x 922, 629 body points, dt 0.002, both solves to 1e-8),
+    plain FP64 against precision MIXED on the same steps: steps warm+1 .. warm+steps of
+    the impulsive start, timed with CUDA events on the solver's stream (the working set,
+    several hundred MB, is larger than L2).  C_D of both runs at the last step is
+    reported beside the times; at these tolerances both are within 1e-6 of a tightly
+    solved FP64 run."""
+    import torch
+
+    import cuibm_gb300 as cb
+    out = {"workload": "impulsively started cylinder Re 550, external (Luo) method, 922x922, 629 points, "
+                       "dt 0.002, BiCGSTAB + diagonal / smoothed aggregation, rtol 1e-8 both",
+           "steps_timed": "%d-%d" % (warm + 1, warm + steps)}
+    for prec in ("FP64", "MIXED"):
+        with tempfile.TemporaryDirectory() as tmp:
+            folder, cells = make_case("cylinder_re550", os.path.join(tmp, "case"), precision=prec)
+            s = cb.NavierStokesSolver(folder, ["-deviceNumber", str(local)])
+            s.set_option("write_output", 0)
+            s.initialise()
+            s.stepTime(warm)
+            stream = torch.cuda.ExternalStream(s.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            s.set_option("step_sync", 0)
+            e0.record(stream)
+            s.stepTime(steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            s.set_option("step_sync", 1)
+            s.stepTime(0)  # raises if a solve failed
+            ms = e0.elapsed_time(e1) / steps
+            fx, _ = s.forces()
+            out[prec.lower()] = {"ms_per_step": round(ms, 4), "value": round(cells / ms / 1e3, 3), "unit": METRIC,
+                                 "iterations_last_step": list(s.iterations()), "cd_last_step": 2 * fx}
+            s.close()
+    out["speedup_mixed_over_fp64"] = round(out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"], 3)
+    out["cd_difference"] = abs(out["fp64"]["cd_last_step"] - out["mixed"]["cd_last_step"])
+    return out
+
+
 def profiled_traffic(kernel):
     """DRAM bytes per launch of the kernel from the committed ncu summary
     (profiles/*.md, a line 'dram_bytes_per_launch <kernel> <bytes>'); None where
@@ -325,6 +372,7 @@ def main():
     ap.add_argument("--workload", default=os.environ.get("CUIBM_BENCH_WORKLOAD", "cylinder_re40"))
     ap.add_argument("--roofline-kernel", default="poisson_solve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the Re 550 FP64 / mixed-precision comparison")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
@@ -353,6 +401,8 @@ def main():
             "drag_lift_last_step": r["drag_lift_last_step"]}
     if not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(a.workload)
+    if not a.no_mixed and world == 1:
+        line["mixed_precision"] = precision_comparison(local)
     print(json.dumps(line))
 
 

@@ -797,6 +797,9 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                                            const Op32 *A32 = nullptr, const FArgs<float> *f = nullptr)
 {
     const bool sa_multi = PC == 2 && a.nlev >= 2;
+    // FP64 cycle with the constant-mode correction (the Poisson system): its output goes
+    // to ym, the corrected vector is written where A is applied to it
+    const bool defl = !MX && sa_multi && a.wdef != nullptr;
     T v[2] = {0, 0};
     double vd[2], o[5];
     FOR_ROWS(i, a.n)
@@ -858,23 +861,43 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                 }
                 if (!vcycle_mixed(*A32, *f, f->bin, a.ym, a.wdef, a.Edef, eb[0], cmx, parity)) return false;
             } else if (sa_multi) {
+                T ve[1] = {0};
                 FOR_ROWS(i, a.n)
                 {
+                    T pi;
                     if (first) {
-                        vcycle_residual0_row(A, a.lev[0], i, acc((const T *)p), __ldcg(p + i));
+                        pi = __ldcg(p + i);
+                        vcycle_residual0_row(A, a.lev[0], i, acc((const T *)p), pi);
                     } else {
-                        const T pi = dir(i);
+                        pi = dir(i);
                         pn[i] = pi;
                         vcycle_residual0_row(A, a.lev[0], i, dir, pi);
                     }
+                    ve[0] += pi;
                 }
-                if (!grid_sync(a.sync, a.trace)) return false;
+                double eb[1] = {0};
+                if (defl) {
+                    double ved[1];
+                    to_double(ve, ved);
+                    if (!grid_reduce<1, 1>(ved, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = t[0]; },
+                                           eb))
+                        return false;
+                } else if (!grid_sync(a.sync, a.trace)) {
+                    return false;
+                }
                 if (!first) {
                     T *tmp = p;
                     p = pn;
                     pn = tmp;
                 }
-                if (!vcycle_rest(A, a, (const T *)p, a.Mp, false, 1.0, dummy, dummy2, parity)) return false;
+                if (defl) {
+                    double wy = 0;
+                    if (!vcycle_rest(A, a, (const T *)p, a.ym, false, 1.0, dummy, dummy2, parity, a.wdef, &wy))
+                        return false;
+                    cmx = (eb[0] - wy) / a.Edef;
+                } else if (!vcycle_rest(A, a, (const T *)p, a.Mp, false, 1.0, dummy, dummy2, parity)) {
+                    return false;
+                }
             } else {
                 if (!first) {
                     FOR_ROWS(i, a.n) pn[i] = dir(i);
@@ -891,7 +914,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
         FOR_ROWS(i, a.n)
         {
             T ai;
-            if (PC == 2 && MX) {
+            if (PC == 2 && (MX || defl)) {
                 const double mi = __ldcg(a.ym + i) + cmx;
                 a.Mp[i] = (T)mi;
                 ai = A.row_x(i, (T)mi, LdShift{a.ym, cmx});
@@ -953,6 +976,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                     const T si = snew(i);
                     a.s[i] = si;
                     v2[0] += si * si;
+                    v2[1] += si;
                     vcycle_residual0_row(A, a.lev[0], i, snew, si);
                 }
             } else {
@@ -979,6 +1003,11 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
             }
             if (MX) {
                 if (!vcycle_mixed(*A32, *f, f->bin, a.ym, a.wdef, a.Edef, o2[1], cmx, parity)) return false;
+            } else if (defl) {
+                double wy = 0;
+                if (!vcycle_rest(A, a, (const T *)a.s, a.ym, false, 1.0, dummy, dummy2, parity, a.wdef, &wy))
+                    return false;
+                cmx = (o2[1] - wy) / a.Edef;
             } else if (sa_multi) {
                 if (!vcycle_rest(A, a, (const T *)a.s, a.Ms, false, 1.0, dummy, dummy2, parity)) return false;
             } else if (!vcycle(A, a, (const T *)a.s, a.Ms, false, 1.0, dummy, dummy2, parity)) {
@@ -989,7 +1018,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
             FOR_ROWS(i, a.n)
             {
                 T ai;
-                if (MX) {
+                if (MX || defl) {
                     const double mi = __ldcg(a.ym + i) + cmx;
                     a.Ms[i] = (T)mi;
                     ai = A.row_x(i, (T)mi, LdShift{a.ym, cmx});
@@ -1268,10 +1297,7 @@ struct MixedState {
     Lhs1T<float> l1{};
     Lhs2T<float> l2{};
     float *diag = nullptr, *dinv = nullptr, *w = nullptr, *winv = nullptr;
-    float *wd0 = nullptr;        // level 0's omega D^-1 (refreshed with the diagonal)
-    double *ym = nullptr;        // the FP32 cycle's output (SA)
-    double *wdef = nullptr;      // A^T e (SA, Poisson): the constant-mode correction
-    double Edef = 0;             // e^T A e
+    float *wd0 = nullptr;  // level 0's omega D^-1 (refreshed with the diagonal)
     FArgs<float> *dev = nullptr;
 };
 
@@ -1427,12 +1453,10 @@ static void upload_fargs(Context &c, LinearSystem &S)
         F.t = L->t;
         F.inv = L->coarse_inv;
     }
+    a.ym = S.ym;
+    a.wdef = S.wdef;
+    a.Edef = S.Edef;
     MixedState *m = static_cast<MixedState *>(S.mixed);
-    if (m) {
-        a.ym = m->ym;
-        a.wdef = m->wdef;
-        a.Edef = m->Edef;
-    }
     FArgs<double> *d = S.fargs ? static_cast<FArgs<double> *>(S.fargs) : c.carve<FArgs<double>>(1);
     CUIBM_TRY(cudaMemcpyAsync(d, &a, sizeof(a), cudaMemcpyHostToDevice, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
@@ -1476,24 +1500,6 @@ static void setup_mixed(Context &c, LinearSystem &S)
         m->w = to_float(c, S.w, n);
         m->winv = to_float(c, S.winv, n);
     }
-    if (mixed_vcycle(S)) {
-        m->ym = c.carve<double>(n);
-        if (S.which == 2) {
-            // w = A^T e (column sums) and E = e^T A e of the operator the solver iterates on
-            std::vector<int> ptr, col;
-            std::vector<double> val, w(n, 0.0);
-            host_operator_csr(c, 2, nullptr, ptr, col, val);
-            for (size_t k = 0; k < col.size(); ++k) w[col[k]] += val[k];
-            double E = 0;
-            for (double v : w) E += v;
-            if (E != 0) {
-                m->wdef = c.carve<double>(n);
-                m->Edef = E;
-                CUIBM_TRY(cudaMemcpyAsync(m->wdef, w.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-                CUIBM_TRY(cudaStreamSynchronize(c.stream));
-            }
-        }
-    }
     FArgs<float> f = {};
     f.n = n;
     float **vecs[] = {&f.r, &f.rs, &f.p, &f.p2, &f.Mp, &f.AMp, &f.AMp2, &f.s, &f.Ms, &f.AMs, &f.bin, &f.xin};
@@ -1527,6 +1533,43 @@ static void setup_mixed(Context &c, LinearSystem &S)
     }
     m->dev = c.carve<FArgs<float>>(1);
     CUIBM_TRY(cudaMemcpyAsync(m->dev, &f, sizeof(f), cudaMemcpyHostToDevice, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+}
+
+// The constant-mode correction of the SA-preconditioned BiCGSTAB on the Poisson system
+// (both precisions): w = A^T e (column sums) and E = e^T A e of the operator the solver
+// iterates on, and the buffer for the cycle's output.  The pressure operator's
+// near-null space is the constant (pinned at one cell); the cycle resolves it poorly,
+// and re-solving it exactly - z = y + e (e.r - w.y) / E, so that e^T (A z - r) = 0 - is
+// a one-vector coarse correction.  The FP32 cycle always gets it.  In FP64 the
+// constant mode's eigenvalue shrinks like 1/n, and the correction pays from about
+// 2e5 unknowns on (the Re 550 cylinder's Poisson solve: 30 iterations instead of 55;
+// at the Re 40 cylinder's 73k it costs a fifth iteration at the steady state); it is
+// used from kDeflateMin unknowns, CUIBM_DEFLATE=1 or 0 overrides that.
+constexpr int kDeflateMin = 200000;
+
+static void setup_deflation(Context &c, LinearSystem &S)
+{
+    S.ym = nullptr;
+    S.wdef = nullptr;
+    S.Edef = 0;
+    if (!(S.which == 2 && mixed_vcycle(S))) return;
+    const char *e = getenv("CUIBM_DEFLATE");
+    const bool mixed = S.precision == PRECISION_MIXED;
+    S.ym = c.carve<double>(S.n);
+    bool on = S.n >= kDeflateMin;
+    if (e && (e[0] == '0' || e[0] == '1')) on = e[0] == '1';
+    if (!mixed && !on) return;
+    std::vector<int> ptr, col;
+    std::vector<double> val, w(S.n, 0.0);
+    host_operator_csr(c, 2, nullptr, ptr, col, val);
+    for (size_t k = 0; k < col.size(); ++k) w[col[k]] += val[k];
+    double E = 0;
+    for (double v : w) E += v;
+    if (!(E != 0)) return;  // no pinned cell: the operator is singular, leave the cycle alone
+    S.wdef = c.carve<double>(S.n);
+    S.Edef = E;
+    CUIBM_TRY(cudaMemcpyAsync(S.wdef, w.data(), S.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
 }
 
@@ -1649,6 +1692,7 @@ void setup_fused(Context &c, LinearSystem &S)
         CUIBM_TRY(cudaMemcpyAsync(S.winv, wi.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
     }
+    setup_deflation(c, S);
     if (mixed) setup_mixed(c, S);
     upload_fargs(c, S);
 }

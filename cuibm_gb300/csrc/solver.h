@@ -125,6 +125,8 @@ struct LinearSystem {
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
     int precision = PRECISION_FP64;
     void *mixed = nullptr;  // mixed precision: the float tables (fused_solve.cu)
+    double *ym = nullptr, *wdef = nullptr;  // constant-mode correction of the SA cycle (Poisson):
+    double Edef = 0;                        // cycle output, A^T e, e^T A e
     FusedSyncState *fsync = nullptr;
     void *fargs = nullptr;  // device copy of the solver arguments
 };
