@@ -8,7 +8,8 @@
 //                        defaults of io/parseSimulationFile.cu:parseSimulation
 //   simParams.yaml       io/parseSimulationFile.cu (unknown SolverType -> NAVIER_STOKES
 //                        with a warning; unknown preconditioner -> NONE; startStep is read
-//                        but the reference never stores it, so it stays 0)
+//                        but the reference never stores it, so it stays 0 - except with
+//                        restart: true, where this build continues from that step's state)
 //   flow.yaml            io/parseFlowFile.cu (bad location/type is an error here, where
 //                        the reference prints and calls exit(0))
 //   domain.yaml          io/parseDomainFile.cu (only the description is read here;
@@ -270,6 +271,12 @@ std::string parse_simulation(const Node *doc, Params &P)
             P.solverType = ST_NAVIERSTOKES;
         }
         if (to_bool(n->get("restart"), b)) P.restart = b;
+        // startStep: the reference reads it and never stores it (the run starts at step
+        // 0); with restart: true it is the step whose saved state the run continues from
+        if (P.restart && to_int(n->get("startStep"), k)) {
+            if (k < 0) return "simParams.yaml: startStep must not be negative";
+            P.startStep = k;
+        }
         P.scaleCV = 2.0;
         if (to_double(n->get("scaleCV"), d)) P.scaleCV = d;
         P.VIV = 0;

@@ -412,8 +412,11 @@ int cuibm_initialise(cuibm_ctx *h)
         int zero[2] = {0, 0};
         CUIBM_TRY(cudaMemcpyAsync(c.step_counter_dev, &c.timeStep, sizeof(int), cudaMemcpyHostToDevice, c.stream));
         CUIBM_TRY(cudaMemcpyAsync(g_err_word_of(c), zero, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        // restart: the state the run wrote at startStep (fields, boundary arrays, body)
+        const bool restart = c.P.restart && c.P.startStep > 0;
+        if (c.has_body) initialise_body(c);  // luo_base::initialise movement at t = dt*timeStep
+        if (restart) read_restart_state(c);
         if (c.has_body) {
-            initialise_body(c);       // luo_base::initialise movement at t = dt*timeStep
             launch_tag_points(c);     // tagPoints()
             if (c.P.solverType == ST_LUO) launch_set_inside(c, c.u);  // luoIBM::zeroVelocity
         }
@@ -422,10 +425,11 @@ int cuibm_initialise(cuibm_ctx *h)
         if (c.P.writeOutput) {
             mkdir(c.P.caseFolder.c_str(), 0755);
             std::string f = c.P.caseFolder + "/iterations";
-            c.iterationsFile = fopen(f.c_str(), "w");
+            const char *mode = restart ? "a" : "w";  // a restarted run appends to the histories
+            c.iterationsFile = fopen(f.c_str(), mode);
             if (c.has_body) {
-                c.forceFile = fopen((c.P.caseFolder + "/forces").c_str(), "w");
-                c.midPositionFile = fopen((c.P.caseFolder + "/midPosition").c_str(), "w");
+                c.forceFile = fopen((c.P.caseFolder + "/forces").c_str(), mode);
+                c.midPositionFile = fopen((c.P.caseFolder + "/midPosition").c_str(), mode);
             }
             write_grid_file(c);
         }

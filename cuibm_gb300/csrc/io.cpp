@@ -10,8 +10,18 @@
 //   forces           luoIBM.cu:76-78 (time, Fx, Fy); fadlunModified.cu:64-78 (time, Fx,
 //                    FxX, FxY, FxU, Fy)
 //   midPosition      luo_base.cu:193-205 (timeStep, X, Y, U, V)
+// and one file of this build's own:
+//   NNNNNNN/state    every nsave steps beside q and lambda: what a step reads from the
+//                    one before it (velocity with its ghost values, the velocity solve's
+//                    start, the convection term for Adams-Bashforth, pressure, the
+//                    boundary arrays the convective outflow updates, the body).  With
+//                    `restart: true` and `startStep: k` initialise reads k/state and the
+//                    run continues as if it had not stopped.  The reference's restart
+//                    flag only sets the step counter (parseSimulationFile.cu:99-106)
+//                    and starts from the initial condition.
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 
@@ -46,6 +56,78 @@ static void write_array(const std::string &path, const std::vector<double> &v)
     fclose(fp);
 }
 
+namespace {
+const char kStateMagic[8] = {'C', 'U', 'I', 'B', 'M', 'R', 'S', '1'};
+
+// the device arrays of the restart state, in file order
+std::vector<std::pair<double *, size_t>> state_arrays(Context &c)
+{
+    const size_t nUV = c.g.nUV, nP = c.g.nP, bx = 2 * (size_t)c.g.ny - 1, by = 2 * (size_t)c.g.nx - 1;
+    std::vector<std::pair<double *, size_t>> S = {{c.u, nUV},          {c.uhat, nUV},        {c.N, nUV},
+                                                  {c.p, nP},           {c.bc[XMINUS], bx},   {c.bc[XPLUS], bx},
+                                                  {c.bc[YMINUS], by},  {c.bc[YPLUS], by}};
+    if (c.has_body) {
+        const size_t nb = c.body.total;
+        for (double *a : {c.ib.bx, c.ib.by, c.ib.uB, c.ib.vB, c.ib.uBk, c.ib.vBk}) S.push_back({a, nb});
+        S.push_back({c.ib.motion, 8});
+    }
+    return S;
+}
+}  // namespace
+
+static void write_restart_state(Context &c, const std::string &dir)
+{
+    auto S = state_arrays(c);
+    std::vector<std::vector<double>> host;
+    for (auto &a : S) {
+        host.emplace_back(a.second);
+        CUIBM_TRY(cudaMemcpyAsync(host.back().data(), a.first, a.second * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c.stream));
+    }
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    const std::string path = dir + "/state";
+    FILE *fp = fopen(path.c_str(), "wb");
+    if (!fp) throw InputError("cannot write " + path);
+    const int head[6] = {1, c.g.nx, c.g.ny, c.timeStep, c.has_body ? c.body.total : 0, (int)S.size()};
+    fwrite(kStateMagic, 1, 8, fp);
+    fwrite(head, sizeof(int), 6, fp);
+    for (auto &h : host) fwrite(h.data(), sizeof(double), h.size(), fp);
+    fclose(fp);
+}
+
+void read_restart_state(Context &c)
+{
+    char path[4096];
+    snprintf(path, sizeof path, "%s/%07d/state", c.P.caseFolder.c_str(), c.P.startStep);
+    FILE *fp = fopen(path, "rb");
+    if (!fp) throw InputError(std::string("restart: cannot open ") + path);
+    auto S = state_arrays(c);
+    char magic[8];
+    int head[6];
+    const bool ok = fread(magic, 1, 8, fp) == 8 && fread(head, sizeof(int), 6, fp) == 6 &&
+                    std::equal(magic, magic + 8, kStateMagic) && head[0] == 1 && head[1] == c.g.nx &&
+                    head[2] == c.g.ny && head[3] == c.P.startStep && head[4] == (c.has_body ? c.body.total : 0) &&
+                    head[5] == (int)S.size();
+    if (!ok) {
+        fclose(fp);
+        throw InputError(std::string("restart: ") + path + " does not hold this case's state at step " +
+                         std::to_string(c.P.startStep));
+    }
+    std::vector<std::vector<double>> host;
+    for (auto &a : S) {
+        host.emplace_back(a.second);
+        if (fread(host.back().data(), sizeof(double), a.second, fp) != a.second) {
+            fclose(fp);
+            throw InputError(std::string("restart: ") + path + " is truncated");
+        }
+    }
+    fclose(fp);
+    for (size_t k = 0; k < S.size(); ++k)
+        CUIBM_TRY(cudaMemcpyAsync(S[k].first, host[k].data(), S[k].second * sizeof(double), cudaMemcpyHostToDevice,
+                                  c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+}
+
 void write_step_output(Context &c)
 {
     if (!c.P.writeOutput) return;
@@ -63,6 +145,7 @@ void write_step_output(Context &c)
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
         write_array(std::string(dir) + "/q", q);
         write_array(std::string(dir) + "/lambda", lam);
+        write_restart_state(c, dir);
         if (c.has_body) {
             std::vector<double> bx(c.body.total), by(c.body.total);
             CUIBM_TRY(cudaMemcpyAsync(bx.data(), c.ib.bx, bx.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));

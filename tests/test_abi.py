@@ -125,3 +125,12 @@ def test_parses_reference_style_files(tmp_path):
     assert info.solver_type == cb.LUO and info.poisson_precond == 2 and info.velocity_precond == 1
     assert info.total_points == 126  # selfSize: int(2*pi*0.5/0.025) = 125 -> made even
     assert info.dt == 0.005 and info.nt == 1000 and info.nsave == 2000
+
+
+def test_start_step_only_with_restart(tmp_path):
+    """startStep is read but not used by the reference; with restart: true it is the
+    step whose saved state the run continues from."""
+    f = cases.cavity(str(tmp_path / "a"), n=16, nt=20, extra={"startStep": 10})
+    assert cb.case_info(f).time_step == 0
+    f = cases.cavity(str(tmp_path / "b"), n=16, nt=20, extra={"startStep": 10, "restart": True})
+    assert cb.case_info(f).time_step == 10
