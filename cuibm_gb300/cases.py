@@ -115,7 +115,7 @@ def cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000, nsave=None, lid=1.0, vel_tol
 def cylinder(folder, h=0.02, ratio=1.03, extent=15.0, core=0.6, points=157, nu=1.0 / 40, dt=0.01, nt=2000,
              nsave=None, method="LUO", vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION",
              pois_krylov=None, vel_krylov=None, vel_pc="DIAGONAL", radius=0.5, scaleCV=None, motion=None,
-             uinf=1.0, quiescent=False, precision=None, extra=None):
+             uinf=1.0, quiescent=False, precision=None, extra=None, vinf=0.0):
     """Circle of diameter 2*radius at the origin in [-extent, extent]^2."""
     sim = {"type": "simulation", "dt": float(dt), "nt": int(nt), "nsave": int(nsave or nt), "SolverType": method,
            "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov,
@@ -125,8 +125,9 @@ def cylinder(folder, h=0.02, ratio=1.03, extent=15.0, core=0.6, points=157, nu=1
     if scaleCV is not None:
         sim["scaleCV"] = float(scaleCV)
     u0 = 0.0 if quiescent else float(uinf)
-    flow = [{"type": "flow", "nu": float(nu), "initialVelocity": [u0, 0.0],
-             "boundaryConditions": bcs((u0, 0), (u0, 0), (u0, 0), (u0, 0), xp_type="CONVECTIVE")}]
+    v0 = 0.0 if quiescent else float(vinf)
+    flow = [{"type": "flow", "nu": float(nu), "initialVelocity": [u0, v0],
+             "boundaryConditions": bcs((u0, v0), (u0, v0), (u0, v0), (u0, v0), xp_type="CONVECTIVE")}]
     subs = [(-core, ratio), (core, 1.0), (extent, ratio)]
     dom = [axis("x", -extent, h, subs), axis("y", -extent, h, subs)]
     body = {"type": "circle", "circleOptions": [0.0, 0.0, float(radius), int(points), False, float(h)]}

@@ -317,9 +317,10 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
             (c.P.krylovVelocity == KRYLOV_CG || c.P.krylovPoisson == KRYLOV_CG))
             throw InputError("the Fadlun and embedded operators are not symmetric: use BICGSTAB (krylov: CG is for "
                              "the other methods)");
-        if (c.has_body && c.P.VIV != 0)
-            throw InputError("simulation VIV (flow-induced body motion) is not implemented by this build; "
-                             "prescribed motion (VIV: 0) is");
+        if (c.has_body && c.P.VIV != 0 && c.P.VIV != 1)
+            throw InputError("simulation VIV: 2 (strongly coupled sub-iterations of the step) is not implemented by "
+                             "this build; VIV: 0 (prescribed motion) and VIV: 1 (loosely coupled) are");
+        if (c.has_body && c.P.VIV == 1 && c.P.Ured <= 0) throw InputError("simulation Ured must be positive");
         if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
             throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
         if (c.has_body) {
@@ -336,6 +337,23 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
                     xs[k] = -a + c.body.dxp[k];
                     xs[n + k] = a + c.body.dxp[k];
                     ys[k] = ys[n + k] = c.body.y[k];
+                }
+                c.bb_tag = bounding_box(xs.data(), ys.data(), 2 * n, c.gx, c.gy, c.P.scaleCV);
+            }
+            if (c.P.VIV == 1) {
+                // flow-induced motion in y of unknown amplitude: tag over the box of the body
+                // displaced by up to half a body height either way (vortex-induced
+                // amplitudes of a free cylinder stay below that; a step whose body leaves the
+                // box reports an error)
+                const int n = c.body.total;
+                double ymin = c.body.y[0], ymax = c.body.y[0];
+                for (double v : c.body.y) ymin = std::min(ymin, v), ymax = std::max(ymax, v);
+                const double a = 0.5 * (ymax - ymin);
+                std::vector<double> xs(2 * n), ys(2 * n);
+                for (int k = 0; k < n; ++k) {
+                    xs[k] = xs[n + k] = c.body.dxp[k];
+                    ys[k] = c.body.y[k] - a;
+                    ys[n + k] = c.body.y[k] + a;
                 }
                 c.bb_tag = bounding_box(xs.data(), ys.data(), 2 * n, c.gx, c.gy, c.P.scaleCV);
             }
@@ -456,6 +474,11 @@ int cuibm_step(cuibm_ctx *h, int nsteps)
         int errw = 0;
         CUIBM_TRY(cudaMemcpyAsync(&errw, g_err_word_of(c), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        if (errw == kErrBodyOutsideTagBox) {
+            c.err = "ERROR: the body left the region it is tagged over by time step " + std::to_string(c.timeStep) +
+                    " (flow-induced motion beyond half a body height)";
+            return CUIBM_ERR_UNSUPPORTED;
+        }
         if (errw) {
             int sys = errw / 16, st = errw % 16;
             char msg[256];

@@ -1119,6 +1119,40 @@ __global__ void k_body_motion(int total, const int *step, int table_len, const d
     }
 }
 
+// flow-induced motion, loose coupling (luo_base/move.cu viv_movement_LC, VIV: 1): the
+// body is a spring-mounted cylinder free in y, reduced mass 2, reduced velocity Ured;
+// from the lift coefficient Cy = 2 Fy of this step and the pre-step centre and
+// velocity (motion[5], motion[7]) an implicit update gives the new velocity and
+// centre, then y = midY + offset, vB = vnew.  Every thread evaluates the same
+// expression from values no thread of this launch writes.
+__global__ void k_body_viv(int total, const double *force, double dt, double Ured, const double *bdy, double *by,
+                           double *vB, double *motion)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double Cy = force[1] * 2.0, Mred = 2.0, vold = motion[7], yold = motion[5];
+    const double a = dt * M_PI * M_PI * 4 / (Ured * Ured), b = dt * dt * 2 * M_PI * M_PI / (Ured * Ured);
+    const double vnew = (vold - a * (yold + dt / 2 * vold) + dt * Cy / 2 / Mred) / (1 + b);
+    const double ynew = yold + dt / 2 * (vnew + vold);
+    if (i < total) {
+        vB[i] = vnew;
+        by[i] = ynew + bdy[i];
+    }
+    if (i == 0) {
+        motion[1] = ynew;
+        motion[3] = vnew;
+    }
+}
+
+// A moving body is tagged over a fixed box that holds its travel; the control-volume
+// box of its current position must stay inside it.  If it does not, the step's error
+// word records it (the tags would be incomplete).
+__global__ void k_check_box(const int *bb, int ti0, int tj0, int tncx, int tncy, int *err, int code)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (bb[0] < ti0 || bb[1] < tj0 || bb[0] + bb[2] > ti0 + tncx || bb[1] + bb[3] > tj0 + tncy)
+        atomicCAS(err, 0, code);
+}
+
 // _pre_step copies of the body velocities: uB0 = uBk = uB (and v)
 __global__ void k_body_pre_step(int total, const double *uB, const double *vB, double *uBk, double *vBk,
                                 double *motion)
@@ -1296,7 +1330,7 @@ void setup_ib(Context &c)
     L.inNode = c.carve<int>(UV);
     CUIBM_TRY(cudaMemsetAsync(L.count, 0, 8 * sizeof(int), c.stream));
     const BodyState &B = c.body;
-    H.moving = B.xCoeff != 0 || B.uCoeff != 0;
+    H.moving = B.xCoeff != 0 || B.uCoeff != 0 || c.P.VIV == 1;
     // the host-evaluated prescribed motion for every step (luo_base/move.cu:121-146):
     // xnew = xC sin(2 pi f t + xPhase), unew = uC cos(2 pi f t + uPhase), t = dt * step
     H.table_len = c.P.nt + c.P.startStep + 2;
@@ -1439,6 +1473,13 @@ void launch_force(Context &c)
 void launch_body_motion(Context &c, double)
 {
     IbHost &H = hostside(c);
+    if (c.P.VIV == 1) {  // moveBody with VIV: 1 calls viv_movement_LC instead of set_movement
+        k_body_viv<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.ib.forceOut, c.P.dt,
+                                                                      (double)c.P.Ured, c.ib.bdy, c.ib.by, c.ib.vB,
+                                                                      c.ib.motion);
+        CUIBM_TRY(cudaGetLastError());
+        return;
+    }
     k_body_motion<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.step_counter_dev, H.table_len,
                                                                      H.motion_table, c.ib.bdx, c.ib.bx, c.ib.uB,
                                                                      c.ib.motion);
@@ -1461,6 +1502,9 @@ void launch_body_box(Context &c)
 {
     k_body_box<<<1, 32, 0, c.stream>>>(c.body.total, c.ib.bx, c.ib.by, c.x, c.y, c.g.nx, c.g.ny, c.P.scaleCV,
                                         hostside(c).bb);
+    CUIBM_TRY(cudaGetLastError());
+    k_check_box<<<1, 32, 0, c.stream>>>(hostside(c).bb, c.bb_tag.i0, c.bb_tag.j0, c.bb_tag.ncx, c.bb_tag.ncy,
+                                        c.err_word, kErrBodyOutsideTagBox);
     CUIBM_TRY(cudaGetLastError());
 }
 

@@ -80,6 +80,8 @@ struct RhsCoef {
 };
 
 // ---- Krylov state living in device memory -------------------------------------
+// the step's error word: solver * 16 + KStatus, or this (a moving body left its tagging box)
+constexpr int kErrBodyOutsideTagBox = 0x100;
 enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3, KS_TIMEOUT = 4,
                KS_STALLED = 5 };  // KS_STALLED: an FP32 inner solve stopped at a breakdown (refinement goes on)
 struct KrylovScalars {

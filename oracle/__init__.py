@@ -673,6 +673,10 @@ class LuoSolver:
         self.uBk = np.full(n, self.coef["uCoefficient"] * np.cos(
             2 * np.pi * self.coef["xfrequency"] * (0 - self.dt) + self.coef["uPhase"]))
         self.midX, self.midY = xnew, my
+        self.bdy = np.array([v - my for v in Y])
+        self.viv = int(self.sim.get("VIV", 0))
+        self.ured = float(int(self.sim.get("Ured", 3)))
+        self.vbody = 0.0
         self.T = tag_points(g, self.bx, self.by, self.uB, self.vB, self.bb, self.midX, self.midY)
         self.u = set_inside(self.u, self.T, self.uB[0], self.vB[0], g)
         self.A1 = Csr(g.nUV, *lhs1_coo(g, self.dt, self.nu))
@@ -695,7 +699,27 @@ class LuoSolver:
 
     @property
     def moving(self):
-        return self.coef["xCoefficient"] != 0 or self.coef["uCoefficient"] != 0
+        return self.coef["xCoefficient"] != 0 or self.coef["uCoefficient"] != 0 or self.viv == 1
+
+    def _move_body(self):
+        """luo_base::moveBody after the force (luo_base.cu:154-178): the prescribed motion
+        at t = dt * timeStep (set_movement, luo_base/move.cu:11-36) or, with VIV: 1, the
+        loosely coupled spring-mounted cylinder (viv_movement_LC, luo_base/move.cu:38-62)."""
+        if self.viv == 1:
+            Cy, Mred, Ured, dt = self.fy * 2.0, 2.0, self.ured, self.dt
+            vold, yold = self.vbody, self.midY  # the _pre_step copies centerVelocityV0, midY0
+            a = dt * np.pi * np.pi * 4 / (Ured * Ured)
+            b = dt * dt * 2 * np.pi * np.pi / (Ured * Ured)
+            vnew = (vold - a * (yold + dt / 2 * vold) + dt * Cy / 2 / Mred) / (1 + b)
+            ynew = yold + dt / 2 * (vnew + vold)
+            self.vbody, self.midY = vnew, ynew
+            self.vB = np.full(len(self.by), vnew)
+            self.by = np.array([ynew + v for v in self.bdy])
+            return
+        xnew, unew = self.motion(self.timeStep)
+        self.bx = np.array([xnew + v for v in self.bdx])
+        self.uB = np.full(len(self.bx), unew)
+        self.midX = xnew
 
     def _update_solver(self):
         """luo_base::updateSolver (luo_base.cu:137-146): the box of the moved body, its tags."""
@@ -764,10 +788,7 @@ class LuoSolver:
         self.u = set_inside(u, T, ub, vb, g)
         # body update: control-volume force, then the prescribed motion at t = dt * timeStep
         self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
-        xnew, unew = self.motion(self.timeStep)
-        self.bx = np.array([xnew + v for v in self.bdx])
-        self.uB = np.full(len(self.bx), unew)
-        self.midX = xnew
+        self._move_body()
         self._update_solver()
         self.iters = (it1, it2)
         self.timeStep += 1
@@ -844,10 +865,7 @@ class FadlunSolver(LuoSolver):
         self.u = fadlun_project(self.uhat, self.p, T, g, dt)
         # body update: control-volume force, then the prescribed motion at t = dt * timeStep
         self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
-        xnew, unew = self.motion(self.timeStep)
-        self.bx = np.array([xnew + v for v in self.bdx])
-        self.uB = np.full(len(self.bx), unew)
-        self.midX = xnew
+        self._move_body()
         self._update_solver()
         self.iters = (it1, it2)
         self.timeStep += 1
@@ -945,10 +963,7 @@ class EmbeddedSolver(LuoSolver):
         self.u = set_inside(u, T, ub, vb, g)
         # body update: control-volume force, then the prescribed motion at t = dt * timeStep
         self.fx, self.fy = force(self.u, self.uold, self.p, T, self.nu, g, dt, bb)
-        xnew, unew = self.motion(self.timeStep)
-        self.bx = np.array([xnew + v for v in self.bdx])
-        self.uB = np.full(len(self.bx), unew)
-        self.midX = xnew
+        self._move_body()
         self._update_solver()
         self.iters = (it1, it2)
         self.timeStep += 1
