@@ -20,7 +20,9 @@ GPU, one process each under torchrun); value = total cell-steps / max time.
 The line also carries "mixed_precision": the Re 550 cylinder (922 x 922) timed over
 the same steps in plain FP64 and with precision MIXED (FP32 multigrid cycles inside
 FP64 BiCGSTAB, FP32 inner solves under FP64 refinement), with both runs' C_D
-(--no-mixed skips it; single-GPU runs only).
+(--no-mixed skips it; single-GPU runs only), and "batched": 64 independent cavities
+and cylinders run one after another and as one batch (cuibm_batch_*), aggregate
+Mcell-steps/s of both (--no-batch skips it).
 
 --impl reference times the reference's algorithm on the host CPU cores: the
 oracle port (oracle/, a C restatement of the reference's kernels and of its
@@ -315,6 +317,82 @@ def precision_comparison(local, warm=20, steps=20):
     return out
 
 
+def batch_cases(tmp, n=64, seed=0):
+    """The batched workload: n instances drawn with numpy's default_rng(seed) - half
+    lid-driven cavities (N from {96, 128, ..., 512}, Re log-uniform in [100, 1000]),
+    half impulsively started cylinders (external method, the Re 40 case's stretching
+    rule with core h from {0.04, 0.03, 0.02}, round(pi/h) body points made even, Re
+    log-uniform in [40, 300], dt 0.005).  The cavities' dt is 0.01 x 64/N (CFL 0.64,
+    as at 64 x 64): at dt 0.01 the finer cavities are unstable (CFL up to 5) and
+    overflow within a few dozen steps."""
+    import numpy as np
+    from cuibm_gb300 import cases
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        if k % 2 == 0:
+            N = int(rng.choice(np.arange(96, 513, 32)))
+            Re = float(np.exp(rng.uniform(np.log(100), np.log(1000))))
+            f = cases.cavity(os.path.join(tmp, "cav%02d" % k), n=N, nu=1.0 / Re, dt=0.01 * 64 / N, nt=1000000,
+                             vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG")
+        else:
+            h = float(rng.choice([0.04, 0.03, 0.02]))
+            Re = float(np.exp(rng.uniform(np.log(40), np.log(300))))
+            pts = int(round(np.pi / h))
+            pts += pts % 2
+            f = cases.cylinder(os.path.join(tmp, "cyl%02d" % k), h=h, ratio=1.03, points=pts, nu=1.0 / Re, dt=0.005,
+                               nt=1000000)
+        out.append(f)
+    return out
+
+
+def batch_comparison(local, n=64, warm=3, steps=20):
+    """The batched workload run one instance after another (each with the whole GPU)
+    and as one batch (cuibm_batch_*: every instance on its own stream, persistent
+    solves on a quarter of the SMs), both plain FP64, timed over the same steps with
+    wall-clock time around synchronised GPU work.  Aggregate Mcell-steps/s."""
+    import time as _time
+
+    import torch
+
+    import cuibm_gb300 as cb
+    out = {"workload": "%d instances (seed 0): half lid-driven cavities N 96-512, half cylinders h 0.04-0.02, "
+                       "external method, FP64" % n, "steps_timed": "%d-%d" % (warm + 1, warm + steps)}
+    with tempfile.TemporaryDirectory() as tmp:
+        folders = batch_cases(tmp, n)
+        cells, el = 0, 0.0
+        for f in folders:  # one after another: each instance alone on the GPU
+            s = cb.NavierStokesSolver(f, ["-deviceNumber", str(local)])
+            s.set_option("write_output", 0)
+            s.initialise()
+            s.stepTime(warm)
+            torch.cuda.synchronize()
+            s.set_option("step_sync", 0)  # steps enqueued back to back, as the batch does
+            t0 = _time.perf_counter()
+            s.stepTime(steps)
+            torch.cuda.synchronize()
+            el += _time.perf_counter() - t0
+            s.set_option("step_sync", 1)
+            s.stepTime(0)  # raises if a solve failed
+            cells += s.info.numP
+            s.close()
+        out["sequential"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC}
+        b = cb.Batch(folders, ["-deviceNumber", str(local)])
+        for s in b.instances:
+            s.set_option("write_output", 0)
+        b.initialise()
+        b.stepTime(warm)
+        torch.cuda.synchronize()
+        t0 = _time.perf_counter()
+        b.stepTime(steps)
+        torch.cuda.synchronize()
+        el = _time.perf_counter() - t0
+        b.close()
+        out["batched"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC}
+    out["speedup_batched_over_sequential"] = round(out["sequential"]["s"] / out["batched"]["s"], 3)
+    return out
+
+
 def profiled_traffic(kernel):
     """DRAM bytes per launch of the kernel from the committed ncu summary
     (profiles/*.md, a line 'dram_bytes_per_launch <kernel> <bytes>'); None where
@@ -373,6 +451,7 @@ def main():
     ap.add_argument("--roofline-kernel", default="poisson_solve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the Re 550 FP64 / mixed-precision comparison")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances comparison")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
@@ -403,6 +482,8 @@ def main():
         line["cpu_baseline"] = cpu_baseline(a.workload)
     if not a.no_mixed and world == 1:
         line["mixed_precision"] = precision_comparison(local)
+    if not a.no_batch and world == 1:
+        line["batched"] = batch_comparison(local)
     print(json.dumps(line))
 
 

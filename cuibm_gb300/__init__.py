@@ -112,6 +112,16 @@ def library():
         L.cuibm_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.cuibm_cv_force_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, ip, ip, ip, ip, ip, ip, ctypes.c_double,
                                              ctypes.c_double, vp, vp]
+        L.cuibm_batch_create.argtypes = [ip, ctypes.POINTER(cp), ip, ctypes.POINTER(cp), ip, ctypes.POINTER(vp)]
+        L.cuibm_batch_initialise.argtypes = [vp]
+        L.cuibm_batch_step.argtypes = [vp, ip]
+        L.cuibm_batch_size.argtypes = [vp]
+        L.cuibm_batch_instance.argtypes = [vp, ip]
+        L.cuibm_batch_instance.restype = vp
+        L.cuibm_batch_error.argtypes = [vp]
+        L.cuibm_batch_error.restype = cp
+        L.cuibm_batch_destroy.argtypes = [vp]
+        L.cuibm_batch_destroy.restype = None
         _lib = L
     return _lib
 
@@ -156,9 +166,18 @@ class NavierStokesSolver:
     def shutDown(self):
         self._check(self._L.cuibm_shutdown(self._h))
 
+    @classmethod
+    def _view(cls, L, h):
+        """A solver object over a context that something else owns (a batch instance)."""
+        s = cls.__new__(cls)
+        s._h, s._L, s._owner = ctypes.c_void_p(h), L, False
+        s.info = s.get_info()
+        return s
+
     def close(self):
         if getattr(self, "_h", None):
-            self._L.cuibm_destroy(self._h)
+            if getattr(self, "_owner", True):
+                self._L.cuibm_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -296,3 +315,55 @@ def case_array(case_folder, name, args=()):
     if st != OK:
         raise CuibmError(st, L.cuibm_case_error().decode())
     return out
+
+
+class Batch:
+    """Many independent cases advanced together on one GPU (cuibm_batch_*).
+
+    Each instance is a full solver with its own stream; its persistent solves use
+    ``solver_blocks`` blocks (None: a quarter of the SMs) so that several instances'
+    solves run at once.  ``instances`` are solver objects for fields, forces and
+    output; the batch owns them.
+    """
+
+    def __init__(self, case_folders, args=(), solver_blocks=None):
+        L = library()
+        folders = [str(f).encode() for f in case_folders]
+        farr = (ctypes.c_char_p * len(folders))(*folders)
+        argv = [a.encode() if isinstance(a, str) else a for a in args]
+        aarr = (ctypes.c_char_p * max(1, len(argv)))(*argv)
+        h = ctypes.c_void_p()
+        st = L.cuibm_batch_create(len(folders), farr, len(argv), aarr, int(solver_blocks or 0), ctypes.byref(h))
+        if st != OK:
+            raise CuibmError(st, L.cuibm_batch_error(None).decode())
+        self._h, self._L = h, L
+        self.instances = [NavierStokesSolver._view(L, L.cuibm_batch_instance(h, k)) for k in range(len(folders))]
+
+    def _check(self, st):
+        if st != OK:
+            raise CuibmError(st, self._L.cuibm_batch_error(self._h).decode())
+
+    def initialise(self):
+        self._check(self._L.cuibm_batch_initialise(self._h))
+
+    def stepTime(self, nsteps=1):
+        self._check(self._L.cuibm_batch_step(self._h, int(nsteps)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for s in self.instances:
+                s._h = None
+            self._L.cuibm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -28,6 +28,7 @@ UNITS = {
     "geometry.cpp": [],
     "fields.cpp": [],
     "io.cpp": [],
+    "batch.cpp": [],
     "context.cu": [],
     "ns_kernels.cu": [],
     "krylov.cu": [],

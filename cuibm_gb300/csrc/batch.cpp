@@ -1,0 +1,122 @@
+// Batched instances: many independent cases advanced together on one GPU, on top
+// of the single-case C ABI (no counterpart in the reference, which runs one case
+// per process, src/cuIBM.cu:61-74).
+//
+// Why this shape on GB300: at the benchmark sizes (10^4..3x10^5 cells) a step is
+// latency-bound - grid barriers of the persistent solves, short dependent phases -
+// and one instance leaves most of the GPU idle.  Each instance here keeps its own
+// stream and step graph, and its persistent solves are launched on a fraction of
+// the SMs (-solverBlocks), so the cooperative solves of several instances are
+// resident at once and the other instances' short kernels fill the gaps.  The
+// instances never wait on one another: an instance that needs more iterations in a
+// step delays only itself (a single launch stepping all instances in lockstep
+// phases would hold every instance to the slowest one's iteration count).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cuibm.h"
+
+struct cuibm_batch {
+    std::vector<cuibm_ctx *> ctx;
+    std::string err;
+};
+
+static std::string g_batch_create_error;
+
+static int batch_fail(cuibm_batch *b, int code, const std::string &msg)
+{
+    if (b) b->err = msg;
+    else g_batch_create_error = msg;
+    return code;
+}
+
+extern "C" {
+
+int cuibm_batch_create(int n, const char *const *case_folders, int argc, const char **argv, int solver_blocks,
+                       cuibm_batch **out)
+{
+    if (!out || n <= 0 || !case_folders) return batch_fail(nullptr, CUIBM_ERR_BAD_INPUT, "batch: no cases");
+    *out = nullptr;
+    int blocks = solver_blocks;
+    if (blocks <= 0) {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return batch_fail(nullptr, CUIBM_ERR_CUDA, "batch: cannot query the device");
+        blocks = sms / 4 > 0 ? sms / 4 : 1;
+    }
+    const std::string nb = std::to_string(blocks);
+    std::vector<const char *> args(argv, argv + (argc > 0 ? argc : 0));
+    args.push_back("-solverBlocks");
+    args.push_back(nb.c_str());
+    cuibm_batch *b = new cuibm_batch();
+    for (int k = 0; k < n; ++k) {
+        cuibm_ctx *c = nullptr;
+        const int st = cuibm_create(case_folders[k], (int)args.size(), args.data(), &c);
+        if (st != CUIBM_OK) {
+            const std::string msg = "batch: instance " + std::to_string(k) + " (" + case_folders[k] +
+                                    "): " + cuibm_last_error(nullptr);
+            cuibm_batch_destroy(b);
+            return batch_fail(nullptr, st, msg);
+        }
+        b->ctx.push_back(c);
+    }
+    *out = b;
+    return CUIBM_OK;
+}
+
+int cuibm_batch_initialise(cuibm_batch *b)
+{
+    if (!b) return CUIBM_ERR_STATE;
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        const int st = cuibm_initialise(b->ctx[k]);
+        if (st != CUIBM_OK)
+            return batch_fail(b, st, "batch: instance " + std::to_string(k) + ": " + cuibm_last_error(b->ctx[k]));
+        // steps are enqueued without waiting; cuibm_batch_step checks them at its end
+        cuibm_set_option(b->ctx[k], "step_sync", 0);
+    }
+    return CUIBM_OK;
+}
+
+int cuibm_batch_step(cuibm_batch *b, int nsteps)
+{
+    if (!b) return CUIBM_ERR_STATE;
+    if (nsteps < 0) return batch_fail(b, CUIBM_ERR_BAD_INPUT, "batch: nsteps < 0");
+    for (int s = 0; s < nsteps; ++s)
+        for (size_t k = 0; k < b->ctx.size(); ++k) {
+            const int st = cuibm_step(b->ctx[k], 1);
+            if (st != CUIBM_OK)
+                return batch_fail(b, st,
+                                  "batch: instance " + std::to_string(k) + ": " + cuibm_last_error(b->ctx[k]));
+        }
+    int first = CUIBM_OK;
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        const int st = cuibm_step(b->ctx[k], 0);  // waits for the instance and checks its solves
+        if (st != CUIBM_OK && first == CUIBM_OK) {
+            first = st;
+            batch_fail(b, st, "batch: instance " + std::to_string(k) + ": " + cuibm_last_error(b->ctx[k]));
+        }
+    }
+    return first;
+}
+
+int cuibm_batch_size(const cuibm_batch *b) { return b ? (int)b->ctx.size() : 0; }
+
+cuibm_ctx *cuibm_batch_instance(cuibm_batch *b, int k)
+{
+    return (b && k >= 0 && k < (int)b->ctx.size()) ? b->ctx[k] : nullptr;
+}
+
+const char *cuibm_batch_error(const cuibm_batch *b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
+
+void cuibm_batch_destroy(cuibm_batch *b)
+{
+    if (!b) return;
+    for (cuibm_ctx *c : b->ctx) cuibm_destroy(c);
+    delete b;
+}
+
+}  // extern "C"

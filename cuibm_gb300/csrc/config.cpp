@@ -512,6 +512,11 @@ std::string load_case(const std::string &folder_in, int argc, const char **argv,
         else if (!strcmp(a, "-dt")) ok = cli_value(argv[++i], P.dt);
         else if (!strcmp(a, "-velocityTol")) ok = cli_value(argv[++i], P.velocity.tolerance);
         else if (!strcmp(a, "-poissonTol")) ok = cli_value(argv[++i], P.poisson.tolerance);
+        // this build's own: the persistent solves' grid size (batched instances share the GPU)
+        else if (!strcmp(a, "-solverBlocks")) ok = cli_value(argv[++i], P.solverBlocks) && P.solverBlocks >= 0;
+        else if (!strcmp(a, "-solverThreads"))
+            ok = cli_value(argv[++i], P.solverThreads) && P.solverThreads >= 0 && P.solverThreads <= 512 &&
+                 P.solverThreads % 32 == 0;
         if (!ok) return std::string("bad value for ") + a;
     }
     if (!(P.dt > 0) || P.nt < 0 || P.nsave <= 0) return "dt must be > 0, nt >= 0 and nsave > 0";

@@ -51,6 +51,8 @@ struct Params {
     // inputs
     std::string caseFolder;
     int deviceNumber = 0;
+    int solverBlocks = 0;   // -solverBlocks: blocks of the persistent solves (0: one per SM)
+    int solverThreads = 0;  // -solverThreads: their block size (0: 512)
     // flow
     double nu = 0.01, uInitial = 1.0, vInitial = 0.0, uPerturb = 0.0, vPerturb = 0.0;
     BC bc[4][2];

@@ -70,7 +70,7 @@
 
 namespace cuibm {
 
-constexpr int kFT = 512;  // threads per block
+constexpr int kFT = 512;  // threads per block at most (the default; -solverThreads asks fewer)
 constexpr int kMaxLevels = 10;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 constexpr int kGroupR = 8;  // lanes per restriction row (15-30 entries)
@@ -437,7 +437,9 @@ __device__ __forceinline__ bool inner_breakdown(double v)
 
 __device__ __forceinline__ int solve_state(double rnorm, double tol, int it, int maxit)
 {
-    if (!(rnorm == rnorm)) return KS_NAN;
+    // a non-finite residual or right-hand side (an overflowed field passes
+    // ||r|| <= tol ||b|| as inf <= inf) is reported, not taken as convergence
+    if (!isfinite(rnorm) || !isfinite(tol)) return KS_NAN;
     if (rnorm <= tol) return KS_CONVERGED;
     if (it >= maxit) return KS_MAXIT;
     return KS_RUNNING;
@@ -1378,7 +1380,7 @@ static cudaLaunchConfig_t coop_config(Context &c, LinearSystem &S, cudaLaunchAtt
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(S.fused_grid);
-    cfg.blockDim = dim3(kFT);
+    cfg.blockDim = dim3(S.fused_threads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = c.stream;
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -1668,11 +1670,13 @@ void setup_fused(Context &c, LinearSystem &S)
     CUIBM_TRY(cudaGetDevice(&dev));
     CUIBM_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CUIBM_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    CUIBM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kFT, 0));
+    S.fused_threads = c.P.solverThreads > 0 ? c.P.solverThreads : kFT;
+    CUIBM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, S.fused_threads, 0));
     if (!coop || per_sm < 1) return;
     int want = 1;
     if (const char *e = getenv("CUIBM_FUSED_BLOCKS_PER_SM")) want = std::max(1, atoi(e));
     S.fused_grid = sms * std::min(per_sm, want);
+    if (c.P.solverBlocks > 0) S.fused_grid = std::min(sms * per_sm, c.P.solverBlocks);
     S.fused_fn = fn;
     const int n = S.n;
     S.p2 = c.carve<double>(n);

@@ -115,7 +115,9 @@ __device__ __forceinline__ void set_cond(cudaGraphConditionalHandle h, int use, 
 __device__ __forceinline__ void finish_status(KrylovScalars *ks, int *err_word, int which)
 {
     if (ks->status == KS_RUNNING) {
-        if (!(ks->rnorm == ks->rnorm)) ks->status = KS_NAN;
+        // a non-finite residual or right-hand side (an overflowed field passes
+        // ||r|| <= tol ||b|| as inf <= inf) is reported, not taken as convergence
+        if (!isfinite(ks->rnorm) || !isfinite(ks->tol)) ks->status = KS_NAN;
         else if (ks->rnorm <= ks->tol) ks->status = KS_CONVERGED;
         else if (ks->it >= ks->maxit) ks->status = KS_MAXIT;
     }

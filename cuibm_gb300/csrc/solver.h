@@ -122,7 +122,7 @@ struct LinearSystem {
     int body_kernels = 0;  // kernel nodes in one captured iteration body
     // persistent solver (fused_solve.cu); fused_fn is null where it does not apply
     void *fused_fn = nullptr;
-    int fused_grid = 0;
+    int fused_grid = 0, fused_threads = 512;
     double *p2 = nullptr, *AMp2 = nullptr, *fpartials = nullptr;
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
     int precision = PRECISION_FP64;

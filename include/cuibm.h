@@ -214,6 +214,27 @@ int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p,
                            const double *dx, const double *dy, int nx, int ny, int bb_i, int bb_j, int bb_ncx,
                            int bb_ncy, double nu, double dt, double *force_out, void *stream);
 
+/* ---- batched instances ------------------------------------------------------
+ * Many independent cases advanced together on one GPU.  No counterpart in the
+ * reference, which runs one case per process (src/cuIBM.cu:61-74).  Each instance
+ * is a full context (cuibm_batch_instance gives its handle for fields, forces and
+ * output) with its own stream; its persistent solves use solver_blocks blocks
+ * (<= 0: a quarter of the SMs), so that several instances' solves run at once
+ * while each instance's step stays one graph.  argc/argv are the command-line
+ * overrides every instance gets (cuibm_create).  cuibm_batch_step enqueues nsteps
+ * steps of every instance, interleaved step by step, then waits for all and
+ * checks their solves; the first failure is reported with its instance index.
+ * Error text: cuibm_batch_error(). */
+typedef struct cuibm_batch cuibm_batch;
+int cuibm_batch_create(int n, const char *const *case_folders, int argc, const char **argv, int solver_blocks,
+                       cuibm_batch **out);
+int cuibm_batch_initialise(cuibm_batch *b);
+int cuibm_batch_step(cuibm_batch *b, int nsteps);
+int cuibm_batch_size(const cuibm_batch *b);
+cuibm_ctx *cuibm_batch_instance(cuibm_batch *b, int k);
+const char *cuibm_batch_error(const cuibm_batch *b);
+void cuibm_batch_destroy(cuibm_batch *b);
+
 /* Host-only (no GPU needed): parse a case folder and build its grid and body
  * exactly as cuibm_create does.  cuibm_case_array copies CUIBM_F_X..CUIBM_F_YV
  * or CUIBM_F_BODY_X/Y into dst (count doubles).  Replaces the reference's

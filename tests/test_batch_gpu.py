@@ -1,0 +1,58 @@
+"""Batched instances (cuibm_batch_*): independent cases of different kinds and sizes
+advanced together, each on its own stream with persistent solves on a fraction of
+the SMs.  Every instance ends where it ends when run alone (tight tolerances: the
+solves' reduction order differs with the grid size, so fields agree to 1e-9
+relative L2, not bit for bit); a bad case is reported with its instance index."""
+import numpy as np
+import pytest
+
+cb = pytest.importorskip("cuibm_gb300")
+from cuibm_gb300 import cases  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def make(tmp_path):
+    return [
+        cases.cavity(str(tmp_path / "cav32"), n=32, nu=0.01, dt=0.01, nt=100, vel_tol=1e-12, pois_tol=1e-12),
+        cases.cavity(str(tmp_path / "cav40"), n=40, nu=0.005, dt=0.01, nt=100, vel_tol=1e-12, pois_tol=1e-12),
+        cases.cylinder(str(tmp_path / "cyl"), h=0.05, ratio=1.1, extent=3.0, core=0.6, points=48, nu=0.025, dt=0.01,
+                       nt=100, vel_tol=1e-12, pois_tol=1e-12, method="LUO"),
+        cases.cylinder(str(tmp_path / "emb"), h=0.05, ratio=1.1, extent=3.0, core=0.6, points=48, nu=0.025,
+                       dt=0.01, nt=100, vel_tol=1e-12, pois_tol=1e-12, method="OSC_CYLINDER"),
+    ]
+
+
+@pytest.mark.parametrize("blocks", [None, 5])
+def test_batch_matches_instances_run_alone(tmp_path, blocks):
+    folders = make(tmp_path)
+    alone = []
+    for f in folders:
+        with cb.NavierStokesSolver(f) as s:
+            s.set_option("write_output", 0)
+            s.initialise()
+            s.stepTime(12)
+            alone.append((s.get("u"), s.get("p"), s.forces() if s.info.total_points else None))
+    with cb.Batch(folders, solver_blocks=blocks) as b:
+        for s in b.instances:
+            s.set_option("write_output", 0)
+        b.initialise()
+        b.stepTime(5)
+        b.stepTime(7)
+        for s, (u, p, f) in zip(b.instances, alone):
+            assert s.timeStep == 12
+            assert rel_l2(s.get("u"), u) < 1e-9
+            assert rel_l2(s.get("p"), p) < 1e-8
+            if f is not None:
+                assert abs(s.forces()[0] - f[0]) < 1e-8
+
+
+def test_batch_reports_the_bad_instance(tmp_path):
+    folders = make(tmp_path)[:2] + [str(tmp_path / "missing")]
+    with pytest.raises(cb.CuibmError) as e:
+        cb.Batch(folders)
+    assert "instance 2" in str(e.value)
