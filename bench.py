@@ -80,6 +80,10 @@ def workload_config(workload):
     if workload == "cavity64":
         return {"workload": "lid-driven cavity 64x64, Re 100, plain method", "nx": 64, "ny": 64, "dt": 0.01,
                 "velocity": "BiCGSTAB + diagonal, rtol 1e-8", "poisson": "CG + smoothed aggregation, rtol 1e-8"}
+    if workload == "cylinder_re550":
+        return {"workload": "impulsively started cylinder Re 550, external (Luo) ghost-node method, " + PRECISION,
+                "nx": 922, "ny": 922, "body_points": 629, "dt": 0.002,
+                "velocity": KRYLOV + " + diagonal, rtol 1e-8", "poisson": KRYLOV + " + smoothed aggregation, rtol 1e-8"}
     return {"workload": "impulsively started cylinder Re 40, external (Luo) ghost-node method, plain FP64",
             "nx": 270, "ny": 270, "body_points": 157, "dt": 0.01,
             "velocity": KRYLOV + " + diagonal, rtol 1e-5", "poisson": KRYLOV + " + smoothed aggregation, rtol 1e-5"}
