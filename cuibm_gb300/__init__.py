@@ -36,7 +36,7 @@ _FIELD_NAMES = [
     "dist_node", "dist_between", "uv_body", "ustar", "pstar", "dpdn", "bi_p",
     "ghost_uv_index", "ghost_uv_coef", "hybrid_uv_index", "hybrid_uv_coef",
     "ghost_p_index", "ghost_p_coef", "hybrid_p_index", "hybrid_p_coef",
-    "image_value_uv", "cfl", "work_x", "work_y", "solve_trace",
+    "image_value_uv", "cfl", "work_x", "work_y", "solve_trace", "body_motion",
 ]
 FIELDS = {n: i for i, n in enumerate(_FIELD_NAMES)}
 _INT_FIELDS = {"ghost_tags_uv", "hybrid_tags_uv", "hybrid_tags_uv2", "ghost_tags_p", "hybrid_tags_p",
@@ -204,7 +204,8 @@ class NavierStokesSolver:
         sizes = {"bc_xminus": 2 * ny - 1, "bc_xplus": 2 * ny - 1, "bc_yminus": 2 * nx - 1, "bc_yplus": 2 * nx - 1,
                  "x": nx, "dx": nx, "xu": nx - 1, "xv": nx, "y": ny, "dy": ny, "yu": ny, "yv": ny - 1,
                  "body_x": nb, "body_y": nb, "body_uB": nb, "body_vB": nb,
-                 "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024}
+                 "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024,
+                 "body_motion": 12}
         if name in sizes:
             return sizes[name]
         if name in ("p", "p_old", "rhs2", "ghost_tags_p", "hybrid_tags_p", "bip_x", "bip_y", "ipp_x", "ipp_y",

@@ -136,14 +136,20 @@ static bool is_fadlun(const Context &c) { return c.P.solverType == ST_FADLUN && 
 static bool is_embedded(const Context &c) { return c.P.solverType == ST_OSC && c.has_body; }
 static bool is_ib(const Context &c) { return is_luo(c) || is_fadlun(c) || is_embedded(c); }
 
-static void phase_generate_rhs1(Context &c)
+static bool strong_coupling(const Context &c) { return is_ib(c) && c.P.VIV == 2; }
+
+// first: the step's first pass, which moves N to Nold; the later passes of a strongly
+// coupled step keep Nold and restart from u = uold (luoIBM/intermediateVelocity.cu:33,
+// luo_iter/intermediateVelocity.cu:29; the Fadlun method has no such reset)
+static void phase_generate_rhs1(Context &c, bool first)
 {
     PhaseTimer t(c, "Intermediate Velocity Setup");
+    if (!first && (is_luo(c) || is_embedded(c))) launch_copy(c, c.u, c.uold, c.g.nUV);
     // updateRobinBoundary, rhs1GNInterpolation, zeroVelocity, rhs1HNInterpolation
     if (is_luo(c)) launch_ib_rhs1(c);
     if (is_fadlun(c)) launch_robin(c);
     if (is_embedded(c)) launch_ib_robin_inside(c);  // updateRobinBoundary, setInsideVelocity
-    launch_rhs1(c, false);  // with the embedded method's update_rhs1_x/y
+    launch_rhs1(c, false, first);  // with the embedded method's update_rhs1_x/y
     if (is_fadlun(c)) launch_fadlun_rhs1(c);  // updateRHS1forIBX/Y
 }
 
@@ -199,14 +205,10 @@ static void phase_update_body(Context &c)
     }
 }
 
-static void record_step(Context &c, bool in_graph)
+// One pass of the step's phases, from the explicit terms to the body update.
+static void record_pass(Context &c, bool in_graph, bool first)
 {
-    if (is_ib(c)) {
-        launch_copy(c, c.p_old, c.p, c.g.nP);    // _pre_step: pressure_old = pressure
-        launch_copy(c, c.uold, c.u, c.g.nUV);    //            uold = u
-        launch_body_pre_step(c);                 //            uB0 = uB, ...
-    }
-    phase_generate_rhs1(c);
+    phase_generate_rhs1(c, first);
     phase_solve_velocity(c, in_graph);
     if (is_luo(c)) {
         PhaseTimer t(c, "Intermediate Velocity Weight");
@@ -219,7 +221,70 @@ static void record_step(Context &c, bool in_graph)
         launch_ib_after_poisson(c);  // hybrid pressure, weightPressure, ghost pressure
     }
     phase_project(c);
-    phase_update_body(c);    // motion reads the step counter before it advances
+    phase_update_body(c);  // motion reads the step counter before it advances
+}
+
+// The strongly coupled step's further passes (luo_base.cu:211-223), after its first:
+// while |SCtol| > 0.001 or fewer than two passes ran.  In a graph the passes are the
+// body of a WHILE conditional node (default value 1: the second pass always runs)
+// whose condition k_coupling_next sets; otherwise the host reads the answer after
+// each pass.
+static void record_coupling_loop(Context &c, bool in_graph)
+{
+    if (!in_graph) {
+        for (int k = 1; k <= kCouplingMaxIterations; ++k) {
+            record_pass(c, false, false);
+            launch_coupling_next(c, 0, 0);
+            double more = 0;
+            CUIBM_TRY(cudaMemcpyAsync(&more, c.ib.motion + 10, sizeof more, cudaMemcpyDeviceToHost, c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            if (more == 0) break;
+        }
+        return;
+    }
+    cudaStreamCaptureStatus st;
+    cudaGraph_t graph;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    CUIBM_TRY(cudaStreamGetCaptureInfo(c.stream, &st, nullptr, &graph, &deps, nullptr, &ndeps));
+    cudaGraphConditionalHandle h;
+    CUIBM_TRY(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CUIBM_TRY(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
+    cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+    cudaStream_t main = c.stream;
+    CUIBM_TRY(cudaStreamBeginCaptureToGraph(c.coupling_stream, bodyg, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeRelaxed));
+    c.stream = c.coupling_stream;
+    try {
+        record_pass(c, true, false);
+        launch_coupling_next(c, h, 1);
+    } catch (...) {
+        c.stream = main;
+        cudaGraph_t dummy;
+        cudaStreamEndCapture(c.coupling_stream, &dummy);
+        throw;
+    }
+    c.stream = main;
+    cudaGraph_t got;
+    CUIBM_TRY(cudaStreamEndCapture(c.coupling_stream, &got));
+    CUIBM_TRY(cudaStreamUpdateCaptureDependencies(c.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+}
+
+static void record_step(Context &c, bool in_graph)
+{
+    if (is_ib(c)) {
+        launch_copy(c, c.p_old, c.p, c.g.nP);    // _pre_step: pressure_old = pressure
+        launch_copy(c, c.uold, c.u, c.g.nUV);    //            uold = u
+        launch_body_pre_step(c);                 //            uB0 = uB, ..., SCtol, SC_count
+    }
+    record_pass(c, in_graph, true);
+    if (strong_coupling(c)) record_coupling_loop(c, in_graph);
     launch_step_counter(c);  // _post_step: timeStep++
     {
         PhaseTimer t(c, "CFL");
@@ -317,10 +382,14 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
             (c.P.krylovVelocity == KRYLOV_CG || c.P.krylovPoisson == KRYLOV_CG))
             throw InputError("the Fadlun and embedded operators are not symmetric: use BICGSTAB (krylov: CG is for "
                              "the other methods)");
-        if (c.has_body && c.P.VIV != 0 && c.P.VIV != 1)
-            throw InputError("simulation VIV: 2 (strongly coupled sub-iterations of the step) is not implemented by "
-                             "this build; VIV: 0 (prescribed motion) and VIV: 1 (loosely coupled) are");
-        if (c.has_body && c.P.VIV == 1 && c.P.Ured <= 0) throw InputError("simulation Ured must be positive");
+        if (c.has_body && c.P.VIV != 0 && c.P.VIV != 1 && c.P.VIV != 2)
+            throw InputError("simulation VIV must be 0 (prescribed motion), 1 (loosely coupled) or 2 (strongly "
+                             "coupled)");
+        if (c.has_body && c.P.VIV != 0 && c.P.Ured <= 0) throw InputError("simulation Ured must be positive");
+        if (c.has_body && c.P.VIV == 2 && c.P.solverType == ST_FADLUN)
+            throw InputError("simulation VIV: 2 needs the LUO or OSC_CYLINDER method: the Fadlun method's "
+                             "generateRHS1 does not restart a sub-iteration from uold, so each one advances the "
+                             "flow by another time step and the coupling test does not settle");
         if (c.P.solverType != ST_NAVIERSTOKES && c.body.total == 0)
             throw InputError("an immersed-boundary SolverType needs a body in bodies.yaml");
         if (c.has_body) {
@@ -340,7 +409,7 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
                 }
                 c.bb_tag = bounding_box(xs.data(), ys.data(), 2 * n, c.gx, c.gy, c.P.scaleCV);
             }
-            if (c.P.VIV == 1) {
+            if (c.P.VIV == 1 || c.P.VIV == 2) {
                 // flow-induced motion in y of unknown amplitude: tag over the box of the body
                 // displaced by up to half a body height either way (vortex-induced
                 // amplitudes of a free cylinder stay below that; a step whose body leaves the
@@ -365,6 +434,7 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
         c.device = c.P.deviceNumber;
         CUIBM_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
         CUIBM_TRY(cudaStreamCreateWithFlags(&c.side_stream, cudaStreamNonBlocking));
+        CUIBM_TRY(cudaStreamCreateWithFlags(&c.coupling_stream, cudaStreamNonBlocking));
         CUIBM_TRY(cudaEventCreate(&c.ev0));
         CUIBM_TRY(cudaEventCreate(&c.ev1));
         CUIBM_TRY(cudaHostAlloc(&c.h_scalars, 64 * sizeof(double), cudaHostAllocDefault));
@@ -474,6 +544,11 @@ int cuibm_step(cuibm_ctx *h, int nsteps)
         int errw = 0;
         CUIBM_TRY(cudaMemcpyAsync(&errw, g_err_word_of(c), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        if (errw == kErrCouplingNotConverged) {
+            c.err = "ERROR: the strongly coupled sub-iterations (VIV: 2) of a step did not converge in " +
+                    std::to_string(kCouplingMaxIterations) + " passes by time step " + std::to_string(c.timeStep);
+            return CUIBM_ERR_NOT_CONVERGED;
+        }
         if (errw == kErrBodyOutsideTagBox) {
             c.err = "ERROR: the body left the region it is tagged over by time step " + std::to_string(c.timeStep) +
                     " (flow-induced motion beyond half a body height)";
@@ -645,7 +720,7 @@ int cuibm_run(cuibm_ctx *h, int op)
         };
         switch (op) {
         case CUIBM_OP_RHS1_TERMS: launch_rhs1(c, true); break;
-        case CUIBM_OP_GENERATE_RHS1: phase_generate_rhs1(c); break;
+        case CUIBM_OP_GENERATE_RHS1: phase_generate_rhs1(c, true); break;
         case CUIBM_OP_SOLVE_VELOCITY: phase_solve_velocity(c, false); break;
         case CUIBM_OP_WEIGHT_UHAT: need_ib(); launch_weight_uhat(c); break;
         case CUIBM_OP_GENERATE_RHS2:  // preRHS2Interpolation, then the right-hand side
@@ -822,6 +897,8 @@ int cuibm_launch_count(cuibm_ctx *h, long long *per_step)
     Context &c = h->c;
     CUIBM_GUARD(h, {
         if (!c.step_exec) return fail(h, CUIBM_ERR_STATE, "launch counts need the step graph");
+        if (strong_coupling(c))
+            return fail(h, CUIBM_ERR_STATE, "a strongly coupled step's launches vary with its sub-iterations");
         *per_step = c.static_kernels + (long long)c.sys1.body_kernels * read_body_runs(c, c.sys1) +
                     (long long)c.sys2.body_kernels * read_body_runs(c, c.sys2);
     });
@@ -949,6 +1026,7 @@ void cuibm_destroy(cuibm_ctx *h)
     if (c.ev0) cudaEventDestroy(c.ev0);
     if (c.ev1) cudaEventDestroy(c.ev1);
     if (c.side_stream) cudaStreamDestroy(c.side_stream);
+    if (c.coupling_stream) cudaStreamDestroy(c.coupling_stream);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
 }

@@ -1143,6 +1143,52 @@ __global__ void k_body_viv(int total, const double *force, double dt, double Ure
     }
 }
 
+// flow-induced motion, strong coupling (luo_base/move.cu viv_movement_SC, VIV: 2):
+// the same implicit update from the pre-step centre and velocity, with the new centre
+// relaxed (factor 0.9) against the one of the previous sub-iteration, motion[1]; the
+// relative change of the centre, (previous - new) / previous, goes to motion[8] (the
+// reference's SCtol).  One block: every thread reads motion[1] before thread 0
+// overwrites it.
+__global__ void k_body_viv_sc(int total, const double *force, double dt, double Ured, const double *bdy,
+                              double *by, double *vB, double *motion)
+{
+    const double Cy = force[1] * 2.0, Mred = 2.0, relax = 0.9, vold = motion[7], yold = motion[5];
+    const double yprev = motion[1];
+    const double a = dt * M_PI * M_PI * 4 / (Ured * Ured), b = dt * dt * 2 * M_PI * M_PI / (Ured * Ured);
+    const double vnew = (vold - a * (yold + dt / 2 * vold) + dt * Cy / 2 / Mred) / (1 + b);
+    const double ynew = relax * (yold + dt / 2 * (vnew + vold)) + (1 - relax) * yprev;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        vB[i] = vnew;
+        by[i] = ynew + bdy[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        motion[1] = ynew;
+        motion[3] = vnew;
+        motion[8] = (yprev - ynew) / yprev;
+    }
+}
+
+// The loop test of a strongly coupled step (luo_base.cu:215): another sub-iteration
+// while |SCtol| > 0.001 or fewer than two ran.  motion[9] counts the passes done
+// (the first included), motion[10] holds the answer for a host-driven loop; in a graph it sets the
+// WHILE node's condition.  The reference has no limit: this one stops after
+// kCouplingMaxIterations and flags the step.  A NaN SCtol (a centre at exactly 0
+// that does not move) fails the test, as it does in the reference.
+__global__ void k_coupling_next(double *motion, int *err, int cap, cudaGraphConditionalHandle h, int use_cond)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const double done = motion[9] + 1;
+    motion[9] = done;
+    int more = fabs(motion[8]) > 0.001 || done < 2;
+    if (more && done >= cap) {
+        atomicCAS(err, 0, kErrCouplingNotConverged);
+        more = 0;
+    }
+    motion[10] = more;
+    if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
 // A moving body is tagged over a fixed box that holds its travel; the control-volume
 // box of its current position must stay inside it.  If it does not, the step's error
 // word records it (the tags would be incomplete).
@@ -1167,6 +1213,8 @@ __global__ void k_body_pre_step(int total, const double *uB, const double *vB, d
         motion[5] = motion[1];
         motion[6] = motion[2];
         motion[7] = motion[3];
+        motion[8] = 0.0001;  // luo_base.cu:213-214: SCtol, and the passes done by the loop
+        motion[9] = 1;       // test: the step's first pass, recorded before the loop
     }
 }
 
@@ -1269,7 +1317,7 @@ void setup_ib(Context &c)
     b.vBk = c.carve<double>(nb);
     b.bdx = c.carve<double>(nb);
     b.bdy = c.carve<double>(nb);
-    b.motion = c.carve<double>(8);
+    b.motion = c.carve<double>(kMotionLen);
     b.forceOut = c.carve<double>(8);  // Fx, Fy, then the six partial sums
     const int fblocks = 64;
     b.forcePart = c.carve<double>(6 * fblocks);
@@ -1330,7 +1378,7 @@ void setup_ib(Context &c)
     L.inNode = c.carve<int>(UV);
     CUIBM_TRY(cudaMemsetAsync(L.count, 0, 8 * sizeof(int), c.stream));
     const BodyState &B = c.body;
-    H.moving = B.xCoeff != 0 || B.uCoeff != 0 || c.P.VIV == 1;
+    H.moving = B.xCoeff != 0 || B.uCoeff != 0 || c.P.VIV == 1 || c.P.VIV == 2;
     // the host-evaluated prescribed motion for every step (luo_base/move.cu:121-146):
     // xnew = xC sin(2 pi f t + xPhase), unew = uC cos(2 pi f t + uPhase), t = dt * step
     H.table_len = c.P.nt + c.P.startStep + 2;
@@ -1374,7 +1422,7 @@ void initialise_body(Context &c)
     up(c.ib.vBk, vBk);
     up(c.ib.bdx, B.dxp);
     up(c.ib.bdy, B.dyp);
-    double motion[8] = {xnew, B.midY, unew, 0, xnew, B.midY, unew, 0};
+    double motion[kMotionLen] = {xnew, B.midY, unew, 0, xnew, B.midY, unew, 0, 0.0001, 0, 0, 0};
     CUIBM_TRY(cudaMemcpyAsync(c.ib.motion, motion, sizeof motion, cudaMemcpyHostToDevice, c.stream));
     int bb[4] = {c.bb.i0, c.bb.j0, c.bb.ncx, c.bb.ncy};
     CUIBM_TRY(cudaMemcpyAsync(H.bb, bb, sizeof bb, cudaMemcpyHostToDevice, c.stream));
@@ -1480,6 +1528,12 @@ void launch_body_motion(Context &c, double)
         CUIBM_TRY(cudaGetLastError());
         return;
     }
+    if (c.P.VIV == 2) {  // ... and with VIV: 2 viv_movement_SC
+        k_body_viv_sc<<<1, kBlock, 0, c.stream>>>(c.body.total, c.ib.forceOut, c.P.dt, (double)c.P.Ured, c.ib.bdy,
+                                                  c.ib.by, c.ib.vB, c.ib.motion);
+        CUIBM_TRY(cudaGetLastError());
+        return;
+    }
     k_body_motion<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.step_counter_dev, H.table_len,
                                                                      H.motion_table, c.ib.bdx, c.ib.bx, c.ib.uB,
                                                                      c.ib.motion);
@@ -1494,6 +1548,12 @@ void launch_body_pre_step(Context &c)
 }
 
 void launch_step_counter(Context &c) { k_step_counter<<<1, 1, 0, c.stream>>>(c.step_counter_dev); }
+
+void launch_coupling_next(Context &c, cudaGraphConditionalHandle h, int use_cond)
+{
+    k_coupling_next<<<1, 32, 0, c.stream>>>(c.ib.motion, c.err_word, kCouplingMaxIterations, h, use_cond);
+    CUIBM_TRY(cudaGetLastError());
+}
 
 bool body_moves(Context &c) { return c.has_body && hostside(c).moving; }
 

@@ -513,16 +513,21 @@ static EmbRhs1 emb_rhs1_args(Context &c)
     return EmbRhs1{E.pid1, E.rscale1, E.pns1, E.pint1, E.cap1, E.gin, P.gvIdx, P.gvMask, P.gvW, c.ib.uB, c.ib.vB};
 }
 
-void launch_rhs1(Context &c, bool debug_terms)
+// shift = false: a later sub-iteration of a strongly coupled step, whose Nold is
+// already the previous step's N (luoIBM/intermediateVelocity.cu:38 keeps Nold)
+void launch_rhs1(Context &c, bool debug_terms, bool shift)
 {
     int nb = blocks_for(c.g.nUV);
     const EmbRhs1 e = debug_terms ? EmbRhs1{} : emb_rhs1_args(c);
     if (debug_terms)
         k_rhs1<false, true><<<nb, kBlock, 0, c.stream>>>(c.rc, c.g, bc_ptrs(c), c.u, c.N, c.Nold, c.rhs1, c.L, c.bc1,
                                                          c.P.nu, c.P.dt, e);
-    else
+    else if (shift)
         k_rhs1<true, false><<<nb, kBlock, 0, c.stream>>>(c.rc, c.g, bc_ptrs(c), c.u, c.N, c.Nold, c.rhs1, nullptr,
                                                          nullptr, c.P.nu, c.P.dt, e);
+    else
+        k_rhs1<false, false><<<nb, kBlock, 0, c.stream>>>(c.rc, c.g, bc_ptrs(c), c.u, c.N, c.Nold, c.rhs1, nullptr,
+                                                          nullptr, c.P.nu, c.P.dt, e);
     CUIBM_TRY(cudaGetLastError());
 }
 

@@ -82,6 +82,10 @@ struct RhsCoef {
 // ---- Krylov state living in device memory -------------------------------------
 // the step's error word: solver * 16 + KStatus, or this (a moving body left its tagging box)
 constexpr int kErrBodyOutsideTagBox = 0x100;
+// ... or this (the strongly coupled sub-iterations of a step reached kCouplingMaxIterations)
+constexpr int kErrCouplingNotConverged = 0x200;
+constexpr int kCouplingMaxIterations = 50;
+constexpr int kMotionLen = 12;  // doubles of IbArrays::motion
 enum KStatus { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXIT = 2, KS_NAN = 3, KS_TIMEOUT = 4,
                KS_STALLED = 5 };  // KS_STALLED: an FP32 inner solve stopped at a breakdown (refinement goes on)
 struct KrylovScalars {
@@ -154,7 +158,8 @@ struct IbArrays {
     // force partial sums
     double *forcePart;
     double *forceOut;  // [fx, fy]
-    double *motion;    // [midX, midY, centerVelocityU, centerVelocityV, midX0, midY0, U0, V0]
+    double *motion;    // kMotionLen: [midX, midY, centerVelocityU, centerVelocityV, midX0, midY0,
+                       //  U0, V0, SCtol, sub-iterations done, continue flag, spare]
 };
 
 struct Context {
@@ -167,6 +172,7 @@ struct Context {
     Grid g{};
     int device = 0;
     cudaStream_t stream = nullptr, side_stream = nullptr;
+    cudaStream_t coupling_stream = nullptr;  // captures the body of a strongly coupled step's loop
     int *err_word = nullptr;          // device: first failing solve, system*16 + status
     int *step_counter_dev = nullptr;  // device copy of timeStep (read by the body motion)
     std::vector<double> htab;         // host copy of the metric tables (see upload_ns_tables)
@@ -253,7 +259,7 @@ void upload_ns_tables(Context &c);
 void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val);
 void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
                        std::vector<double> &val);
-void launch_rhs1(Context &c, bool debug_terms);
+void launch_rhs1(Context &c, bool debug_terms, bool shift = true);  // shift: Nold = N first
 void launch_rhs2(Context &c, const double *uh);
 void launch_project(Context &c);
 void launch_initial_velocity(Context &c);
@@ -318,6 +324,7 @@ void launch_body_pre_step(Context &c);
 bool body_moves(Context &c);
 void launch_body_box(Context &c);
 void launch_step_counter(Context &c);
+void launch_coupling_next(Context &c, cudaGraphConditionalHandle h, int use_cond);  // VIV: 2 loop test
 void initialise_body(Context &c);
 
 // io.cpp / fields.cu

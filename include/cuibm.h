@@ -111,6 +111,9 @@ enum {
     CUIBM_F_SOLVE_TRACE,     /* uint64 2*1024: per-barrier timestamps (ns) of the last persistent
                                 velocity (first 1024) and Poisson solve: [count, start, ...];
                                 written only while the option "trace_solve" is 1 */
+    CUIBM_F_BODY_MOTION,     /* D 12: body centre x, y and centre velocity u, v; the same at the
+                                start of the step; the coupling tolerance and the sub-iterations
+                                of the last strongly coupled step (VIV: 2); 4 spare */
     CUIBM_F_COUNT
 };
 

@@ -618,6 +618,7 @@ def bicgstab_pc(A, b, x, rtol, maxit, pc, amg=None):
 
 
 _PC = {"NONE": 0, "DIAGONAL": 1, "SMOOTHED_AGGREGATION": 2}
+COUPLING_MAX_PASSES = 50  # passes of a strongly coupled step before it is reported unconverged
 
 
 class LuoSolver:
@@ -677,6 +678,10 @@ class LuoSolver:
         self.viv = int(self.sim.get("VIV", 0))
         self.ured = float(int(self.sim.get("Ured", 3)))
         self.vbody = 0.0
+        self.vBk = self.vB.copy()
+        self.Nold = np.zeros(g.nUV)
+        self.midY0, self.vbody0 = self.midY, self.vbody
+        self.sctol, self.sub_iterations = 1e-4, 0
         self.T = tag_points(g, self.bx, self.by, self.uB, self.vB, self.bb, self.midX, self.midY)
         self.u = set_inside(self.u, self.T, self.uB[0], self.vB[0], g)
         self.A1 = Csr(g.nUV, *lhs1_coo(g, self.dt, self.nu))
@@ -699,19 +704,28 @@ class LuoSolver:
 
     @property
     def moving(self):
-        return self.coef["xCoefficient"] != 0 or self.coef["uCoefficient"] != 0 or self.viv == 1
+        return self.coef["xCoefficient"] != 0 or self.coef["uCoefficient"] != 0 or self.viv in (1, 2)
 
     def _move_body(self):
         """luo_base::moveBody after the force (luo_base.cu:154-178): the prescribed motion
         at t = dt * timeStep (set_movement, luo_base/move.cu:11-36) or, with VIV: 1, the
-        loosely coupled spring-mounted cylinder (viv_movement_LC, luo_base/move.cu:38-62)."""
-        if self.viv == 1:
+        loosely coupled spring-mounted cylinder (viv_movement_LC, luo_base/move.cu:38-62),
+        or with VIV: 2 the strongly coupled one (viv_movement_SC, luo_base/move.cu:64-94):
+        the same update with the new centre relaxed (0.9) against the previous
+        sub-iteration's, and SCtol = (previous - new) / previous."""
+        if self.viv in (1, 2):
             Cy, Mred, Ured, dt = self.fy * 2.0, 2.0, self.ured, self.dt
-            vold, yold = self.vbody, self.midY  # the _pre_step copies centerVelocityV0, midY0
+            vold, yold = self.vbody0, self.midY0  # the _pre_step copies centerVelocityV0, midY0
             a = dt * np.pi * np.pi * 4 / (Ured * Ured)
             b = dt * dt * 2 * np.pi * np.pi / (Ured * Ured)
             vnew = (vold - a * (yold + dt / 2 * vold) + dt * Cy / 2 / Mred) / (1 + b)
-            ynew = yold + dt / 2 * (vnew + vold)
+            if self.viv == 1:
+                ynew = yold + dt / 2 * (vnew + vold)
+            else:
+                relax, yprev = 0.9, self.midY
+                ynew = relax * (yold + dt / 2 * (vnew + vold)) + (1 - relax) * yprev
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    self.sctol = float(np.float64(yprev - ynew) / np.float64(yprev))
             self.vbody, self.midY = vnew, ynew
             self.vB = np.full(len(self.by), vnew)
             self.by = np.array([ynew + v for v in self.bdy])
@@ -745,13 +759,40 @@ class LuoSolver:
             raise RuntimeError("oracle %s solve did not converge" % key)
         return x, it
 
-    def step(self):
-        g, T, bb, dt = self.g, self.T, self.bb, self.dt
-        xm, xp, ym, yp = self.bc
-        ub, vb = float(self.uB[0]), float(self.vB[0])
-        # _pre_step
+    def _pre_step(self):
+        """luo_base::_pre_step (luo_base.cu:235-248) and the loop state of luo_base.cu:213-214."""
         self.uold = self.u.copy()
         self.uBk = self.uB.copy()
+        self.vBk = self.vB.copy()
+        self.Nold = self.N
+        self.midY0, self.vbody0 = self.midY, self.vbody
+        self.sctol = 1e-4
+
+    def step(self):
+        """luo_base::stepTime (luo_base.cu:208-233): one pass of the phases, or with VIV: 2
+        passes while |SCtol| > 0.001 or fewer than two ran (this restatement stops with an
+        error after COUPLING_MAX_PASSES; the reference has no limit)."""
+        self._pre_step()
+        self._pass(True)
+        done = 1
+        if self.viv == 2:
+            while True:
+                self._pass(False)
+                done += 1
+                more = abs(self.sctol) > 0.001 or done < 2
+                if not more:
+                    break
+                if done >= COUPLING_MAX_PASSES:
+                    raise RuntimeError("strong coupling did not converge")
+        self.sub_iterations = done
+        self.timeStep += 1
+
+    def _pass(self, first):
+        g, T, bb, dt = self.g, self.T, self.bb, self.dt
+        xm, xp, ym, yp = self.bc
+        if not first:
+            self.u = self.uold.copy()  # generateRHS1: u = uold (luoIBM/intermediateVelocity.cu:33)
+        ub, vb = float(self.uB[0]), float(self.vB[0])
         # generateRHS1: Robin outflow, ghost nodes, inside, hybrid nodes, explicit terms
         xp[:] = robin(self.u, xp, g, dt)
         u, _ = ghost_velocity(0, self.u, T, ub, g, bb)
@@ -761,11 +802,10 @@ class LuoSolver:
         ustar, _ = hybrid_velocity(0, u, ustar, T, ub, g, bb)
         ustar, _ = hybrid_velocity(1, u, ustar, T, vb, g, bb)
         bc = (xm, xp, ym, yp)
-        Nold = self.N
         self.N = generate_N(u, g, bc)
         L = generate_L(u, g, bc, self.nu)
         b1 = generate_bc1(u, g, bc, self.nu, dt)
-        rhs1 = generate_rhs(L, Nold, self.N, u, b1, dt)
+        rhs1 = generate_rhs(L, self.Nold, self.N, u, b1, dt)
         self.uhat, it1 = self._solve(1, rhs1, self.uhat)
         uh = weight(0, self.uhat, ustar, T, g, bb)
         uh = weight(1, uh, ustar, T, g, bb)
@@ -776,7 +816,7 @@ class LuoSolver:
         rhs2 = generate_rhs2(uh, g, bc)
         self.p, it2 = self._solve(2, rhs2, self.p)
         dudt = (float(self.uB[0]) - float(self.uBk[0])) / dt
-        dvdt = (float(self.vB[0]) - 0.0) / dt if False else 0.0
+        dvdt = (float(self.vB[0]) - float(self.vBk[0])) / dt  # nonzero in a later coupled pass
         pstar, _ = hybrid_pressure(self.p, T, dudt, dvdt, g, bb)
         p = weight(2, self.p, pstar, T, g, bb)
         p, _ = ghost_pressure(p, T, dudt, dvdt, g, bb)
@@ -791,7 +831,6 @@ class LuoSolver:
         self._move_body()
         self._update_solver()
         self.iters = (it1, it2)
-        self.timeStep += 1
 
 
 def csr_from_coo_summed(n, row, col, val):
@@ -842,20 +881,17 @@ class FadlunSolver(LuoSolver):
             self.amg1 = Amg(self.A1) if self.cfg["velocity"][2] == 2 else None
             self.amg2 = Amg(self.A2) if self.cfg["Poisson"][2] == 2 else None
 
-    def step(self):
+    def _pass(self, first):
+        # a later coupled pass continues from the current u: generateRHS1 has no u = uold
         g, T, bb, dt = self.g, self.T, self.bb, self.dt
         xm, xp, ym, yp = self.bc
-        # _pre_step
-        self.uold = self.u.copy()
-        self.uBk = self.uB.copy()
-        Nold = self.N
         # generateRHS1
         xp[:] = robin(self.u, xp, g, dt)
         bc = (xm, xp, ym, yp)
         self.N = generate_N(self.u, g, bc)
         L = generate_L(self.u, g, bc, self.nu)
         b1 = generate_bc1(self.u, g, bc, self.nu, dt)
-        rhs1 = generate_rhs(L, Nold, self.N, self.u, b1, dt)
+        rhs1 = generate_rhs(L, self.Nold, self.N, self.u, b1, dt)
         rhs1 = fadlun_update_rhs1(rhs1, T, g)
         self.uhat, it1 = self._solve(1, rhs1, self.uhat)
         # generateRHS2, Poisson
@@ -868,7 +904,6 @@ class FadlunSolver(LuoSolver):
         self._move_body()
         self._update_solver()
         self.iters = (it1, it2)
-        self.timeStep += 1
 
 
 class EmbeddedSolver(LuoSolver):
@@ -919,22 +954,20 @@ class EmbeddedSolver(LuoSolver):
             raise RuntimeError("oracle %s solve did not converge" % ("velocity" if which == 1 else "Poisson"))
         return x, it
 
-    def step(self):
+    def _pass(self, first):
         g, T, bb, dt = self.g, self.T, self.bb, self.dt
         xm, xp, ym, yp = self.bc
         ub, vb = float(self.uB[0]), float(self.vB[0])
-        # _pre_step
-        self.uold = self.u.copy()
-        self.uBk = self.uB.copy()
-        Nold = self.N
         # intermediate_velocity_setup: u = uold, Robin outflow, inside velocity, explicit terms
+        if not first:
+            self.u = self.uold.copy()
         xp[:] = robin(self.u, xp, g, dt)
         u = set_inside(self.u, T, ub, vb, g)
         bc = (xm, xp, ym, yp)
         self.N = generate_N(u, g, bc)
         L = generate_L(u, g, bc, self.nu)
         b1 = generate_bc1(u, g, bc, self.nu, dt)
-        rhs1 = generate_rhs(L, Nold, self.N, u, b1, dt)
+        rhs1 = generate_rhs(L, self.Nold, self.N, u, b1, dt)
         alpha = iter_alpha(0, T, g, bb)
         iter_alpha(1, T, g, bb, alpha)
         S = Stencils(g.nUV)
@@ -948,10 +981,12 @@ class EmbeddedSolver(LuoSolver):
         self.uhat, it1 = self._solve(1, rhs1, self.uhat)
         # poisson_setup
         rhs2 = generate_rhs2(self.uhat, g, bc)
-        dudt = (float(self.uB[0]) - float(self.uBk[0])) / dt  # zero: _pre_step set uBk = uB
+        # zero in a step's first pass (_pre_step set uBk = uB), not in a later coupled pass
+        dudt = (float(self.uB[0]) - float(self.uBk[0])) / dt
+        dvdt = (float(self.vB[0]) - float(self.vBk[0])) / dt
         Sp = Stencils(g.nP)
-        ghost_pressure(self.p, T, dudt, 0.0, g, bb, set_=False, S=Sp)
-        hybrid_pressure(self.p, T, dudt, 0.0, g, bb, S=Sp)
+        ghost_pressure(self.p, T, dudt, dvdt, g, bb, set_=False, S=Sp)
+        hybrid_pressure(self.p, T, dudt, dvdt, g, bb, S=Sp)
         row, col, val, ns, interp = iter_lhs2(g, dt, T, Sp, iter_alpha(2, T, g, bb), bb)
         self.A2 = csr_from_coo_summed(g.nP, row, col, val)
         rhs2 = iter_update_rhs2(rhs2, ns, interp, g)
@@ -966,4 +1001,3 @@ class EmbeddedSolver(LuoSolver):
         self._move_body()
         self._update_solver()
         self.iters = (it1, it2)
-        self.timeStep += 1
