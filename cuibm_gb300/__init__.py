@@ -37,6 +37,7 @@ _FIELD_NAMES = [
     "ghost_uv_index", "ghost_uv_coef", "hybrid_uv_index", "hybrid_uv_coef",
     "ghost_p_index", "ghost_p_coef", "hybrid_p_index", "hybrid_p_coef",
     "image_value_uv", "cfl", "work_x", "work_y", "solve_trace", "body_motion",
+    "surface_force",
 ]
 FIELDS = {n: i for i, n in enumerate(_FIELD_NAMES)}
 _INT_FIELDS = {"ghost_tags_uv", "hybrid_tags_uv", "hybrid_tags_uv2", "ghost_tags_p", "hybrid_tags_p",
@@ -46,7 +47,7 @@ _OP_NAMES = [
     "rhs1_terms", "generate_rhs1", "solve_velocity", "weight_uhat", "generate_rhs2", "rhs2", "solve_poisson",
     "weight_pressure", "project", "project_velocity", "update_body", "apply_lhs1", "apply_lhs2", "tag_points",
     "ghost_velocity_u", "ghost_velocity_uhat", "hybrid_velocity", "hybrid_pressure", "ghost_pressure",
-    "set_inside", "robin_boundary", "force", "cfl",
+    "set_inside", "robin_boundary", "force", "cfl", "surface_force", "surface_force_corrected",
 ]
 OPS = {n: i for i, n in enumerate(_OP_NAMES)}
 
@@ -205,7 +206,7 @@ class NavierStokesSolver:
                  "x": nx, "dx": nx, "xu": nx - 1, "xv": nx, "y": ny, "dy": ny, "yu": ny, "yv": ny - 1,
                  "body_x": nb, "body_y": nb, "body_uB": nb, "body_vB": nb,
                  "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024,
-                 "body_motion": 12}
+                 "body_motion": 12, "surface_force": 3 * nb + 2}
         if name in sizes:
             return sizes[name]
         if name in ("p", "p_old", "rhs2", "ghost_tags_p", "hybrid_tags_p", "bip_x", "bip_y", "ipp_x", "ipp_y",
@@ -238,6 +239,16 @@ class NavierStokesSolver:
         fx, fy = ctypes.c_double(), ctypes.c_double()
         self._check(self._L.cuibm_get_forces(self._h, ctypes.byref(fx), ctypes.byref(fy)))
         return fx.value, fy.value
+
+    def surface_force(self, corrected=False):
+        """The surface-integral force on the body (luo_base::luoForce, which the
+        reference's step leaves unused): (Fx, Fy, pressure, du/dn, dv/dn per body
+        point) from the current fields; corrected=True fixes the reference's two
+        index slips (its pressure search's j start, its v row stride)."""
+        self.run("surface_force_corrected" if corrected else "surface_force")
+        a = self.get("surface_force")
+        n = (a.size - 2) // 3
+        return a[3 * n], a[3 * n + 1], a[:n], a[n:2 * n], a[2 * n:3 * n]
 
     def iterations(self):
         a, b = ctypes.c_int(), ctypes.c_int()

@@ -404,6 +404,7 @@ std::string parse_domain(const Node *doc, Params &P)
             ax.ratios.push_back(r);
         }
         P.axis[a] = ax;
+        P.midH = ax.mid_h;
         seen[a] = true;
     }
     if (!seen[0] || !seen[1]) return "domain.yaml: both x and y directions are required";

@@ -64,6 +64,7 @@ struct Params {
     LinearSolve velocity, poisson;
     // grid and bodies
     AxisDesc axis[2];
+    double midH = 0;  // mid_h of the direction listed last in domain.yaml (the reference's domain::mid_h)
     std::vector<BodyDesc> bodies;
     // build-specific keys (absent from reference cases; ignored by the reference)
     int krylovVelocity = KRYLOV_BICGSTAB;

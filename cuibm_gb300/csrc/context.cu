@@ -752,6 +752,8 @@ int cuibm_run(cuibm_ctx *h, int op)
         case CUIBM_OP_ROBIN_BOUNDARY: launch_robin(c); break;
         case CUIBM_OP_FORCE: need_ib(); launch_force(c); break;
         case CUIBM_OP_CFL: launch_cfl(c); break;
+        case CUIBM_OP_SURFACE_FORCE: need_ib(); launch_surface_force(c, 1, false); break;
+        case CUIBM_OP_SURFACE_FORCE_CORRECTED: need_ib(); launch_surface_force(c, 2, false); break;
         default: return fail(h, CUIBM_ERR_BAD_INPUT, "unknown operation " + std::to_string(op));
         }
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
@@ -818,7 +820,16 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
     } else if (k == "step_sync") {
         c.step_sync = value != 0;
     } else if (k == "write_output") c.P.writeOutput = value != 0;
-    else return fail(h, CUIBM_ERR_BAD_INPUT, "unknown option " + k);
+    else if (k == "force_method") {
+        const int m = (int)value;
+        if (m < 0 || m > 2 || m != value) return fail(h, CUIBM_ERR_BAD_INPUT, "force_method must be 0, 1 or 2");
+        if (m && c.has_body && c.body.total < 2)
+            return fail(h, CUIBM_ERR_BAD_INPUT, "the surface force needs at least two body points");
+        if (m != c.force_method) {
+            c.force_method = m;
+            if (c.initialised && c.use_graph) CUIBM_GUARD(h, { build_step_graph(c); });
+        }
+    } else return fail(h, CUIBM_ERR_BAD_INPUT, "unknown option " + k);
     return CUIBM_OK;
 }
 

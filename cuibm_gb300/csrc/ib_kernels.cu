@@ -1319,6 +1319,7 @@ void setup_ib(Context &c)
     b.bdy = c.carve<double>(nb);
     b.motion = c.carve<double>(kMotionLen);
     b.forceOut = c.carve<double>(8);  // Fx, Fy, then the six partial sums
+    b.surf = c.carve<double>(3 * (size_t)nb + 2);
     const int fblocks = 64;
     b.forcePart = c.carve<double>(6 * fblocks);
 
@@ -1510,8 +1511,146 @@ void launch_ib_after_poisson(Context &c) { launch_ib(c, PH_HYBRID_P | PH_WEIGHT_
 void launch_ib_after_projection(Context &c) { launch_ib(c, PH_GHOST_U | PH_INSIDE, c.u); }
 void launch_ib_robin_inside(Context &c) { launch_ib(c, PH_ROBIN | PH_INSIDE, c.u); }
 
+// ---- surface-integral force (luo_base/calculateForce.cu:76-98 luoForce with
+// luo_base/kernels/calculateForce.cu:12-213; dead code in the reference, whose
+// moveBody calls the control-volume force instead) -------------------------------
+// Per body point: the pressure, interpolated in angle between the two nearest
+// body-intercept pressures of the ghost pressure nodes in a 4x4 window; du/dn and
+// dv/dn, one-sided from the bilinear velocity at a point sqrt(2) mid_h out along the
+// radius; then the traction (viscous tangential stress minus pressure) times the
+// segment length |x0 - x1|, summed over the points in index order.
+// Mode 1 keeps the reference's two index slips: the pressure search starts its j
+// index at the box's i start (luoForce passes startI twice) and dv/dn reads the v
+// block with row stride nx-1.  Mode 2 uses the box's j start and stride nx.
+// Where the reference reads past an array or an unset index (no intercept on one
+// side of the point), the searches stop at the array ends and the point's
+// pressure is NaN.
+struct SurfaceArgs {
+    int n, nx, ny, mode;
+    const double *bx, *by, *uB, *vB, *u, *biP, *bipX, *bipY;
+    const int *ghostP, *bb;
+    const double *xu, *yu, *xv, *yv;
+    const double *motion;  // moving body: centre on the device; else midX, midY
+    double midX, midY, nu, midH;
+    double *surf, *forceOut;
+};
+
+__device__ static double surface_pressure(const SurfaceArgs &A, double x, double y, double midX, double midY)
+{
+    const int nx = A.nx, ny = A.ny;
+    int ii = A.bb[0], jj = A.mode == 1 ? A.bb[0] : A.bb[1];
+    if (jj > ny - 1) jj = ny - 1;
+    while (ii < nx - 1 && A.xv[ii] < x) ii++;
+    while (jj < ny - 1 && A.yu[jj] < y) jj++;
+    const int I0 = ii - 2, If = ii + 1, J0 = jj - 2, Jf = jj + 1;
+    const double dxn = x - midX, dyn = y - midY;
+    double thetaNode = asin(dyn / sqrt(dxn * dxn + dyn * dyn));
+    if (x < midX) thetaNode = M_PI - thetaNode;
+    const bool wrap = thetaNode > M_PI * 5 / 4 || thetaNode < -M_PI / 4;
+    if (wrap && x > midX) thetaNode += 2 * M_PI;
+    double lo = -10, hi = 10;
+    int loID = -1, hiID = -1;
+    for (int i = I0; i <= If; i++)
+        for (int j = J0; j <= Jf; j++) {
+            if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
+            const int ip = j * nx + i;
+            if (A.ghostP[ip] <= 0) continue;
+            const double bxp = A.bipX[ip], byp = A.bipY[ip], ex = bxp - midX, ey = byp - midY;
+            double theta = asin(ey / sqrt(ex * ex + ey * ey));
+            if (bxp < midX) theta = M_PI - theta;
+            if (wrap && bxp > midX) theta += 2 * M_PI;
+            if (theta > thetaNode && theta < hi) {
+                hi = theta;
+                hiID = ip;
+            }
+            if (theta < thetaNode && theta > lo) {
+                lo = theta;
+                loID = ip;
+            }
+        }
+    if (loID < 0 || hiID < 0) return nan("");
+    return A.biP[loID] + (A.biP[hiID] - A.biP[loID]) * (thetaNode - lo) / (hi - lo);
+}
+
+// du/dn (v = 0) or dv/dn (v = 1) at the point
+__device__ static double surface_dvel(const SurfaceArgs &A, int v, double x, double y, double midX, double midY)
+{
+    const int nx = A.nx, ny = A.ny, nU = (nx - 1) * ny;
+    const double *xc = v ? A.xv : A.xu, *yc = v ? A.yv : A.yu;
+    const int nxc = v ? nx : nx - 1, nyc = v ? ny - 1 : ny;
+    int ii = A.bb[0], jj = A.bb[1];
+    const double rise = y - midY, run = x - midX, radius = sqrt(rise * rise + run * run);
+    const double dn = A.midH * sqrt(2.0), ipx = x + dn / radius * run, ipy = y + dn / radius * rise;
+    while (ii < nxc - 1 && xc[ii] < ipx) ii++;
+    while (jj < nyc - 1 && yc[jj] < ipy) jj++;
+    if (ii < 1) ii = 1;
+    if (jj < 1) jj = 1;
+    const double x1 = xc[ii - 1], x2 = xc[ii], y3 = yc[jj], y1 = yc[jj - 1];
+    int row = nx - 1, base = 0;
+    if (v) {
+        row = A.mode == 1 ? nx - 1 : nx;  // the reference's v reads use the u row stride
+        base = A.mode == 1 ? ny * (nx - 1) : nU;
+    }
+    const double q3 = A.u[jj * row + (ii - 1) + base], q4 = A.u[jj * row + ii + base];
+    const double q1 = A.u[(jj - 1) * row + (ii - 1) + base], q2 = A.u[(jj - 1) * row + ii + base];
+    const double topleft = (x2 - ipx) * (y1 - ipy) / (x2 - x1) / (y1 - y3) * q3;
+    const double topright = (ipx - x1) * (y1 - ipy) / (x2 - x1) / (y1 - y3) * q4;
+    const double botleft = (x2 - ipx) * (ipy - y3) / (x2 - x1) / (y1 - y3) * q1;
+    const double botright = (ipx - x1) * (ipy - y3) / (x2 - x1) / (y1 - y3) * q2;
+    const double ipu = botleft + botright + topleft + topright;
+    return (ipu - (v ? A.vB[0] : A.uB[0])) / dn;
+}
+
+__global__ void __launch_bounds__(256) k_surface_force(SurfaceArgs A)
+{
+    const double midX = A.motion ? A.motion[0] : A.midX, midY = A.motion ? A.motion[1] : A.midY;
+    const int n = A.n;
+    const double ax = A.bx[0] - A.bx[1], ay = A.by[0] - A.by[1], area = sqrt(ax * ax + ay * ay);
+    double *pr = A.surf, *du = A.surf + n, *dv = A.surf + 2 * n;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double x = A.bx[k], y = A.by[k];
+        pr[k] = surface_pressure(A, x, y, midX, midY);
+        du[k] = surface_dvel(A, 0, x, y, midX, midY);
+        dv[k] = surface_dvel(A, 1, x, y, midX, midY);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double fx = 0, fy = 0;
+    for (int k = 0; k < n; ++k) {
+        const double ey = A.by[k] - midY, ex = A.bx[k] - midX, h = sqrt(ey * ey + ex * ex);
+        const double n1 = ex / h, n2 = ey / h, mu = A.nu;
+        const double tau_x = mu * ((1 - n1 * n1) * du[k] + (-n1 * n2) * dv[k]);
+        const double tau_y = mu * ((-n1 * n2) * du[k] + (1 - n2 * n2) * dv[k]);
+        fx += area * tau_x - area * n1 * pr[k];
+        fy += area * tau_y - area * n2 * pr[k];
+    }
+    A.surf[3 * n] = fx;
+    A.surf[3 * n + 1] = fy;
+    if (A.forceOut) {
+        A.forceOut[0] = fx;
+        A.forceOut[1] = fy;
+    }
+}
+
+void launch_surface_force(Context &c, int mode, bool to_step)
+{
+    if (mode != 1 && mode != 2) throw InputError("surface force mode must be 1 (as the reference) or 2 (corrected)");
+    if (c.body.total < 2) throw InputError("the surface force needs at least two body points");
+    IbHost &H = hostside(c);
+    IbArrays &b = c.ib;
+    SurfaceArgs A{c.body.total, c.g.nx, c.g.ny, mode, b.bx, b.by, b.uB, b.vB, c.u, b.biP, b.bipX, b.bipY,
+                  b.ghostP, H.bb, c.xu, c.yu, c.xv, c.yv, H.moving ? b.motion : nullptr, c.ib_midX, c.ib_midY,
+                  c.P.nu, c.P.midH, b.surf, to_step ? b.forceOut : nullptr};
+    k_surface_force<<<1, kBlock, 0, c.stream>>>(A);
+    CUIBM_TRY(cudaGetLastError());
+}
+
 void launch_force(Context &c)
 {
+    if (c.force_method) {
+        launch_surface_force(c, c.force_method, true);
+        return;
+    }
     IbHost &H = hostside(c);
     k_force<<<64, kBlock, 0, c.stream>>>(c.g.nx, c.g.ny, H.bb, c.u, c.uold, c.p, c.ib.ghostUV, c.P.nu, c.dx, c.dy,
                                          c.P.dt, c.ib.forcePart, H.force_arrive, c.ib.forceOut);

@@ -158,6 +158,7 @@ struct IbArrays {
     // force partial sums
     double *forcePart;
     double *forceOut;  // [fx, fy]
+    double *surf;      // surface force: pressure, du/dn, dv/dn per body point, then Fx, Fy
     double *motion;    // kMotionLen: [midX, midY, centerVelocityU, centerVelocityV, midX0, midY0,
                        //  U0, V0, SCtol, sub-iterations done, continue flag, spare]
 };
@@ -199,6 +200,7 @@ struct Context {
     bool ib_dirty = false;
     int ib_slot = -1;                   // host-side IB bookkeeping of this context
     double ib_midX = 0, ib_midY = 0;    // body centre used by the tagging
+    int force_method = 0;  // the step's force: 0 control volume, 1/2 surface integral (mode)
     double cfl_max = 0;
     double forceX = 0, forceY = 0;
 
@@ -319,6 +321,9 @@ void launch_ib_after_poisson(Context &c);    // hybrid p, weight p, ghost p
 void launch_ib_after_projection(Context &c); // ghost u, inside
 void launch_ib_robin_inside(Context &c);     // Robin, inside (embedded rhs1)
 void launch_force(Context &c);
+// the surface-integral force (luo_base::luoForce); mode 1 as the reference wrote it,
+// mode 2 with its two index corrections; to_step: also the step's force (forceOut)
+void launch_surface_force(Context &c, int mode, bool to_step);
 void launch_body_motion(Context &c, double t);
 void launch_body_pre_step(Context &c);
 bool body_moves(Context &c);

@@ -114,6 +114,9 @@ enum {
     CUIBM_F_BODY_MOTION,     /* D 12: body centre x, y and centre velocity u, v; the same at the
                                 start of the step; the coupling tolerance and the sub-iterations
                                 of the last strongly coupled step (VIV: 2); 4 spare */
+    CUIBM_F_SURFACE_FORCE,   /* D 3*total_points+2: pressure, du/dn, dv/dn per body point, then Fx, Fy
+                                (written by CUIBM_OP_SURFACE_FORCE*, or each step with the option
+                                "force_method" 1 or 2) */
     CUIBM_F_COUNT
 };
 
@@ -142,6 +145,9 @@ enum {
     CUIBM_OP_ROBIN_BOUNDARY,   /* convective outflow update of the x+ boundary */
     CUIBM_OP_FORCE,            /* control-volume force on body 0 */
     CUIBM_OP_CFL,              /* CFL field */
+    CUIBM_OP_SURFACE_FORCE,    /* surface-integral force on body 0 (luo_base::luoForce, unused by the
+                                  reference's step) into CUIBM_F_SURFACE_FORCE, as the reference wrote it */
+    CUIBM_OP_SURFACE_FORCE_CORRECTED, /* the same with its two index slips corrected */
     CUIBM_OP_COUNT
 };
 
@@ -178,7 +184,10 @@ int cuibm_get_timer(cuibm_ctx *ctx, const char *name, double *ms, int *count);
  * (1: cuibm_step waits and checks the solves' status; 0: it only enqueues the
  * steps on the context's stream and a later cuibm_step(ctx, 0) checks),
  * "trace_solve" (1: record per-barrier timestamps in CUIBM_F_SOLVE_TRACE),
- * "write_output" (0: no files). */
+ * "write_output" (0: no files), "force_method" (the step's body force, which the
+ * forces file, cuibm_get_forces and the flow-induced motion use: 0 the control
+ * volume of luo_base::calculateForce, as the reference; 1 the surface integral of
+ * luo_base::luoForce as the reference wrote it; 2 that integral corrected). */
 int cuibm_set_option(cuibm_ctx *ctx, const char *key, double value);
 
 /* Time one kernel of the step on the context's stream with CUDA events: reps

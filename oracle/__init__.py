@@ -585,6 +585,23 @@ def force(u, uold, p, T, nu, g, dt, bb):
     return fx.value, fy.value
 
 
+def surface_force(mode, bx, by, uB0, vB0, u, bip, bip_x, bip_y, ghostTagsP, xu, yu, xv, yv, bb, nx, ny, midX,
+                  midY, nu, mid_h):
+    """The surface-integral force (or_surfaceForce): (terms [pressure, du/dn, dv/dn per
+    point], Fx, Fy); mode 1 as luo_base::luoForce is written, 2 corrected."""
+    n = len(bx)
+    terms = np.zeros(3 * n)
+    fx, fy = ctypes.c_double(), ctypes.c_double()
+    i0, j0 = int(bb[0]), int(bb[1])
+    _sig("or_surfaceForce", INT, _dp, _dp, INT, D, D, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp, INT, INT, INT,
+         INT, D, D, D, D, _dp, _dp, _dp)(
+        int(mode), _d(f64(bx)), _d(f64(by)), n, float(uB0), float(vB0), _d(f64(u)), _d(f64(bip)), _d(f64(bip_x)),
+        _d(f64(bip_y)), _i(np.ascontiguousarray(ghostTagsP, np.int32)), _d(f64(xu)), _d(f64(yu)), _d(f64(xv)),
+        _d(f64(yv)), i0, j0, int(nx), int(ny), float(midX), float(midY), float(nu), float(mid_h), _d(terms),
+        ctypes.byref(fx), ctypes.byref(fy))
+    return terms, fx.value, fy.value
+
+
 def bounding_box(x, y, g, scale):
     a = [ctypes.c_int() for _ in range(4)]
     _sig("or_bounding_box", INT, _dp, _dp, _dp, _dp, D, _ip, _ip, _ip, _ip)(

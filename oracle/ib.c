@@ -13,6 +13,8 @@
  * or_setInsideVelocity luo_base/kernels/intermediateVelocity.cu setInsideVelocity
  * or_updateRobinBoundary FadlunModified/kernels/intermediateVelocity.cu updateBoundaryX/Y
  * or_calculateForce   luo_base/calculateForce.cu:21-74 with FadlunModified/kernels/calculateForce.cu
+ * or_surfaceForce     luo_base/calculateForce.cu:76-98 (luoForce) with luo_base/kernels/calculateForce.cu
+ *                     force_pressure :12-91, force_velocity_x :93-140, force_velocity_y :142-189, force :191-212
  *
  * Race semantics: threads run one after another in global-index order (write
  * conflicts between neighbouring tagged nodes resolve as "last thread wins");
@@ -743,4 +745,98 @@ void or_calculateForce(const double *u, const double *uold, const double *p, con
                ((u[Iv] * dx[I + i] - uold[Iv] * dx[I + i]) / dt * 0.5 * (dy[J + j] + dy[J - 1 + j]));
     }
     *fy = syx + syy + syu;
+}
+
+/* angle of (px,py) about the centre, continuous over the body as the reference makes
+ * it: pi - asin on the left half, +2 pi on the right half when the point the search
+ * is about lies outside (-pi/4, 5 pi/4) */
+static double surface_angle(double px, double py, double midX, double midY)
+{
+    double t = asin((py - midY) / sqrt((px - midX) * (px - midX) + (py - midY) * (py - midY)));
+    if (px < midX) t = M_PI - t;
+    return t;
+}
+
+/* The surface-integral force (dead code in the reference's step).  mode 1 follows
+ * luoForce as written: the pressure search starts its j index at startI (luoForce
+ * passes B.startI_r for both starts) and force_velocity_y reads v with the u row
+ * stride nx-1.  mode 2 uses startJ and the v stride nx.  The searches stop at the
+ * ends of the coordinate arrays; a point without an intercept on one side gets a
+ * NaN pressure (the reference reads an unset index there).  terms: pressure, du/dn,
+ * dv/dn per point (3n); forces summed in point order. */
+void or_surfaceForce(int mode, const double *bx, const double *by, int n, double uB0, double vB0, const double *u,
+                     const double *bip, const double *bip_x, const double *bip_y, const int *ghostTagsP,
+                     const double *xu, const double *yu, const double *xv, const double *yv, int startI,
+                     int startJ, int nx, int ny, double midX, double midY, double nu, double mid_h, double *terms,
+                     double *fx, double *fy)
+{
+    const int nU = (nx - 1) * ny;
+    double *P = terms, *DU = terms + n, *DV = terms + 2 * n;
+    for (int k = 0; k < n; k++) {
+        /* pressure: nearest intercept angles above and below in the 4x4 window */
+        int ii = startI, jj = mode == 1 ? startI : startJ;
+        if (jj > ny - 1) jj = ny - 1;
+        while (ii < nx - 1 && xv[ii] < bx[k]) ii++;
+        while (jj < ny - 1 && yu[jj] < by[k]) jj++;
+        double tn = surface_angle(bx[k], by[k], midX, midY);
+        int wrap = tn > M_PI * 5 / 4 || tn < -M_PI / 4;
+        if (wrap && bx[k] > midX) tn += 2 * M_PI;
+        double lo = -10, hi = 10;
+        int lo_id = -1, hi_id = -1;
+        for (int i = ii - 2; i <= ii + 1; i++)
+            for (int j = jj - 2; j <= jj + 1; j++) {
+                if (i < 0 || i >= nx || j < 0 || j >= ny) continue;
+                int ip = j * nx + i;
+                if (ghostTagsP[ip] <= 0) continue;
+                double t = surface_angle(bip_x[ip], bip_y[ip], midX, midY);
+                if (wrap && bip_x[ip] > midX) t += 2 * M_PI;
+                if (t > tn && t < hi) {
+                    hi = t;
+                    hi_id = ip;
+                }
+                if (t < tn && t > lo) {
+                    lo = t;
+                    lo_id = ip;
+                }
+            }
+        P[k] = (lo_id < 0 || hi_id < 0) ? NAN : bip[lo_id] + (bip[hi_id] - bip[lo_id]) * (tn - lo) / (hi - lo);
+        /* normal derivatives from the bilinear value sqrt(2) mid_h out along the radius */
+        double rise = by[k] - midY, run = bx[k] - midX, radius = sqrt(rise * rise + run * run);
+        double dn = mid_h * sqrt(2.0), ex = bx[k] + dn / radius * run, ey = by[k] + dn / radius * rise;
+        for (int c = 0; c < 2; c++) {
+            const double *xc = c ? xv : xu, *yc = c ? yv : yu;
+            int nxc = c ? nx : nx - 1, nyc = c ? ny - 1 : ny;
+            int a = startI, b = startJ;
+            while (a < nxc - 1 && xc[a] < ex) a++;
+            while (b < nyc - 1 && yc[b] < ey) b++;
+            if (a < 1) a = 1;
+            if (b < 1) b = 1;
+            int stride = nx - 1, off = 0;
+            if (c) {
+                stride = mode == 1 ? nx - 1 : nx;
+                off = mode == 1 ? ny * (nx - 1) : nU;
+            }
+            double x1 = xc[a - 1], x2 = xc[a], y1 = yc[b - 1], y3 = yc[b];
+            double q1 = u[(b - 1) * stride + a - 1 + off], q2 = u[(b - 1) * stride + a + off];
+            double q3 = u[b * stride + a - 1 + off], q4 = u[b * stride + a + off];
+            double tl = (x2 - ex) * (y1 - ey) / (x2 - x1) / (y1 - y3) * q3;
+            double tr = (ex - x1) * (y1 - ey) / (x2 - x1) / (y1 - y3) * q4;
+            double bl = (x2 - ex) * (ey - y3) / (x2 - x1) / (y1 - y3) * q1;
+            double br = (ex - x1) * (ey - y3) / (x2 - x1) / (y1 - y3) * q2;
+            double val = bl + br + tl + tr;
+            (c ? DV : DU)[k] = (val - (c ? vB0 : uB0)) / dn;
+        }
+    }
+    double area = sqrt((bx[0] - bx[1]) * (bx[0] - bx[1]) + (by[0] - by[1]) * (by[0] - by[1]));
+    double sx = 0, sy = 0;
+    for (int k = 0; k < n; k++) {
+        double h = sqrt((by[k] - midY) * (by[k] - midY) + (bx[k] - midX) * (bx[k] - midX));
+        double n1 = (bx[k] - midX) / h, n2 = (by[k] - midY) / h;
+        double tx = nu * ((1 - n1 * n1) * DU[k] + (-n1 * n2) * DV[k]);
+        double ty = nu * ((-n1 * n2) * DU[k] + (1 - n2 * n2) * DV[k]);
+        sx += area * tx - area * n1 * P[k];
+        sy += area * ty - area * n2 * P[k];
+    }
+    *fx = sx;
+    *fy = sy;
 }

@@ -114,6 +114,11 @@ void or_updateRobinBoundary(const double *u, double *xp, const double *dx, doubl
 void or_calculateForce(const double *u, const double *uold, const double *p, const int *ghostTagsUV, double nu,
                        const double *dx, const double *dy, double dt, int nx, int ny, int I, int J, int ncx,
                        int ncy, double *fx, double *fy);
+void or_surfaceForce(int mode, const double *bx, const double *by, int n, double uB0, double vB0, const double *u,
+                     const double *bip, const double *bip_x, const double *bip_y, const int *ghostTagsP,
+                     const double *xu, const double *yu, const double *xv, const double *yv, int startI,
+                     int startJ, int nx, int ny, double midX, double midY, double nu, double mid_h, double *terms,
+                     double *fx, double *fy);
 
 /* ---- fadlun.c : FadlunModified kernels (modified Fadlun method) ---- */
 void or_fadlun_lhs1_coo(int *row, int *col, double *val, int nnz, const int *hyb, const int *hyb2, const int *ghost,

@@ -39,6 +39,7 @@ thread_local ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
 #include "solvers/NavierStokes/luo_base/kernels/intermediateVelocity.h"
 #include "solvers/NavierStokes/luo_base/kernels/projectVelocity.h"
 #include "solvers/NavierStokes/luo_base/kernels/structure.h"
+#include "solvers/NavierStokes/luo_base/kernels/calculateForce.h"
 #include "solvers/NavierStokes/luoIBM/kernels/LHS1.h"
 #include "solvers/NavierStokes/luoIBM/kernels/LHS2.h"
 #include "solvers/NavierStokes/luoIBM/kernels/intermediatePressure.h"
@@ -439,6 +440,41 @@ void ref_calculateForce(double *u, double *uold, double *p, int *ghostTagsUV, do
     for (double v : FyY) syy += v;
     for (double v : FyU) syu += v;
     *fy = syx + syy + syu;
+}
+
+// luo_base::luoForce (luo_base/calculateForce.cu:76-98, not called by the reference's
+// step): its four kernels on a grid over the body points, with its arguments as
+// written (the pressure kernel gets startI for both starts), forces summed serially
+// (thrust::reduce on the GPU).  terms: pressure, du/dn, dv/dn per point.
+void ref_luoForce(double *bip, double *bip_x, double *bip_y, double *bx, double *by, double *xu, double *yu,
+                  double *xv, double *yv, int *ghostTagsP, double *u, double *uB, double *vB, int startI, int startJ,
+                  int ncx, int ncy, int totalPoints, int nx, int ny, double midX, double midY, double nu,
+                  double mid_h, double *terms, double *fx, double *fy)
+{
+    std::vector<double> fX(totalPoints), fY(totalPoints);
+    double *pr = terms, *du = terms + totalPoints, *dv = terms + 2 * totalPoints;
+    int sI = startI, sJ = startJ;
+    int g = grid_for(totalPoints);
+    launch(g, BS, [&] {
+        kernels::force_pressure(pr, bip, bip_x, bip_y, bx, by, xv, yu, ghostTagsP, &sI, &sI, ncx, ncy, totalPoints,
+                                nx, ny, midX, midY);
+    });
+    launch(g, BS, [&] {
+        kernels::force_velocity_x(du, uB, u, bx, by, xu, yu, &sI, &sJ, ncx, ncy, totalPoints, nx, ny, midX, midY,
+                                  mid_h);
+    });
+    launch(g, BS, [&] {
+        kernels::force_velocity_y(dv, vB, u, bx, by, xv, yv, &sI, &sJ, ncx, ncy, totalPoints, nx, ny, midX, midY,
+                                  mid_h);
+    });
+    launch(g, BS, [&] {
+        kernels::force(fX.data(), fY.data(), pr, du, dv, bx, by, totalPoints, midX, midY, nu);
+    });
+    double sx = 0, sy = 0;
+    for (double v : fX) sx += v;
+    for (double v : fY) sy += v;
+    *fx = sx;
+    *fy = sy;
 }
 
 // luo_base::set_movement's update_body_viv (the reference grid also writes index totalPoints,

@@ -560,12 +560,61 @@ def iter_case(K, IO, name, folder, rng, nu, dt, uB0=0.25, vB0=-0.15, uBk=0.2, vB
         nx, ny, (gU > 0).sum(), (hU > 0).sum(), (gP > 0).sum(), (hP > 0).sum()))
 
 
+def surface_case(K, IO, name, folder, ib_name, nu):
+    """luo_base::luoForce, the surface-integral force the reference's step leaves
+    unused, on the state of an external-method fixture: its tags, body-intercept
+    pressures and ghost-filled velocity, with the domain's mid_h."""
+    nx, ny, h = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+    IO.ref_parse_domain(os.path.join(folder, "domain.json").encode(), ctypes.byref(nx), ctypes.byref(ny),
+                        ctypes.byref(h))
+    z = dict(np.load(os.path.join(HERE, ib_name + ".npz")))
+    assert (nx.value, ny.value) == (int(z["nx"]), int(z["ny"]))
+    n = len(z["bx"])
+    i0, j0, ncx, ncy = (int(v) for v in z["bb"])
+    args = [z["body_intercept_p"], z["tag_body_intercept_p_x"], z["tag_body_intercept_p_y"], z["bx"], z["by"],
+            z["grid_xu"], z["grid_yu"], z["grid_xv"], z["grid_yv"]]
+    args = [np.ascontiguousarray(a, np.float64) for a in args]
+    gP = np.ascontiguousarray(z["tag_ghostTagsP"], np.int32)
+    u = np.ascontiguousarray(z["u_ghost"], np.float64)
+    uB, vB = np.ascontiguousarray(z["uB"]), np.ascontiguousarray(z["vB"])
+    # the reference reads an unset index where a point has no intercept on one side:
+    # only cases where every point has both are run through it
+    sys.path.insert(0, ROOT)
+    import oracle
+    t0, _, _ = oracle.surface_force(1, z["bx"], z["by"], float(uB[0]), float(vB[0]), u, z["body_intercept_p"],
+                                    z["tag_body_intercept_p_x"], z["tag_body_intercept_p_y"], gP, z["grid_xu"],
+                                    z["grid_yu"], z["grid_xv"], z["grid_yv"], (i0, j0, ncx, ncy), nx.value, ny.value,
+                                    float(z["midX"]), float(z["midY"]), nu, h.value)
+    assert np.all(np.isfinite(t0[:n])), "a body point without intercepts on both sides"
+    terms = np.zeros(3 * n)
+    fx, fy = ctypes.c_double(), ctypes.c_double()
+    K.ref_luoForce.argtypes = [_dp] * 9 + [_ip, _dp, _dp, _dp] + [ctypes.c_int] * 7 + [ctypes.c_double] * 4 + \
+        [_dp, _dp, _dp]
+    K.ref_luoForce(*(d(a) for a in args), i(gP), d(u), d(uB), d(vB), i0, j0, ncx, ncy, n, nx.value, ny.value,
+                   float(z["midX"]), float(z["midY"]), nu, h.value, d(terms), ctypes.byref(fx), ctypes.byref(fy))
+    out = {"ib_fixture": np.array(ib_name), "mid_h": np.float64(h.value), "nu": np.float64(nu), "terms": terms,
+           "force": np.array([fx.value, fy.value])}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "F = (%.6e, %.6e)" % (fx.value, fy.value))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
-    ap.add_argument("--only", default=None, help="generate one group: fadlun, iter")
+    ap.add_argument("--only", default=None, help="generate one group: fadlun, iter, surface")
     a = ap.parse_args()
     K, IO = ref_libs(a.ref)
+    if a.only == "surface":
+        with tempfile.TemporaryDirectory() as tmp:
+            # the case folders of ib_circle48 and ib_circle101
+            f = os.path.join(tmp, "ib1")
+            cases.cylinder(f, h=0.05, ratio=1.1, extent=2.0, core=0.6, points=48, nu=0.02, dt=0.01, nt=1)
+            surface_case(K, IO, "surface_circle48", f, "ib_circle48", nu=0.02)
+            f = os.path.join(tmp, "ib2")
+            cases.cylinder(f, h=0.025, ratio=1.08, extent=2.5, core=0.7, points=101, nu=0.02, dt=0.005, nt=1,
+                           radius=0.43)
+            surface_case(K, IO, "surface_circle101", f, "ib_circle101", nu=0.02)
+        return
     if a.only == "fadlun":
         with tempfile.TemporaryDirectory() as tmp:
             rng = np.random.default_rng(20261204)
