@@ -52,7 +52,7 @@ KRYLOV = os.environ.get("CUIBM_BENCH_KRYLOV", "BICGSTAB")
 PRECISION = os.environ.get("CUIBM_BENCH_PRECISION", "FP64")
 
 
-def make_case(workload, folder, tight=False, precision=None):
+def make_case(workload, folder, tight=False, precision=None, strength=None):
     from cuibm_gb300 import cases
     prec = precision or PRECISION
     prec = None if prec == "FP64" else prec
@@ -71,7 +71,7 @@ def make_case(workload, folder, tight=False, precision=None):
         # velocity solve stops after one iteration and C_D is off by about 2e-3 at step 40)
         f = cases.cylinder(folder, h=0.005, ratio=1.01, points=629, nu=1.0 / 550, dt=0.002, nt=1000000,
                            vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", vel_krylov=k, pois_krylov=k,
-                           precision=prec)
+                           precision=prec, strength=strength)
         return f, 922 * 922
     raise SystemExit("unknown workload " + workload)
 
@@ -287,16 +287,19 @@ def precision_comparison(local, warm=20, steps=20):
     the impulsive start, timed with CUDA events on the solver's stream (the working set,
     several hundred MB, is larger than L2).  C_D of both runs at the last step is
     reported beside the times; at these tolerances both are within 1e-6 of a tightly
-    solved FP64 run."""
+    solved FP64 run.  Each precision also runs with the smoothed aggregation's
+    strengthThreshold at 0.05 (the reference's CUSP default is 0)."""
     import torch
 
     import cuibm_gb300 as cb
     out = {"workload": "impulsively started cylinder Re 550, external (Luo) method, 922x922, 629 points, "
                        "dt 0.002, BiCGSTAB + diagonal / smoothed aggregation, rtol 1e-8 both",
            "steps_timed": "%d-%d" % (warm + 1, warm + steps)}
-    for prec in ("FP64", "MIXED"):
+    for prec, strength, key in (("FP64", None, "fp64"), ("MIXED", None, "mixed"),
+                                ("FP64", 0.05, "fp64_strength_0.05"), ("MIXED", 0.05, "mixed_strength_0.05")):
         with tempfile.TemporaryDirectory() as tmp:
-            folder, cells = make_case("cylinder_re550", os.path.join(tmp, "case"), precision=prec)
+            folder, cells = make_case("cylinder_re550", os.path.join(tmp, "case"), precision=prec,
+                                      strength=strength)
             s = cb.NavierStokesSolver(folder, ["-deviceNumber", str(local)])
             s.set_option("write_output", 0)
             s.initialise()
@@ -313,11 +316,15 @@ def precision_comparison(local, warm=20, steps=20):
             s.stepTime(0)  # raises if a solve failed
             ms = e0.elapsed_time(e1) / steps
             fx, _ = s.forces()
-            out[prec.lower()] = {"ms_per_step": round(ms, 4), "value": round(cells / ms / 1e3, 3), "unit": METRIC,
-                                 "iterations_last_step": list(s.iterations()), "cd_last_step": 2 * fx}
+            out[key] = {"ms_per_step": round(ms, 4), "value": round(cells / ms / 1e3, 3), "unit": METRIC,
+                        "iterations_last_step": list(s.iterations()), "cd_last_step": 2 * fx}
             s.close()
-    out["speedup_mixed_over_fp64"] = round(out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"], 3)
-    out["cd_difference"] = abs(out["fp64"]["cd_last_step"] - out["mixed"]["cd_last_step"])
+    base = out["fp64"]
+    out["speedup_mixed_over_fp64"] = round(base["ms_per_step"] / out["mixed"]["ms_per_step"], 3)
+    out["cd_difference"] = abs(base["cd_last_step"] - out["mixed"]["cd_last_step"])
+    best = out["mixed_strength_0.05"]
+    out["speedup_mixed_strength_over_fp64"] = round(base["ms_per_step"] / best["ms_per_step"], 3)
+    out["cd_difference_mixed_strength"] = abs(base["cd_last_step"] - best["cd_last_step"])
     return out
 
 

@@ -63,10 +63,10 @@ def write_case(folder, sim, flow, domain, bodies):
 
 
 def solvers(vel_pc="DIAGONAL", vel_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", pois_tol=1e-5, vel_krylov=None,
-            pois_krylov=None, vel_maxit=10000, pois_maxit=20000, precision=None):
+            pois_krylov=None, vel_maxit=10000, pois_maxit=20000, precision=None, strength=None):
     """The linearSolvers entries; precision "MIXED" runs both solves' multigrid cycles
-    (or, without one, inner solves) in FP32 under FP64 Krylov iterations (an extension
-    of the reference's schema)."""
+    (or, without one, inner solves) in FP32 under FP64 Krylov iterations, strength sets
+    the smoothed aggregation's strengthThreshold (extensions of the reference's schema)."""
     v = {"system": "velocity", "solver": "CG", "preconditioner": vel_pc, "tolerance": vel_tol,
          "maxIterations": vel_maxit}
     p = {"system": "Poisson", "solver": "CG", "preconditioner": pois_pc, "tolerance": pois_tol,
@@ -77,6 +77,8 @@ def solvers(vel_pc="DIAGONAL", vel_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION", poi
         p["krylov"] = pois_krylov
     if precision:
         v["precision"] = p["precision"] = precision
+    if strength is not None:
+        v["strengthThreshold"] = p["strengthThreshold"] = float(strength)
     return [v, p]
 
 
@@ -97,12 +99,12 @@ def axis(direction, start, mid_h, subs):
 
 def cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000, nsave=None, lid=1.0, vel_tol=1e-8, pois_tol=1e-8,
            pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG", vel_pc="DIAGONAL", vel_krylov=None, extra=None,
-           precision=None):
+           precision=None, strength=None):
     """Lid-driven cavity on [0,1]^2, uniform n x n cells, fluid at rest."""
     sim = {"type": "simulation", "dt": float(dt), "nt": int(nt), "nsave": int(nsave or nt),
            "SolverType": "NAVIER_STOKES_SOLVER",
            "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov,
-                                    precision=precision)}
+                                    precision=precision, strength=strength)}
     if extra:
         sim.update(extra)
     flow = [{"type": "flow", "nu": float(nu), "initialVelocity": [0.0, 0.0], "initialPerturbation": [0.0, 0.0],
@@ -115,11 +117,11 @@ def cavity(folder, n=64, nu=0.01, dt=0.01, nt=1000, nsave=None, lid=1.0, vel_tol
 def cylinder(folder, h=0.02, ratio=1.03, extent=15.0, core=0.6, points=157, nu=1.0 / 40, dt=0.01, nt=2000,
              nsave=None, method="LUO", vel_tol=1e-5, pois_tol=1e-5, pois_pc="SMOOTHED_AGGREGATION",
              pois_krylov=None, vel_krylov=None, vel_pc="DIAGONAL", radius=0.5, scaleCV=None, motion=None,
-             uinf=1.0, quiescent=False, precision=None, extra=None, vinf=0.0):
+             uinf=1.0, quiescent=False, precision=None, extra=None, vinf=0.0, strength=None):
     """Circle of diameter 2*radius at the origin in [-extent, extent]^2."""
     sim = {"type": "simulation", "dt": float(dt), "nt": int(nt), "nsave": int(nsave or nt), "SolverType": method,
            "linearSolvers": solvers(vel_pc, vel_tol, pois_pc, pois_tol, vel_krylov, pois_krylov,
-                                    precision=precision)}
+                                    precision=precision, strength=strength)}
     if extra:
         sim.update(extra)
     if scaleCV is not None:

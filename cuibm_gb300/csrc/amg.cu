@@ -3,7 +3,8 @@
 // "preconditioner: SMOOTHED_AGGREGATION", src/preconditioner.h:84-113).
 //
 // Setup (host, once per operator):
-//   strength   all off-diagonal entries are strong (CUSP's default theta = 0)
+//   strength   |a_ij| >= theta sqrt(|a_ii a_jj|), theta from strengthThreshold (default 0,
+//              CUSP's: every off-diagonal entry is strong)
 //   aggregates standard three-phase greedy aggregation over the matrix graph
 //   tentative  T: piecewise-constant prolongator, columns normalised
 //   smoothing  P = (I - w D^-1 A) T,  w = 4 / (3 rho(D^-1 A)), rho by power iteration
@@ -121,13 +122,50 @@ static double rho_dinv_a(const HostCsr &A, const std::vector<double> &d)
     return lam;
 }
 
-// three-phase greedy aggregation; returns aggregate id per node and the count
+// The strength graph for theta > 0: i - j when |a_ij| >= theta sqrt(|a_ii a_jj|) or
+// |a_ji| >= theta sqrt(|a_ii a_jj|) (symmetric), off-diagonal; a link carries row i's
+// |a_ij| where row i has the entry (phase 2 of the aggregation picks the strongest).
+static HostCsr strength_graph(const HostCsr &A, const std::vector<double> &d, double theta)
+{
+    std::vector<std::vector<std::pair<int, double>>> adj(A.n);
+    for (int i = 0; i < A.n; ++i)
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+            const int j = A.col[k];
+            const double a = std::fabs(A.val[k]);
+            if (j == i || A.val[k] == 0) continue;
+            if (a < theta * std::sqrt(std::fabs(d[i] * d[j]))) continue;
+            adj[i].push_back({j, a});
+            adj[j].push_back({i, -a});  // the reverse link, used where row j lacks the entry
+        }
+    HostCsr S;
+    S.n = S.m = A.n;
+    S.ptr.assign(A.n + 1, 0);
+    for (int i = 0; i < A.n; ++i) {
+        auto &v = adj[i];
+        std::sort(v.begin(), v.end(), [](const std::pair<int, double> &x, const std::pair<int, double> &y) {
+            return x.first != y.first ? x.first < y.first : x.second > y.second;  // own entry first
+        });
+        int last = -1;
+        for (auto &e : v) {
+            if (e.first == last) continue;
+            S.col.push_back(e.first);
+            S.val.push_back(std::fabs(e.second));
+            last = e.first;
+        }
+        S.ptr[i + 1] = (int)S.col.size();
+    }
+    return S;
+}
+
+// three-phase greedy aggregation over the strength graph A (off-diagonal links);
+// returns aggregate id per node and the count
 static int aggregate(const HostCsr &A, std::vector<int> &agg)
 {
     const int n = A.n;
     agg.assign(n, -1);
     int na = 0;
     // phase 1: a node whose neighbours are all free seeds an aggregate with them
+    // (a node without strong links becomes an aggregate of its own)
     for (int i = 0; i < n; ++i) {
         if (agg[i] >= 0) continue;
         bool free_ = true;
@@ -268,7 +306,8 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
         double rho = rho_dinv_a(Al, d);
         L->omega = 4.0 / (3.0 * rho);
         std::vector<int> agg;
-        int na = aggregate(Al, agg);
+        // theta = 0: every nonzero entry of the level's matrix is a link
+        int na = S.strength > 0 ? aggregate(strength_graph(Al, d, S.strength), agg) : aggregate(Al, agg);
         std::vector<int> size(na, 0);
         for (int a : agg) size[a]++;
         HostCsr T;

@@ -315,12 +315,14 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-__device__ __forceinline__ void trace_stamp(unsigned long long *trace)
+// entry k: the source line of the barrier's call site in the top 16 bits, the
+// global timer (ns) in the low 48
+__device__ __forceinline__ void trace_stamp(unsigned long long *trace, int site)
 {
     if (trace && blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long k = trace[0] + 1;
         if (k < (unsigned long long)kTraceLen) {
-            trace[k] = global_ns();
+            trace[k] = ((unsigned long long)(site & 0xffff) << 48) | (global_ns() & 0xffffffffffffull);
             trace[0] = k;
         }
     }
@@ -329,7 +331,7 @@ __device__ __forceinline__ void trace_stamp(unsigned long long *trace)
 // Arrivals count up from zero (reset by the host before each launch); barrier k
 // is complete when the counter reaches k * gridDim.x.  Returns false when this
 // block gave up waiting or saw another block give up.
-__device__ bool grid_sync(FusedSyncState *st, unsigned long long *trace)
+__device__ bool grid_sync(FusedSyncState *st, unsigned long long *trace, int site = __builtin_LINE())
 {
     __shared__ int ok;
     __syncthreads();
@@ -360,7 +362,7 @@ __device__ bool grid_sync(FusedSyncState *st, unsigned long long *trace)
         __threadfence();
         ok = good;
     }
-    trace_stamp(trace);
+    trace_stamp(trace, site);
     __syncthreads();
     return ok;
 }
@@ -372,7 +374,8 @@ __device__ bool grid_sync(FusedSyncState *st, unsigned long long *trace)
 // once per thread: FP64 issue is the scarce resource).  The per-thread values
 // are summed in double whatever the vectors' precision.
 template <int NV, int NO, class A, class Fn>
-__device__ bool grid_reduce(const double (&v)[NV], const A &a, int &parity, const Fn &fn, double (&o)[NO])
+__device__ bool grid_reduce(const double (&v)[NV], const A &a, int &parity, const Fn &fn, double (&o)[NO],
+                            int site = __builtin_LINE())
 {
     __shared__ double sh[NV][32];
     __shared__ double res[NO];
@@ -394,7 +397,7 @@ __device__ bool grid_reduce(const double (&v)[NV], const A &a, int &parity, cons
             if (lane == 0) part[blockIdx.x * 4 + k] = t;
         }
     }
-    if (!grid_sync(a.sync, a.trace)) return false;
+    if (!grid_sync(a.sync, a.trace, site)) return false;
     if (wid == 0) {
         double tot[NV];
 #pragma unroll
@@ -1115,14 +1118,14 @@ __global__ void __launch_bounds__(kFT, 1) k_fused_solve(Op A, const FArgs<double
     const FArgs<double> &a = *ap;
     if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
         a.trace[0] = 1;
-        a.trace[1] = global_ns();
+        a.trace[1] = global_ns() & 0xffffffffffffull;  // the start (site 0)
     }
     double res[4];
     int it = 0, status = KS_RUNNING, parity = 0;
     const bool ok = KRY == KRYLOV_CG
                         ? cg_solve<Op, PC, double>(A, a, b, x, a.ks->rtol, a.ks->maxit, parity, res, it, status)
                         : bicg_solve<Op, PC, double>(A, a, b, x, a.ks->rtol, a.ks->maxit, parity, res, it, status);
-    trace_stamp(a.trace);
+    trace_stamp(a.trace, __LINE__);
     if (threadIdx.x != 0) return;
     if (!ok) {
         atomicCAS(a.err, 0, a.which * 16 + KS_TIMEOUT);
@@ -1150,13 +1153,13 @@ __global__ void __launch_bounds__(kFT, 1) k_fused_mixed(Op64 A, Op32 A32, const 
     const FArgs<double> &a = *ap;
     if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
         a.trace[0] = 1;
-        a.trace[1] = global_ns();
+        a.trace[1] = global_ns() & 0xffffffffffffull;  // the start (site 0)
     }
     double res[4];
     int it = 0, status = KS_RUNNING, parity = 0;
     const bool ok = bicg_solve<Op64, 2, double, true, Op32>(A, a, b, x, a.ks->rtol, a.ks->maxit, parity, res, it,
                                                             status, &A32, fp);
-    trace_stamp(a.trace);
+    trace_stamp(a.trace, __LINE__);
     if (threadIdx.x != 0) return;
     if (!ok) {
         atomicCAS(a.err, 0, a.which * 16 + KS_TIMEOUT);
@@ -1186,7 +1189,7 @@ __global__ void __launch_bounds__(kFT, 1) k_fused_ir(Op64 A, Op32 A32, const FAr
     const FArgs<float> &f = *fp;
     if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
         a.trace[0] = 1;
-        a.trace[1] = global_ns();
+        a.trace[1] = global_ns() & 0xffffffffffffull;  // the start (site 0)
     }
     const double rtol = a.ks->rtol, floor_in = a.ks->inner_rtol;
     const int maxit = a.ks->maxit, maxit_in = a.ks->inner_maxit;
@@ -1239,7 +1242,7 @@ __global__ void __launch_bounds__(kFT, 1) k_fused_ir(Op64 A, Op32 A32, const FAr
         FOR_ROWS(i, a.n) x[i] = __ldcg(x + i) + (double)__ldcg(f.xin + i);
         ok = grid_sync(a.sync, a.trace);
     }
-    trace_stamp(a.trace);
+    trace_stamp(a.trace, __LINE__);
     if (threadIdx.x != 0) return;
     if (!ok) {
         atomicCAS(a.err, 0, a.which * 16 + KS_TIMEOUT);

@@ -441,6 +441,7 @@ void setup_system(Context &c, LinearSystem &S)
     S.rtol = L.tolerance;
     S.maxit = L.maxIterations;
     S.precision = L.precision;
+    S.strength = L.strength;
     if (S.precond == PC_AINV)
         throw InputError("preconditioner AINV is not implemented by this build; use DIAGONAL or SMOOTHED_AGGREGATION");
     const int n = S.n;

@@ -130,6 +130,7 @@ struct LinearSystem {
     double *p2 = nullptr, *AMp2 = nullptr, *fpartials = nullptr;
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
     int precision = PRECISION_FP64;
+    double strength = 0.0;  // smoothed aggregation's strength threshold
     void *mixed = nullptr;  // mixed precision: the float tables (fused_solve.cu)
     double *ym = nullptr, *wdef = nullptr;  // constant-mode correction of the SA cycle (Poisson):
     double Edef = 0;                        // cycle output, A^T e, e^T A e

@@ -109,8 +109,10 @@ enum {
     CUIBM_F_WORK_X,          /* D max(UV,P) operator test input  */
     CUIBM_F_WORK_Y,          /* D max(UV,P) operator test output */
     CUIBM_F_SOLVE_TRACE,     /* uint64 2*1024: per-barrier timestamps (ns) of the last persistent
-                                velocity (first 1024) and Poisson solve: [count, start, ...];
-                                written only while the option "trace_solve" is 1 */
+                                velocity (first 1024) and Poisson solve: [count, start, ...], each
+                                entry the timer's low 48 bits with the barrier's source line of
+                                fused_solve.cu in the top 16; written only while the option
+                                "trace_solve" is 1 */
     CUIBM_F_BODY_MOTION,     /* D 12: body centre x, y and centre velocity u, v; the same at the
                                 start of the step; the coupling tolerance and the sub-iterations
                                 of the last strongly coupled step (VIV: 2); 4 spare */

@@ -91,6 +91,14 @@ def test_precision_option(tmp_path):
     assert e.value.status == cb.ERR_BAD_INPUT and "precision" in str(e.value)
 
 
+def test_strength_threshold_option(tmp_path):
+    cb.case_info(cases.cavity(str(tmp_path / "s"), n=16, nt=1, strength=0.05))
+    for bad in (-0.1, 1.0):
+        with pytest.raises(cb.CuibmError) as e:
+            cb.case_info(cases.cavity(str(tmp_path / ("b%g" % bad)), n=16, nt=1, strength=bad))
+        assert e.value.status == cb.ERR_BAD_INPUT and "strengthThreshold" in str(e.value)
+
+
 def test_unknown_solver_type_falls_back_to_navier_stokes(tmp_path):
     f = cases.cavity(str(tmp_path / "c"), n=16, nt=1)
     p = os.path.join(f, "simParams.yaml")

@@ -35,7 +35,8 @@ def stretched_case(path, **kw):
            "linearSolvers": cases.solvers(kw.get("vel_pc", "DIAGONAL"), kw.get("vel_tol", 1e-12),
                                           kw.get("pois_pc", "DIAGONAL"), kw.get("pois_tol", 1e-12),
                                           kw.get("vel_krylov"), kw.get("pois_krylov"),
-                                          kw.get("vel_maxit", 10000), kw.get("pois_maxit", 20000))}
+                                          kw.get("vel_maxit", 10000), kw.get("pois_maxit", 20000),
+                                          strength=kw.get("strength"))}
     flow = [{"type": "flow", "nu": 0.02, "initialVelocity": [0.3, -0.1], "initialPerturbation": [0.1, 0.05],
              "boundaryConditions": cases.bcs((1, 0.1), (0.5, -0.2), (0.2, 0.3), (1, -0.1))}]
     h = kw.get("h", 0.1)
@@ -135,16 +136,20 @@ def test_rhs2_and_projection(solver):
 
 
 @pytest.mark.parametrize("fused", [1, 0])
-@pytest.mark.parametrize("pc,krylov", [("DIAGONAL", None), ("DIAGONAL", "CG"), ("SMOOTHED_AGGREGATION", None),
-                                       ("SMOOTHED_AGGREGATION", "CG"), ("NONE", None), ("NONE", "CG")])
-def test_solves_converge_to_direct_solution(tmp_path, pc, krylov, fused):
+@pytest.mark.parametrize("pc,krylov,strength", [("DIAGONAL", None, None), ("DIAGONAL", "CG", None),
+                                                ("SMOOTHED_AGGREGATION", None, None),
+                                                ("SMOOTHED_AGGREGATION", "CG", None),
+                                                ("SMOOTHED_AGGREGATION", None, 0.05), ("NONE", None, None),
+                                                ("NONE", "CG", None)])
+def test_solves_converge_to_direct_solution(tmp_path, pc, krylov, strength, fused):
     """Both solve paths - one persistent launch (fused) and a launch per phase -
-    for every Krylov method and preconditioner."""
+    for every Krylov method and preconditioner (smoothed aggregation also with a
+    strength threshold)."""
     # smoothed aggregation on a grid large enough for a multilevel hierarchy (the
     # coarsest level is solved densely below 1500 unknowns)
     h = 0.03 if pc == "SMOOTHED_AGGREGATION" else 0.1
     f = stretched_case(str(tmp_path / "c"), vel_pc=pc, pois_pc=pc, vel_krylov=krylov, pois_krylov=krylov,
-                       vel_tol=1e-12, pois_tol=1e-12, h=h)
+                       vel_tol=1e-12, pois_tol=1e-12, h=h, strength=strength)
     with cb.NavierStokesSolver(f) as s:
         s.set_option("write_output", 0)
         s.set_option("fused_solve", fused)
