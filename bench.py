@@ -360,7 +360,7 @@ def batch_cases(tmp, n=64, seed=0):
 def batch_comparison(local, n=64, warm=3, steps=20):
     """The batched workload run one instance after another (each with the whole GPU)
     and as one batch (cuibm_batch_*: every instance on its own stream, persistent
-    solves on a quarter of the SMs), both plain FP64, timed over the same steps with
+    solves on an eighth of the SMs), both plain FP64, timed over the same steps with
     wall-clock time around synchronised GPU work.  Aggregate Mcell-steps/s."""
     import time as _time
 

@@ -60,7 +60,7 @@ def main(argv=None):
         it = s.iterations()
         i = s.info
         print("case %s: %d x %d, SA levels %d, iterations (velocity, Poisson) %s at step %d" % (
-            a.case, i.nx, i.ny, i.amg_levels, it, i.time_step))
+            a.case, i.nx, i.ny, i.amg_levels, it, s.timeStep - 1))
         for name, t in (("velocity", tr[:1024]), ("poisson", tr[1024:])):
             if a.system not in (name, "both"):
                 continue

@@ -233,7 +233,7 @@ int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p,
  * reference, which runs one case per process (src/cuIBM.cu:61-74).  Each instance
  * is a full context (cuibm_batch_instance gives its handle for fields, forces and
  * output) with its own stream; its persistent solves use solver_blocks blocks
- * (<= 0: a quarter of the SMs), so that several instances' solves run at once
+ * (<= 0: an eighth of the SMs), so that several instances' solves run at once
  * while each instance's step stays one graph.  argc/argv are the command-line
  * overrides every instance gets (cuibm_create).  cuibm_batch_step enqueues nsteps
  * steps of every instance, interleaved step by step, then waits for all and
