@@ -357,26 +357,44 @@ def batch_cases(tmp, n=64, seed=0):
     return out
 
 
-def batch_comparison(local, n=64, warm=3, steps=20):
-    """The batched workload run one instance after another (each with the whole GPU)
-    and as one batch (cuibm_batch_*: every instance on its own stream, persistent
-    solves on an eighth of the SMs), both plain FP64, timed over the same steps with
-    wall-clock time around synchronised GPU work.  Aggregate Mcell-steps/s."""
+def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
+    """The batched workload run as one batch (cuibm_batch_*: every instance on its own
+    stream, the persistent solves' block count picked by the batch autotuner during
+    warm-up) and one instance after another (each with the whole GPU), both plain
+    FP64, timed over the same steps with wall-clock time around synchronised GPU work.
+    Aggregate Mcell-steps/s."""
     import time as _time
 
     import torch
 
     import cuibm_gb300 as cb
     out = {"workload": "%d instances (seed 0): half lid-driven cavities N 96-512, half cylinders h 0.04-0.02, "
-                       "external method, FP64" % n, "steps_timed": "%d-%d" % (warm + 1, warm + steps)}
+                       "external method, FP64" % n}
     with tempfile.TemporaryDirectory() as tmp:
         folders = batch_cases(tmp, n)
-        cells, el = 0, 0.0
-        for f in folders:  # one after another: each instance alone on the GPU
+        b = cb.Batch(folders, ["-deviceNumber", str(local)])
+        for s in b.instances:
+            s.set_option("write_output", 0)
+        b.initialise()
+        b.stepTime(warm)
+        blocks = b.autotune(tune_steps)  # advances every instance by up to 10 x tune_steps
+        warm_all = b.instances[0].timeStep
+        cells = sum(s.info.numP for s in b.instances)
+        torch.cuda.synchronize()
+        t0 = _time.perf_counter()
+        b.stepTime(steps)
+        torch.cuda.synchronize()
+        el = _time.perf_counter() - t0
+        b.close()
+        out["steps_timed"] = "%d-%d" % (warm_all + 1, warm_all + steps)
+        out["batched"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC,
+                          "solver_blocks": blocks}
+        el = 0.0
+        for f in folders:  # one after another, the same steps: each instance alone on the GPU
             s = cb.NavierStokesSolver(f, ["-deviceNumber", str(local)])
             s.set_option("write_output", 0)
             s.initialise()
-            s.stepTime(warm)
+            s.stepTime(warm_all)
             torch.cuda.synchronize()
             s.set_option("step_sync", 0)  # steps enqueued back to back, as the batch does
             t0 = _time.perf_counter()
@@ -385,21 +403,8 @@ def batch_comparison(local, n=64, warm=3, steps=20):
             el += _time.perf_counter() - t0
             s.set_option("step_sync", 1)
             s.stepTime(0)  # raises if a solve failed
-            cells += s.info.numP
             s.close()
         out["sequential"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC}
-        b = cb.Batch(folders, ["-deviceNumber", str(local)])
-        for s in b.instances:
-            s.set_option("write_output", 0)
-        b.initialise()
-        b.stepTime(warm)
-        torch.cuda.synchronize()
-        t0 = _time.perf_counter()
-        b.stepTime(steps)
-        torch.cuda.synchronize()
-        el = _time.perf_counter() - t0
-        b.close()
-        out["batched"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC}
     out["speedup_batched_over_sequential"] = round(out["sequential"]["s"] / out["batched"]["s"], 3)
     return out
 

@@ -116,6 +116,7 @@ def library():
         L.cuibm_batch_create.argtypes = [ip, ctypes.POINTER(cp), ip, ctypes.POINTER(cp), ip, ctypes.POINTER(vp)]
         L.cuibm_batch_initialise.argtypes = [vp]
         L.cuibm_batch_step.argtypes = [vp, ip]
+        L.cuibm_batch_autotune.argtypes = [vp, ip, ctypes.POINTER(ip)]
         L.cuibm_batch_size.argtypes = [vp]
         L.cuibm_batch_instance.argtypes = [vp, ip]
         L.cuibm_batch_instance.restype = vp
@@ -360,6 +361,13 @@ class Batch:
 
     def stepTime(self, nsteps=1):
         self._check(self._L.cuibm_batch_step(self._h, int(nsteps)))
+
+    def autotune(self, steps=2):
+        """Pick the persistent solves' block count by timing the batch (cuibm_batch_autotune;
+        every instance advances 10 x steps); returns the choice."""
+        nb = ctypes.c_int()
+        self._check(self._L.cuibm_batch_autotune(self._h, int(steps), ctypes.byref(nb)))
+        return nb.value
 
     def close(self):
         if getattr(self, "_h", None):

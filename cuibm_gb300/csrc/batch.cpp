@@ -13,6 +13,7 @@
 // phases would hold every instance to the slowest one's iteration count).
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -103,6 +104,50 @@ int cuibm_batch_step(cuibm_batch *b, int nsteps)
         }
     }
     return first;
+}
+
+// The best grid depends on the instances' sizes and count (fewer, larger blocks give
+// each solve more of the GPU; more, smaller shares let more solves run at once), so
+// it is measured on the batch itself.
+int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out)
+{
+    if (!b) return CUIBM_ERR_STATE;
+    if (steps <= 0) return batch_fail(b, CUIBM_ERR_BAD_INPUT, "batch: autotune needs steps > 0");
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return batch_fail(b, CUIBM_ERR_CUDA, "batch: cannot query the device");
+    std::vector<int> cand;
+    for (int d : {4, 6, 8, 12, 16}) {
+        const int nb = sms / d > 0 ? sms / d : 1;
+        if (cand.empty() || cand.back() != nb) cand.push_back(nb);
+    }
+    auto use = [&](int nb) {
+        for (size_t k = 0; k < b->ctx.size(); ++k) {
+            const int st = cuibm_set_option(b->ctx[k], "solver_blocks", nb);
+            if (st != CUIBM_OK)
+                return batch_fail(b, st, "batch: instance " + std::to_string(k) + ": " + cuibm_last_error(b->ctx[k]));
+        }
+        return (int)CUIBM_OK;
+    };
+    std::vector<double> t(cand.size(), 0.0);
+    for (int pass = 0; pass < 2; ++pass)
+        for (size_t q = 0; q < cand.size(); ++q) {
+            const size_t k = pass == 0 ? q : cand.size() - 1 - q;
+            int st = use(cand[k]);
+            if (st != CUIBM_OK) return st;
+            const auto t0 = std::chrono::steady_clock::now();
+            st = cuibm_batch_step(b, steps);  // returns after every instance finished
+            if (st != CUIBM_OK) return st;
+            t[k] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
+    size_t best = 0;
+    for (size_t k = 1; k < cand.size(); ++k)
+        if (t[k] < t[best]) best = k;
+    const int st = use(cand[best]);
+    if (st != CUIBM_OK) return st;
+    if (blocks_out) *blocks_out = cand[best];
+    return CUIBM_OK;
 }
 
 int cuibm_batch_size(const cuibm_batch *b) { return b ? (int)b->ctx.size() : 0; }

@@ -820,7 +820,14 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
     } else if (k == "step_sync") {
         c.step_sync = value != 0;
     } else if (k == "write_output") c.P.writeOutput = value != 0;
-    else if (k == "force_method") {
+    else if (k == "solver_blocks") {
+        const int nb = (int)value;
+        if (nb != value || nb < 0) return fail(h, CUIBM_ERR_BAD_INPUT, "solver_blocks must be a count >= 0");
+        c.P.solverBlocks = nb;
+        set_fused_grid(c.sys1, nb);
+        set_fused_grid(c.sys2, nb);
+        if (c.initialised && c.use_graph) CUIBM_GUARD(h, { build_step_graph(c); });
+    } else if (k == "force_method") {
         const int m = (int)value;
         if (m < 0 || m > 2 || m != value) return fail(h, CUIBM_ERR_BAD_INPUT, "force_method must be 0, 1 or 2");
         if (m && c.has_body && c.body.total < 2)

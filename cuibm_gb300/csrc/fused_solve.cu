@@ -1656,6 +1656,12 @@ double solve_bytes(const LinearSystem &S, int it)
 // block per SM unless CUIBM_FUSED_BLOCKS_PER_SM asks for more and the kernel's
 // registers allow it) and build its tables.  A mixed-precision system gets its
 // mixed kernel and the float tables.
+void set_fused_grid(LinearSystem &S, int blocks)
+{
+    if (!S.fused_fn) return;
+    S.fused_grid = blocks > 0 ? std::min(S.fused_grid_max, blocks) : S.fused_grid_default;
+}
+
 void setup_fused(Context &c, LinearSystem &S)
 {
     S.fused_fn = nullptr;
@@ -1678,13 +1684,14 @@ void setup_fused(Context &c, LinearSystem &S)
     if (!coop || per_sm < 1) return;
     int want = 1;
     if (const char *e = getenv("CUIBM_FUSED_BLOCKS_PER_SM")) want = std::max(1, atoi(e));
-    S.fused_grid = sms * std::min(per_sm, want);
-    if (c.P.solverBlocks > 0) S.fused_grid = std::min(sms * per_sm, c.P.solverBlocks);
+    S.fused_grid_default = sms * std::min(per_sm, want);
+    S.fused_grid_max = sms * per_sm;
     S.fused_fn = fn;
+    set_fused_grid(S, c.P.solverBlocks);
     const int n = S.n;
     S.p2 = c.carve<double>(n);
     S.AMp2 = c.carve<double>(n);
-    S.fpartials = c.carve<double>((size_t)2 * 4 * S.fused_grid);
+    S.fpartials = c.carve<double>((size_t)2 * 4 * S.fused_grid_max);  // room for any grid
     S.fsync = c.carve<FusedSyncState>(1);
     S.diag = c.carve<double>(n);
     CUIBM_TRY(cudaMemsetAsync(S.fsync, 0, sizeof(FusedSyncState), c.stream));

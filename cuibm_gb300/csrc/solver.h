@@ -127,6 +127,7 @@ struct LinearSystem {
     // persistent solver (fused_solve.cu); fused_fn is null where it does not apply
     void *fused_fn = nullptr;
     int fused_grid = 0, fused_threads = 512;
+    int fused_grid_default = 0, fused_grid_max = 0;  // one block per SM; every block the SMs hold
     double *p2 = nullptr, *AMp2 = nullptr, *fpartials = nullptr;
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
     int precision = PRECISION_FP64;
@@ -331,6 +332,9 @@ bool body_moves(Context &c);
 void launch_body_box(Context &c);
 void launch_step_counter(Context &c);
 void launch_coupling_next(Context &c, cudaGraphConditionalHandle h, int use_cond);  // VIV: 2 loop test
+// fused_solve.cu: the persistent solves' grid (blocks <= 0: the default); the step graph
+// must be rebuilt after
+void set_fused_grid(LinearSystem &S, int blocks);
 void initialise_body(Context &c);
 
 // io.cpp / fields.cu

@@ -186,7 +186,9 @@ int cuibm_get_timer(cuibm_ctx *ctx, const char *name, double *ms, int *count);
  * (1: cuibm_step waits and checks the solves' status; 0: it only enqueues the
  * steps on the context's stream and a later cuibm_step(ctx, 0) checks),
  * "trace_solve" (1: record per-barrier timestamps in CUIBM_F_SOLVE_TRACE),
- * "write_output" (0: no files), "force_method" (the step's body force, which the
+ * "write_output" (0: no files), "solver_blocks" (blocks of the persistent solves,
+ * 0: one per SM; as -solverBlocks, changeable after cuibm_initialise),
+ * "force_method" (the step's body force, which the
  * forces file, cuibm_get_forces and the flow-induced motion use: 0 the control
  * volume of luo_base::calculateForce, as the reference; 1 the surface integral of
  * luo_base::luoForce as the reference wrote it; 2 that integral corrected). */
@@ -244,6 +246,12 @@ int cuibm_batch_create(int n, const char *const *case_folders, int argc, const c
                        cuibm_batch **out);
 int cuibm_batch_initialise(cuibm_batch *b);
 int cuibm_batch_step(cuibm_batch *b, int nsteps);
+/* Autotuner of the batch's persistent-solve grid: times `steps` batch steps with each
+ * candidate block count (a quarter, sixth, eighth, twelfth and sixteenth of the SMs),
+ * in two passes of opposite order, and keeps the fastest for every instance
+ * (option "solver_blocks").  The timed steps are steps of the simulation (each
+ * instance advances at most 10 x steps).  *blocks_out (may be null) gets the choice. */
+int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out);
 int cuibm_batch_size(const cuibm_batch *b);
 cuibm_ctx *cuibm_batch_instance(cuibm_batch *b, int k);
 const char *cuibm_batch_error(const cuibm_batch *b);

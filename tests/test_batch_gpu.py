@@ -51,6 +51,28 @@ def test_batch_matches_instances_run_alone(tmp_path, blocks):
                 assert abs(s.forces()[0] - f[0]) < 1e-8
 
 
+def test_autotune_keeps_every_instance_exact(tmp_path):
+    folders = make(tmp_path)
+    alone = []
+    for f in folders:
+        with cb.NavierStokesSolver(f) as s:
+            s.set_option("write_output", 0)
+            s.initialise()
+            s.stepTime(12)
+            alone.append((s.get("u"), s.get("p")))
+    with cb.Batch(folders) as b:
+        for s in b.instances:
+            s.set_option("write_output", 0)
+        b.initialise()
+        nb = b.autotune(1)  # ten steps
+        assert 1 <= nb <= 38
+        assert all(s.timeStep == 10 for s in b.instances)
+        b.stepTime(2)
+        for s, (u, p) in zip(b.instances, alone):
+            assert rel_l2(s.get("u"), u) < 1e-9
+            assert rel_l2(s.get("p"), p) < 1e-8
+
+
 def test_batch_reports_the_bad_instance(tmp_path):
     folders = make(tmp_path)[:2] + [str(tmp_path / "missing")]
     with pytest.raises(cb.CuibmError) as e:
