@@ -1007,14 +1007,20 @@ __device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx
     const int nU = (nx - 1) * ny;
     double s[6] = {0, 0, 0, 0, 0, 0};
     const int stride = gridDim.x * blockDim.x;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < (ncx + 1) * (ncy + 1); idx += stride) {
-        if (idx < ncy) {
+    // the six terms' items laid end to end, one item per thread and pass: the four
+    // edge sums (a few divisions each) spread over many threads instead of riding on
+    // the first few of block 0
+    const int o1 = ncy, o3 = o1 + ncx + 1, o4 = o3 + ncy + 1, o2 = o4 + ncx, o5 = o2 + (ncx + 1) * ncy;
+    const int total = o5 + ncx * (ncy + 1);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+        if (q < o1) {
+            const int idx = q;
             const int Ip = (J + idx) * nx + I, Iu = (J + idx) * (nx - 1) + I;
             const double a = u[Iu + ncx] + u[Iu + ncx - 1], b = u[Iu - 1] + u[Iu];
             s[0] += -((p[Ip + ncx] - p[Ip]) * dy[J + idx] + (a * a / 4 - b * b / 4) * dy[J + idx] -
                       nu * ((u[Iu + ncx] - u[Iu + ncx - 1]) / dx[I + ncx] - (u[Iu] - u[Iu - 1]) / dx[I]) * dy[J + idx]);
-        }
-        if (idx <= ncx) {
+        } else if (q < o3) {
+            const int idx = q - o1;
             const int Iu = J * (nx - 1) + (I - 1 + idx), Iv = nU + (J - 1) * nx + I + idx;
             s[1] += -((0.25 * (u[Iu + ncy * (nx - 1)] + u[Iu + (ncy - 1) * (nx - 1)]) *
                            (u[Iv + ncy * nx] + u[Iv + ncy * nx - 1]) -
@@ -1024,12 +1030,8 @@ __device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx
                             ((u[Iu] - u[Iu - (nx - 1)]) / 2.0 / (dy[J] + dy[J - 1]) +
                              (u[Iv] - u[Iv - 1]) / 2.0 / (dx[I + idx] + dx[I + idx - 1])))) *
                     0.5 * (dx[I + idx] + dx[I + idx - 1]);
-        }
-        if (idx < (ncx + 1) * ncy) {
-            const int i = idx % (ncx + 1), j = idx / (ncx + 1), Iu = (J + j) * (nx - 1) + (I - 1 + i);
-            s[2] += -(gtags[Iu] == -1) * ((u[Iu] * dy[J + j] - uold[Iu] * dy[J + j]) / dt * 0.5 * (dx[I + i] + dx[I - 1 + i]));
-        }
-        if (idx <= ncy) {
+        } else if (q < o4) {
+            const int idx = q - o3;
             const int Iu = (J + idx) * (nx - 1) + (I - 1), Iv = nU + (J - 1 + idx) * nx + I;
             s[3] += -((0.25 * (u[Iu + ncx] + u[Iu + ncx - (nx - 1)]) * (u[Iv + ncx] + u[Iv + ncx - 1]) -
                        0.25 * (u[Iu] + u[Iu - (nx - 1)]) * (u[Iv] + u[Iv - 1])) -
@@ -1038,15 +1040,19 @@ __device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx
                             ((u[Iu] - u[Iu - (nx - 1)]) / 2.0 / (dy[J + idx] + dy[J - 1 + idx]) +
                              (u[Iv] - u[Iv - 1]) / 2.0 / (dx[I] + dx[I - 1])))) *
                     0.5 * (dy[J + idx] + dy[J - 1 + idx]);
-        }
-        if (idx < ncx) {
+        } else if (q < o2) {
+            const int idx = q - o4;
             const int Ip = J * nx + I + idx, Iv = nU + (J - 1) * nx + I + idx;
             const double a = u[Iv + (ncy + 1) * nx] + u[Iv + ncy * nx], b = u[Iv] + u[Iv - nx];
             s[4] += -((p[Ip + ncy * nx] - p[Ip - nx]) * dx[I + idx] + (0.25 * a * a - 0.25 * b * b) * dx[I + idx] -
                       nu * ((u[Iv + (ncy + 1) * nx] - u[Iv + ncy * nx]) * dx[I + idx] / dy[J + ncy] -
                             (u[Iv] - u[Iv - nx]) * dx[I] / dy[J - 1]));
-        }
-        if (idx < ncx * (ncy + 1)) {
+        } else if (q < o5) {
+            const int idx = q - o2;
+            const int i = idx % (ncx + 1), j = idx / (ncx + 1), Iu = (J + j) * (nx - 1) + (I - 1 + i);
+            s[2] += -(gtags[Iu] == -1) * ((u[Iu] * dy[J + j] - uold[Iu] * dy[J + j]) / dt * 0.5 * (dx[I + i] + dx[I - 1 + i]));
+        } else {
+            const int idx = q - o5;
             const int i = idx % ncx, j = idx / ncx, Iv = (J - 1 + j) * nx + (I + i) + nU;
             s[5] += -(gtags[Iv] == -1) * ((u[Iv] * dx[I + i] - uold[Iv] * dx[I + i]) / dt * 0.5 * (dy[J + j] + dy[J - 1 + j]));
         }
@@ -1072,10 +1078,18 @@ __device__ __forceinline__ void force_body(int nx, int ny, int I, int J, int ncx
     __syncthreads();
     if (!last) return;
     __threadfence();
+    // warp k sums term k over the blocks (lanes stride the blocks, then a fixed shuffle
+    // tree): the partials are read in parallel, not one dependent load after another
+    if (wid < 6) {
+        double a = 0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) a += __ldcg(part + b * 6 + wid);
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) sh[wid][0] = a;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        double t[6] = {0, 0, 0, 0, 0, 0};  // blocks in order, then the six terms
-        for (int b = 0; b < (int)gridDim.x; ++b)
-            for (int k = 0; k < 6; ++k) t[k] += __ldcg(part + b * 6 + k);
+        double t[6];
+        for (int k = 0; k < 6; ++k) t[k] = sh[k][0];
         out[0] = t[0] + t[1] + t[2];
         out[1] = t[3] + t[4] + t[5];
         if (comp)
@@ -1709,8 +1723,9 @@ void launch_body_box(Context &c)
 
 // ---- control-volume force without allocation -------------------------------------
 // The scratch of k_force (6 partial sums per block, then an arrival counter) as a
-// fixed array in the library image: kCvForceMaxBlocks blocks of 256 threads cover
-// (ncx+1)*(ncy+1) <= 262144 box nodes with one node per thread.
+// fixed array in the library image: up to kCvForceMaxBlocks blocks of 256 threads, one
+// per box node ((ncx+1)*(ncy+1) <= 262144), loop over the force's items (about two per
+// node).
 constexpr int kCvForceMaxBlocks = 1024;
 static __device__ __align__(256) double g_cvforce_scratch[6 * kCvForceMaxBlocks + 32];
 
