@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libcuibm_gb300.so")
 
 # status codes (cuibm_status)
 OK, ERR_BAD_INPUT, ERR_IO, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NAN, ERR_STATE, ERR_UNSUPPORTED = range(8)
+ASYNC = 2  # CUIBM_COPY_ASYNC: field copies enqueued on the solver's stream
 STATUS_NAMES = {0: "OK", 1: "BAD_INPUT", 2: "IO", 3: "CUDA", 4: "NOT_CONVERGED", 5: "NAN", 6: "STATE",
                 7: "UNSUPPORTED"}
 
@@ -37,7 +38,7 @@ _FIELD_NAMES = [
     "ghost_uv_index", "ghost_uv_coef", "hybrid_uv_index", "hybrid_uv_coef",
     "ghost_p_index", "ghost_p_coef", "hybrid_p_index", "hybrid_p_coef",
     "image_value_uv", "cfl", "work_x", "work_y", "solve_trace", "body_motion",
-    "surface_force",
+    "surface_force", "forces",
 ]
 FIELDS = {n: i for i, n in enumerate(_FIELD_NAMES)}
 _INT_FIELDS = {"ghost_tags_uv", "hybrid_tags_uv", "hybrid_tags_uv2", "ghost_tags_p", "hybrid_tags_p",
@@ -207,7 +208,7 @@ class NavierStokesSolver:
                  "x": nx, "dx": nx, "xu": nx - 1, "xv": nx, "y": ny, "dy": ny, "yu": ny, "yv": ny - 1,
                  "body_x": nb, "body_y": nb, "body_uB": nb, "body_vB": nb,
                  "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024,
-                 "body_motion": 12, "surface_force": 3 * nb + 2}
+                 "body_motion": 12, "surface_force": 3 * nb + 2, "forces": 2}
         if name in sizes:
             return sizes[name]
         if name in ("p", "p_old", "rhs2", "ghost_tags_p", "hybrid_tags_p", "bip_x", "bip_y", "ipp_x", "ipp_y",
@@ -232,9 +233,16 @@ class NavierStokesSolver:
             raise ValueError("%s needs %d values, got %d" % (name, self.field_size(name), a.size))
         self._check(self._L.cuibm_set_field(self._h, FIELDS[name], a.ctypes.data, a.nbytes, 0))
 
-    def get_into(self, name, ptr, nbytes, on_device=False):
-        """Copy a field into caller memory (host pointer, or device pointer when on_device)."""
-        self._check(self._L.cuibm_get_field(self._h, FIELDS[name], ctypes.c_void_p(ptr), nbytes, int(on_device)))
+    def get_into(self, name, ptr, nbytes, on_device=False, asynchronous=False):
+        """Copy a field into caller memory (host pointer, or device pointer when on_device);
+        asynchronous: enqueue on the solver's stream and return (pinned host memory)."""
+        flags = int(bool(on_device)) | (ASYNC if asynchronous else 0)
+        self._check(self._L.cuibm_get_field(self._h, FIELDS[name], ctypes.c_void_p(ptr), nbytes, flags))
+
+    def set_from(self, name, ptr, nbytes, on_device=False, asynchronous=False):
+        """Copy caller memory into a field (the counterpart of get_into)."""
+        flags = int(bool(on_device)) | (ASYNC if asynchronous else 0)
+        self._check(self._L.cuibm_set_field(self._h, FIELDS[name], ctypes.c_void_p(ptr), nbytes, flags))
 
     def forces(self):
         fx, fy = ctypes.c_double(), ctypes.c_double()

@@ -638,9 +638,9 @@ int cuibm_get_field(cuibm_ctx *h, int field, void *dst, size_t bytes, int dst_on
         if (bytes != need)
             return fail(h, CUIBM_ERR_BAD_INPUT, "field " + std::to_string(field) + " needs " + std::to_string(need) +
                                                     " bytes, got " + std::to_string(bytes));
-        CUIBM_TRY(cudaMemcpyAsync(dst, src, bytes, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                  c.stream));
-        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        CUIBM_TRY(cudaMemcpyAsync(dst, src, bytes,
+                                  (dst_on_device & 1) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c.stream));
+        if (!(dst_on_device & CUIBM_COPY_ASYNC)) CUIBM_TRY(cudaStreamSynchronize(c.stream));
     });
     return CUIBM_OK;
 }
@@ -654,9 +654,9 @@ int cuibm_set_field(cuibm_ctx *h, int field, const void *src, size_t bytes, int 
         void *dst = field_pointer(c, field, &need);
         if (!dst) return fail(h, CUIBM_ERR_BAD_INPUT, "unknown or unavailable field " + std::to_string(field));
         if (bytes != need) return fail(h, CUIBM_ERR_BAD_INPUT, "wrong byte count for field " + std::to_string(field));
-        CUIBM_TRY(cudaMemcpyAsync(dst, src, bytes, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                  c.stream));
-        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        CUIBM_TRY(cudaMemcpyAsync(dst, src, bytes,
+                                  (src_on_device & 1) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c.stream));
+        if (!(src_on_device & CUIBM_COPY_ASYNC)) CUIBM_TRY(cudaStreamSynchronize(c.stream));
         field_changed(c, field);
     });
     return CUIBM_OK;

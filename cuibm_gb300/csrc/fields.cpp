@@ -52,6 +52,7 @@ void *field_pointer(Context &c, int f, size_t *bytes)
     case CUIBM_F_BODY_VB: return ret(b.vB, nb * D);
     case CUIBM_F_BODY_MOTION: return ret(b.motion, kMotionLen * D);
     case CUIBM_F_SURFACE_FORCE: return ret(b.surf, (3 * nb + 2) * D);
+    case CUIBM_F_FORCES: return ret(b.forceOut, 2 * D);
     case CUIBM_F_GHOST_TAGS_UV: return ret(b.ghostUV, UV * I);
     case CUIBM_F_HYBRID_TAGS_UV: return ret(b.hybridUV, UV * I);
     case CUIBM_F_HYBRID_TAGS_UV2: return ret(b.hybrid2UV, UV * I);

@@ -119,6 +119,7 @@ enum {
     CUIBM_F_SURFACE_FORCE,   /* D 3*total_points+2: pressure, du/dn, dv/dn per body point, then Fx, Fy
                                 (written by CUIBM_OP_SURFACE_FORCE*, or each step with the option
                                 "force_method" 1 or 2) */
+    CUIBM_F_FORCES,          /* D 2: Fx, Fy of the last step (what cuibm_get_forces reads) */
     CUIBM_F_COUNT
 };
 
@@ -163,8 +164,12 @@ void cuibm_destroy(cuibm_ctx *ctx);
 const char *cuibm_last_error(const cuibm_ctx *ctx);
 
 int cuibm_get_info(const cuibm_ctx *ctx, cuibm_info *info);
-/* copy a field; bytes must equal the field size; *_on_device != 0 means the
- * caller's pointer is device memory of the context's GPU */
+/* copy a field; bytes must equal the field size.  Flags (*_on_device): bit 0 set
+ * means the caller's pointer is device memory of the context's GPU; bit 1 set
+ * (CUIBM_COPY_ASYNC) enqueues the copy on the context's stream after the work
+ * already there and returns without waiting (host memory should then be pinned and
+ * must stay valid until the stream has passed the copy) */
+#define CUIBM_COPY_ASYNC 2
 int cuibm_get_field(cuibm_ctx *ctx, int field, void *dst, size_t bytes, int dst_on_device);
 int cuibm_set_field(cuibm_ctx *ctx, int field, const void *src, size_t bytes, int src_on_device);
 int cuibm_get_forces(cuibm_ctx *ctx, double *fx, double *fy);

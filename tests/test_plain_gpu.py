@@ -234,3 +234,29 @@ def test_fused_and_stepwise_solves_agree(tmp_path):
     (u1, p1, it1), (u0, p0, it0) = out
     assert it1 == it0
     assert rel_l2(u1, u0) < 1e-12 and rel_l2(p1, p0) < 1e-9
+
+
+def test_asynchronous_field_copies(tmp_path):
+    """CUIBM_COPY_ASYNC: copies enqueued on the solver's stream, in order with the
+    steps, from and into pinned host memory; the forces field holds what
+    cuibm_get_forces reads."""
+    torch = pytest.importorskip("torch")
+    f = cases.cylinder(str(tmp_path / "c"), h=0.05, ratio=1.1, extent=3.0, core=0.6, points=48, nu=0.025, dt=0.01,
+                       nt=20, vel_tol=1e-12, pois_tol=1e-12)
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.initialise()
+        s.stepTime(2)
+        xp = torch.from_numpy(s.get("bc_xplus") * 1.01).pin_memory()
+        u = torch.empty(s.info.numUV, dtype=torch.float64).pin_memory()
+        fo = torch.empty(2, dtype=torch.float64).pin_memory()
+        s.set_option("step_sync", 0)
+        s.set_from("bc_xplus", xp.data_ptr(), xp.numel() * 8, asynchronous=True)
+        s.stepTime(1)
+        s.get_into("u", u.data_ptr(), u.numel() * 8, asynchronous=True)
+        s.get_into("forces", fo.data_ptr(), 16, asynchronous=True)
+        s.set_option("step_sync", 1)
+        s.stepTime(0)  # waits for the stream
+        assert np.array_equal(u.numpy(), s.get("u"))
+        assert tuple(fo.tolist()) == s.forces()
+        assert s.forces()[0] != 0
