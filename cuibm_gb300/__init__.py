@@ -342,7 +342,7 @@ class Batch:
     """Many independent cases advanced together on one GPU (cuibm_batch_*).
 
     Each instance is a full solver with its own stream; its persistent solves use
-    ``solver_blocks`` blocks (None: an eighth of the SMs) so that several instances'
+    ``solver_blocks`` blocks (None: a quarter of the SMs, two blocks per SM) so that several instances'
     solves run at once.  ``instances`` are solver objects for fields, forces and
     output; the batch owns them.
     """

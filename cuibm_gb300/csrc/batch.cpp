@@ -47,14 +47,17 @@ int cuibm_batch_create(int n, const char *const *case_folders, int argc, const c
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return batch_fail(nullptr, CUIBM_ERR_CUDA, "batch: cannot query the device");
-        // an eighth of the SMs: on the 64-instance benchmark 19 blocks of 512 threads gave
-        // 152 Mcell-steps/s against 136 with 38 blocks, 147 with 12 and 130 with 16 x 256
-        blocks = sms / 8 > 0 ? sms / 8 : 1;
+        // a quarter of the SMs, with the solves built for two blocks per SM: on the
+        // 64-instance benchmark 38 blocks gave 176 Mcell-steps/s, 19 blocks 172 and 12
+        // blocks 142 (built for one block per SM: 136, 152 and 143)
+        blocks = sms / 4 > 0 ? sms / 4 : 1;
     }
     const std::string nb = std::to_string(blocks);
     std::vector<const char *> args(argv, argv + (argc > 0 ? argc : 0));
     args.push_back("-solverBlocks");
     args.push_back(nb.c_str());
+    args.push_back("-solverPack");  // two instances' solve blocks may share an SM
+    args.push_back("2");
     cuibm_batch *b = new cuibm_batch();
     for (int k = 0; k < n; ++k) {
         cuibm_ctx *c = nullptr;
@@ -118,7 +121,7 @@ int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return batch_fail(b, CUIBM_ERR_CUDA, "batch: cannot query the device");
     std::vector<int> cand;
-    for (int d : {4, 6, 8, 12, 16}) {
+    for (int d : {2, 4, 6, 8, 12}) {
         const int nb = sms / d > 0 ? sms / d : 1;
         if (cand.empty() || cand.back() != nb) cand.push_back(nb);
     }

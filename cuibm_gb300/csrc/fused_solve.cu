@@ -1111,9 +1111,11 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
     return true;
 }
 
-template <class Op, int PC, int KRY>
-__global__ void __launch_bounds__(kFT, 1) k_fused_solve(Op A, const FArgs<double> *__restrict__ ap, const double *b,
-                                                        double *x)
+// MINB: blocks per SM the kernel is built for (2: at most 64 registers a thread, for
+// batched instances whose solves share the SMs)
+template <class Op, int PC, int KRY, int MINB = 1>
+__global__ void __launch_bounds__(kFT, MINB) k_fused_solve(Op A, const FArgs<double> *__restrict__ ap,
+                                                           const double *b, double *x)
 {
     const FArgs<double> &a = *ap;
     if (a.trace && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1346,8 +1348,15 @@ void refresh_fused_level0(Context &c, LinearSystem &S)
 }
 
 template <class Op>
-static void *pick_kernel(int precond, int krylov)
+static void *pick_kernel(int precond, int krylov, int pack)
 {
+    if (pack == 2 && (precond == PC_SMOOTHED_AGGREGATION || precond == PC_DIAGONAL)) {
+        if (krylov == KRYLOV_CG)
+            return precond == PC_SMOOTHED_AGGREGATION ? (void *)k_fused_solve<Op, 2, KRYLOV_CG, 2>
+                                                      : (void *)k_fused_solve<Op, 1, KRYLOV_CG, 2>;
+        return precond == PC_SMOOTHED_AGGREGATION ? (void *)k_fused_solve<Op, 2, KRYLOV_BICGSTAB, 2>
+                                                  : (void *)k_fused_solve<Op, 1, KRYLOV_BICGSTAB, 2>;
+    }
     if (krylov == KRYLOV_CG) {
         if (precond == PC_SMOOTHED_AGGREGATION) return (void *)k_fused_solve<Op, 2, KRYLOV_CG>;
         if (precond == PC_DIAGONAL) return (void *)k_fused_solve<Op, 1, KRYLOV_CG>;
@@ -1672,9 +1681,11 @@ void setup_fused(Context &c, LinearSystem &S)
     const bool mixed = S.precision == PRECISION_MIXED;
     void *fn;
     if (S.which == 1)
-        fn = mixed ? pick_mixed_kernel<Op1D<double>, Op1D<float>>(S) : pick_kernel<Op1D<double>>(S.precond, S.krylov);
+        fn = mixed ? pick_mixed_kernel<Op1D<double>, Op1D<float>>(S)
+                   : pick_kernel<Op1D<double>>(S.precond, S.krylov, c.P.solverPack);
     else
-        fn = mixed ? pick_mixed_kernel<Op2D<double>, Op2D<float>>(S) : pick_kernel<Op2D<double>>(S.precond, S.krylov);
+        fn = mixed ? pick_mixed_kernel<Op2D<double>, Op2D<float>>(S)
+                   : pick_kernel<Op2D<double>>(S.precond, S.krylov, c.P.solverPack);
     int dev = 0, sms = 0, coop = 0, per_sm = 0;
     CUIBM_TRY(cudaGetDevice(&dev));
     CUIBM_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -240,7 +240,8 @@ int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p,
  * reference, which runs one case per process (src/cuIBM.cu:61-74).  Each instance
  * is a full context (cuibm_batch_instance gives its handle for fields, forces and
  * output) with its own stream; its persistent solves use solver_blocks blocks
- * (<= 0: an eighth of the SMs), so that several instances' solves run at once
+ * (<= 0: a quarter of the SMs; the solves are built for two blocks per SM,
+ * -solverPack 2), so that several instances' solves run at once
  * while each instance's step stays one graph.  argc/argv are the command-line
  * overrides every instance gets (cuibm_create).  cuibm_batch_step enqueues nsteps
  * steps of every instance, interleaved step by step, then waits for all and
@@ -252,7 +253,7 @@ int cuibm_batch_create(int n, const char *const *case_folders, int argc, const c
 int cuibm_batch_initialise(cuibm_batch *b);
 int cuibm_batch_step(cuibm_batch *b, int nsteps);
 /* Autotuner of the batch's persistent-solve grid: times `steps` batch steps with each
- * candidate block count (a quarter, sixth, eighth, twelfth and sixteenth of the SMs),
+ * candidate block count (a half, quarter, sixth, eighth and twelfth of the SMs),
  * in two passes of opposite order, and keeps the fastest for every instance
  * (option "solver_blocks").  The timed steps are steps of the simulation (each
  * instance advances at most 10 x steps).  *blocks_out (may be null) gets the choice. */
