@@ -598,11 +598,38 @@ def surface_case(K, IO, name, folder, ib_name, nu):
     print("wrote", name, "F = (%.6e, %.6e)" % (fx.value, fy.value))
 
 
+def recorded_run(ref_root, name, case_dir):
+    """Outputs the reference's authors recorded for one of its validation cases
+    (validation/<case_dir>: forces_init = time, Fx, Fy for the first 1000 steps;
+    midPosition_init = step, X, Y, U, V; iterations_init = velocity and Poisson
+    iterations per step, which holds two lines per step).  The case's parameters are
+    restated in the test that uses the fixture."""
+    d = os.path.join(ref_root, "validation", case_dir)
+
+    def table(fname, skip):
+        rows = []
+        with open(os.path.join(d, fname)) as f:
+            for k, line in enumerate(f):
+                if k < skip or not line.strip():
+                    continue
+                rows.append([float(v) for v in line.replace(",", " ").split()])
+        return np.array(rows)
+
+    out = {"forces": table("forces_init", 1), "mid_position": table("midPosition_init", 1),
+           "iterations": table("iterations_init", 0)}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, {k: v.shape for k, v in out.items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/src")
-    ap.add_argument("--only", default=None, help="generate one group: fadlun, iter, surface")
+    ap.add_argument("--only", default=None, help="generate one group: fadlun, iter, surface, recorded")
     a = ap.parse_args()
+    if a.only == "recorded":  # data files of the reference tree, no build needed
+        recorded_run(os.path.dirname(os.path.abspath(a.ref)), "recorded_osc_static_external",
+                     "osc/static/external")
+        return
     K, IO = ref_libs(a.ref)
     if a.only == "surface":
         with tempfile.TemporaryDirectory() as tmp:
