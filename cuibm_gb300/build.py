@@ -18,6 +18,7 @@ SRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB = os.path.join(LIB_DIR, "libcuibm_gb300.so")
+CLI = os.path.join(LIB_DIR, "cuibm")  # the command-line program (csrc/cli.cpp) on the C ABI
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall,-Wno-unused-function",
@@ -67,12 +68,17 @@ def build(verbose=False):
     os.makedirs(OBJ_DIR, exist_ok=True)
     with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda kv: _compile(*kv), UNITS.items()))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))
+    cli_src = os.path.join(SRC, "cli.cpp")
+    if not (os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(LIB), os.path.getmtime(cli_src))):
+        cmd = [nvcc()] + COMMON + [cli_src, "-o", CLI, "-L" + LIB_DIR, "-lcuibm_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("cli build failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))
     if verbose:
         print("built", LIB)
     return LIB

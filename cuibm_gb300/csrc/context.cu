@@ -520,6 +520,7 @@ int cuibm_initialise(cuibm_ctx *h)
                 c.midPositionFile = fopen((c.P.caseFolder + "/midPosition").c_str(), mode);
             }
             write_grid_file(c);
+            write_info_file(c);
         }
         if (c.use_graph) build_step_graph(c);
         c.initialised = true;

@@ -46,6 +46,26 @@ void write_grid_file(Context &c)
     fclose(fp);
 }
 
+// io::writeInfoFile (io/io.cu:406-420): the run's summary for the post-processing
+// scripts, "--key<TAB>value" with the key right-aligned in 20 columns, numbers as an
+// ostream prints them (6 significant digits)
+void write_info_file(Context &c)
+{
+    std::string f = c.P.caseFolder + "/run.info";
+    FILE *fp = fopen(f.c_str(), "w");
+    if (!fp) throw InputError("cannot write " + f);
+    fprintf(fp, "%20s\t%d\n", "--nx", c.g.nx);
+    fprintf(fp, "%20s\t%d\n", "--ny", c.g.ny);
+    fprintf(fp, "%20s\t%d\n", "--startStep", c.P.startStep);
+    fprintf(fp, "%20s\t%d\n", "--nt", c.P.nt);
+    fprintf(fp, "%20s\t%d\n", "--nsave", c.P.nsave);
+    fprintf(fp, "%20s\t%g\n", "--dt", c.P.dt);
+    fprintf(fp, "%20s\t%d\n", "--vortlim", 15);
+    fprintf(fp, "%20s\t%s\n", "--folder", c.P.caseFolder.c_str());
+    fprintf(fp, "%20s\t%g\n", "--nu", c.P.nu);
+    fclose(fp);
+}
+
 static void write_array(const std::string &path, const std::vector<double> &v)
 {
     FILE *fp = fopen(path.c_str(), "wb");

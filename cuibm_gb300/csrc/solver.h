@@ -339,6 +339,7 @@ void initialise_body(Context &c);
 
 // io.cpp / fields.cu
 void write_grid_file(Context &c);
+void write_info_file(Context &c);  // run.info
 void write_step_output(Context &c);
 void read_restart_state(Context &c);  // restart: the state written at step startStep
 void *field_pointer(Context &c, int field, size_t *bytes);
