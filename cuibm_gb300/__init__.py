@@ -72,7 +72,7 @@ class Info(ctypes.Structure):
                [(n, ctypes.c_int) for n in ("total_points", "bb_start_i", "bb_start_j", "bb_ncx", "bb_ncy",
                                             "nnz_lhs1", "nnz_lhs2", "velocity_precond", "poisson_precond",
                                             "velocity_krylov", "poisson_krylov", "amg_levels",
-                                            "velocity_precision", "poisson_precision")]
+                                            "velocity_precision", "poisson_precision", "sa_rebuilds")]
 
 
 _lib = None

@@ -243,14 +243,36 @@ static void dense_inverse(const HostCsr &A, std::vector<double> &inv)
 void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
                        std::vector<double> &val);
 
-static DevCsr upload(Context &c, const HostCsr &H)
+// device memory of the hierarchy: the context's arena, or (a hierarchy that will be
+// rebuilt) allocations of its own, freed with it
+template <class T>
+static T *sa_alloc(Context &c, LinearSystem &S, size_t n)
+{
+    if (!S.sa_dynamic) return c.carve<T>(n);
+    void *p = nullptr;
+    CUIBM_TRY(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)));
+    S.sa_blocks.push_back(p);
+    return static_cast<T *>(p);
+}
+
+// the level objects, and the device memory of a hierarchy that has its own (the arena's
+// goes with the context)
+void free_sa_hierarchy(LinearSystem &S)
+{
+    for (SaLevel *L : S.amg) delete L;
+    S.amg.clear();
+    for (void *p : S.sa_blocks) cudaFree(p);
+    S.sa_blocks.clear();
+}
+
+static DevCsr upload(Context &c, LinearSystem &S, const HostCsr &H)
 {
     DevCsr D;
     D.n = H.n;
     D.nnz = (int)H.col.size();
-    D.ptr = c.carve<int>(H.ptr.size());
-    D.col = c.carve<int>(std::max<size_t>(1, H.col.size()));
-    D.val = c.carve<double>(std::max<size_t>(1, H.val.size()));
+    D.ptr = sa_alloc<int>(c, S, H.ptr.size());
+    D.col = sa_alloc<int>(c, S, std::max<size_t>(1, H.col.size()));
+    D.val = sa_alloc<double>(c, S, std::max<size_t>(1, H.val.size()));
     CUIBM_TRY(cudaMemcpyAsync(D.ptr, H.ptr.data(), H.ptr.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     if (!H.col.empty()) {
         CUIBM_TRY(cudaMemcpyAsync(D.col, H.col.data(), H.col.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
@@ -284,19 +306,19 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
             if (v == 0) v = 1.0;
         std::vector<double> dinv(d.size());
         for (size_t i = 0; i < d.size(); ++i) dinv[i] = 1.0 / d[i];
-        L->dinv = c.carve<double>(L->n);
+        L->dinv = sa_alloc<double>(c, S, L->n);
         keepD.push_back(dinv);
         CUIBM_TRY(cudaMemcpyAsync(L->dinv, keepD.back().data(), L->n * sizeof(double), cudaMemcpyHostToDevice,
                                   c.stream));
-        L->x = c.carve<double>(L->n);
-        L->b = c.carve<double>(L->n);
-        L->r = c.carve<double>(L->n);
-        L->t = c.carve<double>(L->n);
-        if (lev > 0) L->A = upload(c, Al);
+        L->x = sa_alloc<double>(c, S, L->n);
+        L->b = sa_alloc<double>(c, S, L->n);
+        L->r = sa_alloc<double>(c, S, L->n);
+        L->t = sa_alloc<double>(c, S, L->n);
+        if (lev > 0) L->A = upload(c, S, Al);
         if (Al.n <= kCoarse || lev == 24) {
             std::vector<double> inv;
             dense_inverse(Al, inv);
-            L->coarse_inv = c.carve<double>((size_t)Al.n * Al.n);
+            L->coarse_inv = sa_alloc<double>(c, S, (size_t)Al.n * Al.n);
             keepD.push_back(inv);
             CUIBM_TRY(cudaMemcpyAsync(L->coarse_inv, keepD.back().data(), inv.size() * sizeof(double),
                                       cudaMemcpyHostToDevice, c.stream));
@@ -345,13 +367,13 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
         keepP.push_back(P);
         keepR.push_back(R);
         keepAP.push_back(AP);
-        L->P = upload(c, keepP.back());
-        L->R = upload(c, keepR.back());
-        L->AP = upload(c, keepAP.back());
+        L->P = upload(c, S, keepP.back());
+        L->R = upload(c, S, keepR.back());
+        L->AP = upload(c, S, keepAP.back());
         {
             std::vector<double> wd(L->n);
             for (int i = 0; i < L->n; ++i) wd[i] = L->omega * dinv[i];
-            L->wd = c.carve<double>(L->n);
+            L->wd = sa_alloc<double>(c, S, L->n);
             keepD.push_back(wd);
             CUIBM_TRY(cudaMemcpyAsync(L->wd, keepD.back().data(), L->n * sizeof(double), cudaMemcpyHostToDevice,
                                       c.stream));
@@ -386,12 +408,6 @@ double sa_vcycle_bytes(const LinearSystem &S)
 }
 
 int sa_coarsest_size(const LinearSystem &S) { return S.amg.empty() ? 0 : S.amg.back()->n; }
-
-void free_sa_hierarchy(LinearSystem &S)
-{
-    for (SaLevel *L : S.amg) delete L;  // device memory belongs to the context arena
-    S.amg.clear();
-}
 
 // ---------------------------------------------------------------------------
 // V-cycle kernels

@@ -459,8 +459,21 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
             initialise_body(c);
             launch_tag_points(c);
         }
+        // a moving embedded body changes the operator's rows at every tagging: an SA
+        // hierarchy is rebuilt whenever the set of patched rows changes (the reference
+        // rebuilds its preconditioner every step, luo_iter/poisson.cu:38-45)
+        if (c.P.solverType == ST_OSC && c.has_body && body_moves(c)) {
+            for (LinearSystem *S : {&c.sys1, &c.sys2}) {
+                const LinearSolve &L = S->which == 1 ? c.P.velocity : c.P.poisson;
+                if (L.precond == PC_SMOOTHED_AGGREGATION && L.precision != PRECISION_MIXED) {
+                    S->sa_dynamic = true;
+                    c.sa_rebuild = true;
+                }
+            }
+        }
         setup_system(c, c.sys1);
         setup_system(c, c.sys2);
+        if (c.sa_rebuild) c.sys1.sa_key = c.sys2.sa_key = read_rows_key(c);
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
         const char *ev = getenv("CUIBM_GRAPH");
         c.use_graph = !(ev && ev[0] == '0');
@@ -528,6 +541,24 @@ int cuibm_initialise(cuibm_ctx *h)
     return CUIBM_OK;
 }
 
+// Between steps: a moving embedded body whose patched rows changed gets new SA
+// hierarchies, built from the current rows (and the step graph follows them).
+static void rebuild_hierarchies(Context &c)
+{
+    const unsigned long long key = read_rows_key(c);
+    bool rebuilt = false;
+    for (LinearSystem *S : {&c.sys1, &c.sys2}) {
+        if (!S->sa_dynamic || S->sa_key == key) continue;
+        free_sa_hierarchy(*S);
+        build_sa_hierarchy(c, *S);
+        refresh_fused_hierarchy(c, *S);
+        S->sa_key = key;
+        c.sa_rebuilds++;
+        rebuilt = true;
+    }
+    if (rebuilt && c.use_graph) build_step_graph(c);
+}
+
 int cuibm_step(cuibm_ctx *h, int nsteps)
 {
     if (!h || !h->c.initialised) return CUIBM_ERR_STATE;
@@ -540,6 +571,7 @@ int cuibm_step(cuibm_ctx *h, int nsteps)
             else
                 record_step(c, false);
             c.timeStep++;
+            if (c.sa_rebuild) rebuild_hierarchies(c);
         }
         if (!c.step_sync && nsteps > 0) return CUIBM_OK;  // enqueued only; checked by a later synchronising call
         int errw = 0;
@@ -624,6 +656,7 @@ int cuibm_get_info(const cuibm_ctx *h, cuibm_info *info)
     info->poisson_krylov = c.P.krylovPoisson;
     info->velocity_precision = c.P.velocity.precision;
     info->poisson_precision = c.P.poisson.precision;
+    info->sa_rebuilds = c.sa_rebuilds;
     info->amg_levels = (int)c.sys2.amg.size();
     return CUIBM_OK;
 }

@@ -243,6 +243,7 @@ void setup_embedded(Context &c)
     E.cap1 = P.cap_v;
     E.cap2 = P.cap_p;
     const size_t s1 = 2 * (size_t)E.cap1, s2 = 2 * (size_t)E.cap2;
+    c.rows_key_dev = c.carve<unsigned long long>(1);
     E.pid1 = c.carve<int>(c.g.nUV);
     E.pcol1 = c.carve<int>(5 * s1);
     E.pval1 = c.carve<double>(5 * s1);
@@ -268,6 +269,33 @@ void setup_embedded(Context &c)
     c.l2.patch = RowPatch{E.pid2, E.pcol2, E.pval2, E.pdiag2};
 }
 
+// A checksum of which Poisson rows are patched: the sum over patched rows i of
+// (i + 1) times an odd constant, modulo 2^64 (order-free, so one block's tree sum
+// gives the same word every time).  A moving body changes it when it crosses cells.
+__global__ void __launch_bounds__(256) k_rows_key(const int *__restrict__ pid, int n, unsigned long long *key)
+{
+    __shared__ unsigned long long sh[256];
+    unsigned long long s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (pid[i] >= 0) s += (unsigned long long)(i + 1) * 0x9E3779B97F4A7C15ull;
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *key = sh[0];
+}
+
+unsigned long long read_rows_key(Context &c)
+{
+    unsigned long long k = 0;
+    if (!c.rows_key_dev) return 0;
+    CUIBM_TRY(cudaMemcpyAsync(&k, c.rows_key_dev, sizeof k, cudaMemcpyDeviceToHost, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    return k;
+}
+
 void launch_embedded_rows(Context &c)
 {
     auto &E = c.emb;
@@ -278,6 +306,8 @@ void launch_embedded_rows(Context &c)
     EmbGeom G{c.g.nx, c.g.ny, c.P.dt, c.P.nu, c.dx, c.dy, c.ib.ghostUV, c.ib.ghostP, c.ib.uB, c.ib.vB};
     const int cap = std::max(P.cap_v, P.cap_p);
     k_emb_rows<<<dim3(blocks_for(cap), 4), kBlock, 0, c.stream>>>(G, P, E);
+    CUIBM_TRY(cudaGetLastError());
+    k_rows_key<<<1, 256, 0, c.stream>>>(E.pid2, c.g.nP, c.rows_key_dev);
     CUIBM_TRY(cudaGetLastError());
     // the rows changed: the solvers' diagonal tables follow (not while the solvers are
     // being set up, which computes them from these rows)

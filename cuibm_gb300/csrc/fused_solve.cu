@@ -1665,6 +1665,15 @@ double solve_bytes(const LinearSystem &S, int it)
 // block per SM unless CUIBM_FUSED_BLOCKS_PER_SM asks for more and the kernel's
 // registers allow it) and build its tables.  A mixed-precision system gets its
 // mixed kernel and the float tables.
+// the SA hierarchy was rebuilt (new levels, same vectors): the solver's arguments follow
+void refresh_fused_hierarchy(Context &c, LinearSystem &S)
+{
+    if (!S.fused_fn) return;
+    if (S.amg.empty() || (int)S.amg.size() > kMaxLevels || sa_coarsest_size(S) > kDenseMax)
+        throw InputError("the rebuilt smoothed-aggregation hierarchy does not fit the persistent solver");
+    upload_fargs(c, S);
+}
+
 void set_fused_grid(LinearSystem &S, int blocks)
 {
     if (!S.fused_fn) return;

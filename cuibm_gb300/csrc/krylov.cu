@@ -498,8 +498,9 @@ __global__ void k_sa_level0_tables(int n, const double *__restrict__ dinv, doubl
 
 // The operator's rows changed (the embedded method's rows after a body moved): the
 // Jacobi table, the persistent solver's diagonal and the SA smoother's level-0 tables
-// follow.  The reference rebuilds its whole preconditioner each step instead; the
-// coarser SA levels here keep the operator of the initial tags.
+// follow.  The reference rebuilds its whole preconditioner each step; here the SA
+// hierarchy is rebuilt between steps when the set of patched rows changes
+// (rebuild_hierarchies in context.cu).
 void refresh_system_diagonals(Context &c, LinearSystem &S)
 {
     const int n = S.n;

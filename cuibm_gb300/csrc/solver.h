@@ -132,6 +132,11 @@ struct LinearSystem {
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
     int precision = PRECISION_FP64;
     double strength = 0.0;  // smoothed aggregation's strength threshold
+    // the SA hierarchy in its own allocations (so that it can be rebuilt) and the
+    // checksum of the patched-row pattern it was built from
+    bool sa_dynamic = false;
+    std::vector<void *> sa_blocks;
+    unsigned long long sa_key = 0;
     void *mixed = nullptr;  // mixed precision: the float tables (fused_solve.cu)
     double *ym = nullptr, *wdef = nullptr;  // constant-mode correction of the SA cycle (Poisson):
     double Edef = 0;                        // cycle output, A^T e, e^T A e
@@ -203,6 +208,11 @@ struct Context {
     int ib_slot = -1;                   // host-side IB bookkeeping of this context
     double ib_midX = 0, ib_midY = 0;    // body centre used by the tagging
     int force_method = 0;  // the step's force: 0 control volume, 1/2 surface integral (mode)
+    // moving body with the embedded method and an SA preconditioner: the hierarchy is
+    // rebuilt when the pattern of the patched rows changes (checksum below, per tagging)
+    bool sa_rebuild = false;
+    unsigned long long *rows_key_dev = nullptr;
+    int sa_rebuilds = 0;
     double cfl_max = 0;
     double forceX = 0, forceY = 0;
 
@@ -335,6 +345,9 @@ void launch_coupling_next(Context &c, cudaGraphConditionalHandle h, int use_cond
 // fused_solve.cu: the persistent solves' grid (blocks <= 0: the default); the step graph
 // must be rebuilt after
 void set_fused_grid(LinearSystem &S, int blocks);
+void refresh_fused_hierarchy(Context &c, LinearSystem &S);  // after the SA hierarchy was rebuilt
+// embedded.cu: the checksum of the Poisson patched-row pattern (written at every tagging)
+unsigned long long read_rows_key(Context &c);
 void initialise_body(Context &c);
 
 // io.cpp / fields.cu

@@ -62,6 +62,7 @@ typedef struct {
     int velocity_krylov, poisson_krylov;     /* 0 BiCGSTAB, 1 CG */
     int amg_levels;                   /* levels of the Poisson SA hierarchy (0 if none) */
     int velocity_precision, poisson_precision; /* 0 FP64, 1 MIXED (simParams.yaml `precision`) */
+    int sa_rebuilds;                  /* SA hierarchies rebuilt for a moving embedded body so far */
 } cuibm_info;
 
 /* Fields readable/writable through cuibm_get_field / cuibm_set_field.

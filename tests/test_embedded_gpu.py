@@ -182,7 +182,10 @@ def test_cg_is_rejected(tmp_path):
 @pytest.mark.parametrize("graph", [1, 0])
 def test_oscillating_cylinder_steps_match_oracle(tmp_path, graph):
     """A prescribed oscillation: the tags, the interpolation plan and the operator rows
-    follow the body every step (the reference rebuilds its matrices each step too)."""
+    follow the body every step (the reference rebuilds its matrices each step too), and
+    the Poisson solve's smoothed-aggregation hierarchy is rebuilt from the current rows
+    whenever the set of patched rows changes (the reference rebuilds its preconditioner
+    every step)."""
     motion = {"xCoefficient": 0.05, "uCoefficient": 0.05 * 2 * np.pi, "xfrequency": 1.0, "xPhase": 0.0,
               "uPhase": 0.0}
     f = emb_case(str(tmp_path / "c"), nt=30, motion=motion)
@@ -199,3 +202,4 @@ def test_oscillating_cylinder_steps_match_oracle(tmp_path, graph):
         assert np.array_equal(s.get("hybrid_tags_p"), ref.T.hybridTagsP)
         assert rel_l2(s.get("u"), ref.u) < 1e-9
         assert rel_l2(s.get("p"), ref.p) < 1e-8
+        assert s.get_info().sa_rebuilds > 0  # the body crossed cells
