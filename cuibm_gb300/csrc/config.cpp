@@ -9,7 +9,7 @@
 //   simParams.yaml       io/parseSimulationFile.cu (unknown SolverType -> NAVIER_STOKES
 //                        with a warning; unknown preconditioner -> NONE; startStep is read
 //                        but the reference never stores it, so it stays 0 - except with
-//                        restart: true, where this build continues from that step's state)
+//                        restart: true, where the library continues from that step's state)
 //   flow.yaml            io/parseFlowFile.cu (bad location/type is an error here, where
 //                        the reference prints and calls exit(0))
 //   domain.yaml          io/parseDomainFile.cu (only the description is read here;
@@ -516,7 +516,7 @@ std::string load_case(const std::string &folder_in, int argc, const char **argv,
         else if (!strcmp(a, "-dt")) ok = cli_value(argv[++i], P.dt);
         else if (!strcmp(a, "-velocityTol")) ok = cli_value(argv[++i], P.velocity.tolerance);
         else if (!strcmp(a, "-poissonTol")) ok = cli_value(argv[++i], P.poisson.tolerance);
-        // this build's own: the persistent solves' grid size (batched instances share the GPU)
+        // extensions of the reference's flags: the persistent solves' grid (batched instances share the GPU)
         else if (!strcmp(a, "-solverBlocks")) ok = cli_value(argv[++i], P.solverBlocks) && P.solverBlocks >= 0;
         else if (!strcmp(a, "-solverPack"))
             ok = cli_value(argv[++i], P.solverPack) && (P.solverPack == 1 || P.solverPack == 2);

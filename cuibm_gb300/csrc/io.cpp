@@ -1,5 +1,5 @@
 // Output files in the reference's formats, so its post-processing scripts read
-// this build's output unchanged:
+// the library's output unchanged:
 //   grid             src/io/io.cu:428-444 (int nx, nx+1 doubles, int ny, ny+1 doubles; the
 //                    reference writes one double past the cell centres - here the domain
 //                    end coordinate)
@@ -10,7 +10,7 @@
 //   forces           luoIBM.cu:76-78 (time, Fx, Fy); fadlunModified.cu:64-78 (time, Fx,
 //                    FxX, FxY, FxU, Fy)
 //   midPosition      luo_base.cu:193-205 (timeStep, X, Y, U, V)
-// and one file of this build's own:
+// and one file the reference does not write:
 //   NNNNNNN/state    every nsave steps beside q and lambda: what a step reads from the
 //                    one before it (velocity with its ghost values, the velocity solve's
 //                    start, the convection term for Adams-Bashforth, pressure, the

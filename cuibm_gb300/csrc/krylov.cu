@@ -443,7 +443,7 @@ void setup_system(Context &c, LinearSystem &S)
     S.precision = L.precision;
     S.strength = L.strength;
     if (S.precond == PC_AINV)
-        throw InputError("preconditioner AINV is not implemented by this build; use DIAGONAL or SMOOTHED_AGGREGATION");
+        throw InputError("preconditioner AINV is not implemented by libcuibm_gb300; use DIAGONAL or SMOOTHED_AGGREGATION");
     const int n = S.n;
     S.r = c.carve<double>(n);
     S.rs = c.carve<double>(n);

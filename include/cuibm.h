@@ -44,7 +44,7 @@ typedef enum {
     CUIBM_ERR_NOT_CONVERGED = 4, /* a linear solve hit maxIterations (reference: std::exit(-1)) */
     CUIBM_ERR_NAN = 5,           /* a non-finite residual appeared in a solve */
     CUIBM_ERR_STATE = 6,         /* call out of order (e.g. step before initialise) */
-    CUIBM_ERR_UNSUPPORTED = 7    /* a configuration this build does not implement */
+    CUIBM_ERR_UNSUPPORTED = 7    /* a configuration the library does not implement */
 } cuibm_status;
 
 /* solver types, same order and names as the reference's src/types.h */

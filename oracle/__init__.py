@@ -1,7 +1,7 @@
 """CPU oracle of the fractional-step path (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
-legs use this package, as the checker or the CPU baseline.  The product
+legs use this package, as the test oracle or the CPU baseline.  The product
 (cuibm_gb300) never imports it.
 
 liboracle.so (oracle/*.c) is a plain-C restatement of the reference's kernels

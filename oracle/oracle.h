@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline leg of bench.py load this library (through oracle/__init__.py),
- * and only as the checker or the CPU baseline.  The product never links it.
+ * and only as the test oracle or the CPU baseline.  The product never links it.
  *
  * Every function names the reference file and function it restates.  The
  * arithmetic keeps the reference's association order and the library is

@@ -149,7 +149,7 @@ def test_cg_is_rejected(tmp_path):
 def test_moving_cylinder_steps_match_oracle(tmp_path):
     """Fadlun with a prescribed motion: tags follow the body, the operators stay those of
     the initial tags (the reference's updateSolver does not rebuild them).  That mix
-    diverges after about a dozen steps here, in the oracle as in this build, so the
+    diverges after about a dozen steps here, in the oracle as in the library, so the
     comparison covers the first six."""
     motion = {"xCoefficient": 0.05, "uCoefficient": 0.05 * 2 * np.pi, "xfrequency": 1.0, "xPhase": 0.0,
               "uPhase": 0.0}

@@ -5,7 +5,7 @@ extracted by tests/golden/make_golden.py --only recorded).  The case is restated
 here from its simParams/flow/domain/bodies files.
 
 The body's prescribed position and velocity (midPosition_init, 6 significant
-figures) are reproduced step for step.  The recorded forces are not: this build and
+figures) are reproduced step for step.  The recorded forces are not: the library and
 the oracle restatement (direct solves) agree with each other to 1e-5 but sit 8-11 %
 above the recording in the first steps and about 11 % off (median over the first
 300 steps where |Fx| > 0.05; up to 80 % next to sign changes) later; the restatement's
