@@ -545,6 +545,7 @@ int cuibm_initialise(cuibm_ctx *h)
 // hierarchies, built from the current rows (and the step graph follows them).
 static void rebuild_hierarchies(Context &c)
 {
+    if (c.sa_rebuild_interval <= 0 || c.timeStep - c.sa_last_rebuild < c.sa_rebuild_interval) return;
     const unsigned long long key = read_rows_key(c);
     bool rebuilt = false;
     for (LinearSystem *S : {&c.sys1, &c.sys2}) {
@@ -554,6 +555,7 @@ static void rebuild_hierarchies(Context &c)
         refresh_fused_hierarchy(c, *S);
         S->sa_key = key;
         c.sa_rebuilds++;
+        c.sa_last_rebuild = c.timeStep;
         rebuilt = true;
     }
     if (rebuilt && c.use_graph) build_step_graph(c);
@@ -854,7 +856,10 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
     } else if (k == "step_sync") {
         c.step_sync = value != 0;
     } else if (k == "write_output") c.P.writeOutput = value != 0;
-    else if (k == "solver_blocks") {
+    else if (k == "sa_rebuild_interval") {
+        if (value != (int)value) return fail(h, CUIBM_ERR_BAD_INPUT, "sa_rebuild_interval must be a whole number");
+        c.sa_rebuild_interval = (int)value;
+    } else if (k == "solver_blocks") {
         const int nb = (int)value;
         if (nb != value || nb < 0) return fail(h, CUIBM_ERR_BAD_INPUT, "solver_blocks must be a count >= 0");
         c.P.solverBlocks = nb;

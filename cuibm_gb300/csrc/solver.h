@@ -213,6 +213,8 @@ struct Context {
     bool sa_rebuild = false;
     unsigned long long *rows_key_dev = nullptr;
     int sa_rebuilds = 0;
+    int sa_rebuild_interval = 1;   // option "sa_rebuild_interval": fewest steps between rebuilds
+    int sa_last_rebuild = 0;       // time step of the last one
     double cfl_max = 0;
     double forceX = 0, forceY = 0;
 

@@ -192,7 +192,11 @@ int cuibm_get_timer(cuibm_ctx *ctx, const char *name, double *ms, int *count);
  * (1: cuibm_step waits and checks the solves' status; 0: it only enqueues the
  * steps on the context's stream and a later cuibm_step(ctx, 0) checks),
  * "trace_solve" (1: record per-barrier timestamps in CUIBM_F_SOLVE_TRACE),
- * "write_output" (0: no files), "solver_blocks" (blocks of the persistent solves,
+ * "write_output" (0: no files), "sa_rebuild_interval" (a moving body with the
+ * embedded method: the SA hierarchy is rebuilt from the current rows when the set of
+ * patched rows changed and at least this many steps passed since the last rebuild;
+ * default 1, as the reference rebuilds every step; <= 0 never), "solver_blocks"
+ * (blocks of the persistent solves,
  * 0: one per SM; as -solverBlocks, changeable after cuibm_initialise),
  * "force_method" (the step's body force, which the
  * forces file, cuibm_get_forces and the flow-induced motion use: 0 the control
