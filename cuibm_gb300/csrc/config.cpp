@@ -304,9 +304,12 @@ std::string parse_simulation(const Node *doc, Params &P)
                 ls.precond = precond_from(precond);
                 ls.tolerance = tol;
                 ls.maxIterations = maxIter;
-                if (s->get("strengthThreshold") && !to_double(s->get("strengthThreshold"), ls.strength))
-                    return "simParams.yaml: strengthThreshold must be a number";
-                if (ls.strength < 0 || ls.strength >= 1) return "simParams.yaml: strengthThreshold must be in [0, 1)";
+                if (s->get("strengthThreshold")) {
+                    if (!to_double(s->get("strengthThreshold"), ls.strength))
+                        return "simParams.yaml: strengthThreshold must be a number";
+                    if (ls.strength < 0 || ls.strength >= 1)
+                        return "simParams.yaml: strengthThreshold must be in [0, 1)";
+                }
                 if (s->get("precision")) {
                     const std::string &pv = s->get("precision")->text;
                     if (pv == "MIXED") ls.precision = PRECISION_MIXED;

@@ -25,8 +25,9 @@ struct LinearSolve {
     // `strengthThreshold`: smoothed aggregation links i and j when |a_ij| >= theta sqrt(|a_ii a_jj|)
     // (either way round).  0 (CUSP's default) makes every entry strong.  On the stretched cylinder
     // grids theta = 0.05 halves the Poisson iterations (anisotropic cells coarsen along their strong
-    // direction) at about twice the hierarchy's operator complexity
-    double strength = 0.0;
+    // direction) at about twice the hierarchy's operator complexity.  Unset (-1): 0, except 0.05
+    // for the embedded method with a moving body, where theta = 0 broke down (krylov.cu)
+    double strength = -1.0;
 };
 
 struct AxisDesc {

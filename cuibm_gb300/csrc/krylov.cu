@@ -441,7 +441,10 @@ void setup_system(Context &c, LinearSystem &S)
     S.rtol = L.tolerance;
     S.maxit = L.maxIterations;
     S.precision = L.precision;
-    S.strength = L.strength;
+    // unset threshold: CUSP's 0, but 0.05 for a moving embedded body (its SA-preconditioned
+    // Poisson solves stalled or broke down with 0 on the oscillating-cylinder cases)
+    S.strength = L.strength >= 0 ? L.strength
+                                 : (c.P.solverType == ST_OSC && c.has_body && body_moves(c) ? 0.05 : 0.0);
     if (S.precond == PC_AINV)
         throw InputError("preconditioner AINV is not implemented by libcuibm_gb300; use DIAGONAL or SMOOTHED_AGGREGATION");
     const int n = S.n;
