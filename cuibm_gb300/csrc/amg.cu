@@ -127,30 +127,47 @@ static double rho_dinv_a(const HostCsr &A, const std::vector<double> &d)
 // |a_ij| where row i has the entry (phase 2 of the aggregation picks the strongest).
 static HostCsr strength_graph(const HostCsr &A, const std::vector<double> &d, double theta)
 {
-    std::vector<std::vector<std::pair<int, double>>> adj(A.n);
-    for (int i = 0; i < A.n; ++i)
-        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
-            const int j = A.col[k];
-            const double a = std::fabs(A.val[k]);
-            if (j == i || A.val[k] == 0) continue;
-            if (a < theta * std::sqrt(std::fabs(d[i] * d[j]))) continue;
-            adj[i].push_back({j, a});
-            adj[j].push_back({i, -a});  // the reverse link, used where row j lacks the entry
-        }
+    const int n = A.n;
+    auto strong = [&](int i, int k) {
+        const int j = A.col[k];
+        return j != i && A.val[k] != 0 && std::fabs(A.val[k]) >= theta * std::sqrt(std::fabs(d[i] * d[j]));
+    };
+    // the links of every row in one flat array (counted first: a rebuilt hierarchy of a
+    // moving body repeats this at every step, and a list per row cost most of it)
+    std::vector<int> start(n + 1, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (strong(i, k)) {
+                start[i + 1]++;
+                start[A.col[k] + 1]++;
+            }
+    for (int i = 0; i < n; ++i) start[i + 1] += start[i];
+    std::vector<std::pair<int, double>> e(start[n]);
+    std::vector<int> pos(start.begin(), start.end() - 1);
+    for (int i = 0; i < n; ++i)
+        for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+            if (strong(i, k)) {
+                const int j = A.col[k];
+                const double a = std::fabs(A.val[k]);
+                e[pos[i]++] = {j, a};
+                e[pos[j]++] = {i, -a};  // the reverse link, used where row j lacks the entry
+            }
     HostCsr S;
-    S.n = S.m = A.n;
-    S.ptr.assign(A.n + 1, 0);
-    for (int i = 0; i < A.n; ++i) {
-        auto &v = adj[i];
-        std::sort(v.begin(), v.end(), [](const std::pair<int, double> &x, const std::pair<int, double> &y) {
-            return x.first != y.first ? x.first < y.first : x.second > y.second;  // own entry first
-        });
+    S.n = S.m = n;
+    S.ptr.assign(n + 1, 0);
+    S.col.reserve(e.size());
+    S.val.reserve(e.size());
+    for (int i = 0; i < n; ++i) {
+        std::sort(e.begin() + start[i], e.begin() + start[i + 1],
+                  [](const std::pair<int, double> &x, const std::pair<int, double> &y) {
+                      return x.first != y.first ? x.first < y.first : x.second > y.second;  // own entry first
+                  });
         int last = -1;
-        for (auto &e : v) {
-            if (e.first == last) continue;
-            S.col.push_back(e.first);
-            S.val.push_back(std::fabs(e.second));
-            last = e.first;
+        for (int q = start[i]; q < start[i + 1]; ++q) {
+            if (e[q].first == last) continue;
+            S.col.push_back(e[q].first);
+            S.val.push_back(std::fabs(e[q].second));
+            last = e[q].first;
         }
         S.ptr[i + 1] = (int)S.col.size();
     }

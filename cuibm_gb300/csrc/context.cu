@@ -9,6 +9,7 @@
 // and is recorded once into a CUDA graph whose linear solves are WHILE
 // conditional nodes: one graph launch per step, no host synchronisation inside a
 // step.  cuibm_step checks the solver status once at the end of the call.
+#include <chrono>
 #include <cstdio>
 #include <cmath>
 #include <cstring>
@@ -550,12 +551,16 @@ static void rebuild_hierarchies(Context &c)
     bool rebuilt = false;
     for (LinearSystem *S : {&c.sys1, &c.sys2}) {
         if (!S->sa_dynamic || S->sa_key == key) continue;
+        const auto t0 = std::chrono::steady_clock::now();
         free_sa_hierarchy(*S);
         build_sa_hierarchy(c, *S);
         refresh_fused_hierarchy(c, *S);
         S->sa_key = key;
         c.sa_rebuilds++;
         c.sa_last_rebuild = c.timeStep;
+        Timer &tm = c.timers["SA rebuild"];  // host time, read with cuibm_get_timer
+        tm.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        tm.count++;
         rebuilt = true;
     }
     if (rebuilt && c.use_graph) build_step_graph(c);
