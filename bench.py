@@ -244,10 +244,11 @@ def run_ours(a, rank, world, local, pg):
     achieved = b / (ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-            "traffic": profiled_traffic(dom), "bytes_per_launch": b, "ms_per_launch": round(ms, 5),
+            "bytes_per_launch": b, "ms_per_launch": round(ms, 5),
             "iterations_per_launch": its,
             "other_kernels": {k: {"ms": round(v[0], 5), "GB/s": round(v[1] / (v[0] * 1e-3) / 1e9, 1)}
                               for k, v in prof.items()}}
+    roof["traffic"], roof["traffic_source"] = profiled_traffic(dom, a.workload)
     s.close()
 
     # end to end through the public API with host buffers, on a fresh instance over
@@ -417,22 +418,24 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
     return out
 
 
-def profiled_traffic(kernel):
-    """DRAM bytes per launch of the kernel from the committed ncu summary
-    (profiles/*.md, a line 'dram_bytes_per_launch <kernel> <bytes>'); None where
-    there is none."""
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of the kernel as an ncu capture measured them: the line
+    'dram_bytes_per_launch <kernel> <workload> <bytes>' of a committed summary under
+    profiles/.  This run does not measure DRAM traffic (that needs ncu); the number is
+    returned with the summary it comes from, which names the captured launch.  (None,
+    None) where no summary has one for this kernel and workload."""
     here = os.path.dirname(os.path.abspath(__file__))
     d = os.path.join(here, "profiles")
     if not os.path.isdir(d):
-        return None
+        return None, None
     for fn in sorted(os.listdir(d)):
         if not fn.endswith((".md", ".txt")):
             continue
         for line in open(os.path.join(d, fn)):
             f = line.strip().strip("`").split()
-            if len(f) == 3 and f[0] == "dram_bytes_per_launch" and f[1] == kernel:
-                return int(f[2])
-    return None
+            if len(f) == 4 and f[0] == "dram_bytes_per_launch" and f[1] == kernel and f[2] == workload:
+                return int(f[3]), "ncu capture summarised in profiles/" + fn + " (not measured by this run)"
+    return None, None
 
 
 def cpu_baseline(workload, budget_s=15.0, warmup=1, max_steps=200):

@@ -402,24 +402,33 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
 }
 
-// Algorithmic bytes of one V-cycle: per level with a coarser one, the smoother
-// and residual read b and write x and r; restriction reads r and the R matrix;
-// prolongation reads the coarse x and P and updates x; the post-smoother reads
-// b and x and writes the result.  Matrices count 12 bytes per entry.
+// Algorithmic bytes of one V-cycle of launch_vcycle, kernel by kernel: per level with
+// a coarser one, the downward sweep reads b and the Jacobi weights and writes x and r
+// (and reads the level's CSR matrix below level 0, whose operator is matrix-free); the
+// restriction reads r and R and writes the coarse b; on the way up the prolongation
+// reads the coarse x and P and updates x, and the smoothing sweep reads b, the
+// weights and x (and the matrix) and writes its result.  A CSR matrix is 12 bytes per
+// entry plus its row pointers.  The coarsest level's dense inverse (8 n_c^2 bytes) is
+// an implementation choice, not algorithmic: it is left out, the coarsest level
+// counting only its right-hand side and solution.
 double sa_vcycle_bytes(const LinearSystem &S)
 {
+    auto csr = [](const DevCsr &M) { return 12.0 * M.nnz + 4.0 * (M.n + 1); };
+    const int nl = (int)S.amg.size();
     double b = 0;
-    for (size_t l = 0; l < S.amg.size(); ++l) {
+    for (int l = 0; l < nl; ++l) {
         const SaLevel *L = S.amg[l];
-        if (l + 1 == S.amg.size()) {
-            b += (double)L->n * L->n * 8 + 2.0 * L->n * 8;
+        const double n = L->n;
+        if (l + 1 == nl) {
+            b += 16.0 * n;
             break;
         }
-        double nnzP = 0, nnzR = 0;
-        (void)nnzP;
-        (void)nnzR;
-        b += 8.0 * L->n * 8;  // b, x, r (down); x rmw, b, out (up)
-        b += 12.0 * L->P.n * 2.5 + 12.0 * L->R.n * 20;  // approximate matrix traffic
+        const double nc = S.amg[l + 1]->n;
+        const double a = l > 0 ? csr(L->A) : 0.0;
+        b += 32.0 * n + a;                   // down: b, dinv in; x, r out
+        b += 8.0 * n + csr(L->R) + 8.0 * nc; // restriction
+        b += 8.0 * nc + csr(L->P) + 16.0 * n;  // prolongation into x
+        b += 32.0 * n + a;                   // up: b, dinv, x in; result out
     }
     return b;
 }

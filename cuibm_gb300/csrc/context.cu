@@ -339,7 +339,10 @@ static int fail(cuibm_ctx *h, int code, const std::string &msg)
         return fail(h, CUIBM_ERR_BAD_INPUT, e.what());                            \
     }
 
-static std::string g_create_error;
+// error text of the context-free entry points, one per host thread: cuibm_case_error
+// returns the calling thread's last message, so a failure on one thread cannot free or
+// overwrite the text another thread is reading
+static thread_local std::string g_create_error;
 
 // error text of the context-free entry points (read back through cuibm_case_error)
 std::string cuibm_noalloc_error_sink(const std::string &msg)

@@ -1644,8 +1644,10 @@ double solve_bytes(const LinearSystem &S, int it)
     auto csr = [E](const DevCsr &M) { return E * M.nnz + 4.0 * (M.n + 1); };
     double vc = 0;  // one V-cycle without its first sweep's vector reads
     const int L = (int)S.amg.size();
+    // the coarsest level's dense inverse (8 n_c^2 bytes a cycle) is an implementation
+    // choice, not algorithmic: solve_dense_bytes reports it apart
     if (L == 1) {
-        vc = 8.0 * (double)S.amg[0]->n * S.amg[0]->n + 2 * DL * S.amg[0]->n;
+        vc = 2 * DL * S.amg[0]->n;
     } else if (L > 1) {
         vc += 2 * DL * n;  // first sweep: omega D^-1 and r_0 (its input is counted by the caller)
         for (int l = 0; l < L - 1; ++l) {
@@ -1655,7 +1657,7 @@ double solve_bytes(const LinearSystem &S, int it)
             vc += 4 * DL * V->n + csr(V->P) + csr(V->AP) + DL * C->n;          // prolongation and sweep
         }
         const double nc = S.amg[L - 1]->n;
-        vc += 8.0 * nc * nc + 2 * DL * nc;
+        vc += 2 * DL * nc;
     }
     double per_it, init;
     if (S.krylov == KRYLOV_CG) {
@@ -1669,6 +1671,16 @@ double solve_bytes(const LinearSystem &S, int it)
             per_it = 9 * D * n + 7 * D * n + 8 * D * n;
     }
     return init + it * per_it;
+}
+
+// Bytes of the coarsest level's dense inverse read by the solve's V-cycles (two per
+// BiCGSTAB iteration, one per CG iteration and one before it), apart from solve_bytes
+double solve_dense_bytes(const LinearSystem &S, int it)
+{
+    if (S.precond != PC_SMOOTHED_AGGREGATION || S.amg.empty()) return 0;
+    const double nc = S.amg.back()->n;
+    const double cycles = S.krylov == KRYLOV_CG ? it + 1.0 : 2.0 * it;
+    return cycles * 8.0 * nc * nc;
 }
 
 // Decide whether the system can use the persistent solver, size its grid (one

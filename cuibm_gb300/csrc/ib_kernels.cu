@@ -9,8 +9,9 @@
 //
 // This translation unit is compiled with -fmad=false: every tag decision uses the
 // reference's arithmetic exactly, so tag arrays are bit-identical to the
-// reference's.  Intercepts use CUDA's acos/sin/tan, which may differ from the
-// host C library in the last bit; interpolation weights then agree to a few ulp.
+// reference's.  Intercepts use the closed form of the reference's trigonometric
+// expression (intercept_dev), so they and the interpolation weights are exact
+// functions of correctly rounded operations.
 //
 // Determinism.  The reference's tagging threads write into neighbouring nodes
 // (ghost tags, body intercepts, image points), so the result depends on thread
@@ -55,19 +56,26 @@ struct TagGeom {
     const double *motion;  // moving body: the centre is motion[0], motion[1] (set on the device)
 };
 
+// Foot of the perpendicular from (px, py) onto the line through body points k and l.
+// The reference (tagPoints.cu, e.g. :107-117) takes the angle th at point k from the
+// law of cosines with acos, then moves a / tan(th) along the segment, a = b sin(th).
+// That distance is b cos(th) = (p^2 + b^2 - o^2) / (2 p), computed here with +, -, x, /
+// and sqrt only: correctly rounded operations, so (with -fmad=false) the intercepts
+// and every interpolation weight built from them are the same on the GPU and in a
+// host restatement, bit for bit, where the transcendental form differed in the last
+// bits between CUDA's and the host library's acos/sin/tan.
 __device__ __forceinline__ void intercept_dev(const double *bx, const double *by, int k, int l, double px,
                                               double py, double *ix, double *iy)
 {
-    double dxs = bx[l] - bx[k], dys = by[l] - by[k];
-    double dxo = bx[l] - px, dyo = by[l] - py;
-    double dxb = px - bx[k], dyb = py - by[k];
-    double p = sqrt(dxs * dxs + dys * dys);
-    double o = sqrt(dxo * dxo + dyo * dyo);
-    double b = sqrt(dxb * dxb + dyb * dyb);
-    double th = acos((p * p + b * b - o * o) / (2 * p * b));
-    double a = sin(th) * b;
-    *iy = by[k] + (by[l] - by[k]) / p * a / tan(th);
-    *ix = bx[k] + (bx[l] - bx[k]) / p * a / tan(th);
+    const double dxs = bx[l] - bx[k], dys = by[l] - by[k];
+    const double dxo = bx[l] - px, dyo = by[l] - py;
+    const double dxb = px - bx[k], dyb = py - by[k];
+    const double p = sqrt(dxs * dxs + dys * dys);
+    const double o = sqrt(dxo * dxo + dyo * dyo);
+    const double b = sqrt(dxb * dxb + dyb * dyb);
+    const double t = (p * p + b * b - o * o) / (2 * p);
+    *iy = by[k] + (by[l] - by[k]) / p * t;
+    *ix = bx[k] + (bx[l] - bx[k]) / p * t;
 }
 
 struct RecWriter {
@@ -1751,8 +1759,10 @@ extern "C" int cuibm_cv_force_noalloc(const double *u, const double *uold, const
     };
     if (!u || !uold || !p || !ghost_tags_uv || !dx || !dy || !force_out)
         return fail(1, "cuibm_cv_force_noalloc: null pointer argument");
-    if (nx < 3 || ny < 3 || bb_ncx < 1 || bb_ncy < 1 || bb_i < 1 || bb_j < 1 || bb_i + bb_ncx >= nx ||
-        bb_j + bb_ncy >= ny || !(dt > 0))
+    // the box's east column reads u at column bb_i + bb_ncx (u has columns 0..nx-2) and its
+    // north row reads v at row bb_j + bb_ncy (v has rows 0..ny-2)
+    if (nx < 3 || ny < 3 || bb_ncx < 1 || bb_ncy < 1 || bb_i < 1 || bb_j < 1 || bb_i + bb_ncx > nx - 2 ||
+        bb_j + bb_ncy > ny - 2 || !(dt > 0))
         return fail(1, "cuibm_cv_force_noalloc: box or grid sizes out of range");
     const long long nodes = (long long)(bb_ncx + 1) * (bb_ncy + 1);
     if (nodes > (long long)kCvForceMaxBlocks * kBlock)

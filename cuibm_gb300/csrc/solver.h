@@ -295,7 +295,8 @@ void refresh_system_diagonals(Context &c, LinearSystem &S);  // after the operat
 void setup_fused(Context &c, LinearSystem &S);
 void launch_fused_solve(Context &c, LinearSystem &S, const double *b, double *x);
 void set_fused_trace(Context &c, LinearSystem &S, bool on);
-double solve_bytes(const LinearSystem &S, int iterations);
+double solve_bytes(const LinearSystem &S, int iterations);        // algorithmic bytes
+double solve_dense_bytes(const LinearSystem &S, int iterations);  // the coarsest dense inverse's
 void refresh_fused_diag(Context &c, LinearSystem &S);
 void refresh_fused_level0(Context &c, LinearSystem &S);
 void free_fused(LinearSystem &S);

@@ -229,13 +229,18 @@ int cuibm_launch_count(cuibm_ctx *ctx, long long *per_step);
  * Inputs (device pointers of the current device): u and uold (numUV doubles,
  * velocity at the new and previous step), p (numP), ghost_tags_uv (numUV ints,
  * -1 marks fluid nodes), dx (nx), dy (ny); the box (bb_i, bb_j, bb_ncx, bb_ncy)
- * in cell indices; nu and dt.  Output: force_out[0..1] = (Fx, Fy), device
- * memory.  Limit: (bb_ncx+1)*(bb_ncy+1) <= 262144 box nodes (a 511 x 511 box);
- * larger boxes are rejected with CUIBM_ERR_BAD_INPUT.  The first call on a
+ * in cell indices, which must be the box of the current step (a moving body's
+ * box moves every step; a stale box gives a wrong force, not an error); nu and
+ * dt.  Output: force_out[0..1] = (Fx, Fy), device memory.  Limits:
+ * (bb_ncx+1)*(bb_ncy+1) <= 262144 box nodes (a 511 x 511 box), bb_i, bb_j >= 1,
+ * bb_i + bb_ncx <= nx - 2 and bb_j + bb_ncy <= ny - 2 (the box's east and north
+ * edges read one more u column and v row); other boxes are rejected with
+ * CUIBM_ERR_BAD_INPUT.  The first call on a
  * device looks up the scratch address with cudaGetSymbolAddress; make it
  * before any stream capture.  Every call shares the one scratch array, so
  * calls that overlap on the GPU (different streams, or different host
- * threads) race: order them on one stream.  Error text: cuibm_case_error(). */
+ * threads) race: order them on one stream.  Error text: cuibm_case_error(),
+ * which returns the calling host thread's last message. */
 int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p, const int *ghost_tags_uv,
                            const double *dx, const double *dy, int nx, int ny, int bb_i, int bb_j, int bb_ncx,
                            int bb_ncy, double nu, double dt, double *force_out, void *stream);
@@ -274,6 +279,7 @@ void cuibm_batch_destroy(cuibm_batch *b);
  * io::readInputs + io::parseDomainFile/parseBodiesFile (src/io/io.cu:108-138). */
 int cuibm_case_info(const char *case_folder, int argc, const char **argv, cuibm_info *info);
 int cuibm_case_array(const char *case_folder, int argc, const char **argv, int field, double *dst, size_t count);
+/* the calling host thread's last error of a context-free entry point */
 const char *cuibm_case_error(void);
 
 #ifdef __cplusplus

@@ -364,6 +364,30 @@ class Stencils:
                        q1=_d(self.q[0]), q2=_d(self.q[1]), q3=_d(self.q[2]), q4=_d(self.q[3]))
 
 
+def set_intercept_form(form):
+    """Body intercepts of the tagging: 0 the reference's trigonometric form (acos, sin,
+    tan), 1 its closed form (the default, what the GPU computes).  Returns the previous
+    form."""
+    prev = _sig("or_get_intercept_form", restype=INT)()
+    _sig("or_set_intercept_form", INT)(int(form))
+    return prev
+
+
+class intercept_form:
+    """Context manager: tag with the given intercept form inside the block."""
+
+    def __init__(self, form):
+        self.form = form
+
+    def __enter__(self):
+        self.prev = set_intercept_form(self.form)
+        return self
+
+    def __exit__(self, *exc):
+        set_intercept_form(self.prev)
+        return False
+
+
 # arrays luo_base::tagPoints does not refill (luo_base/tagPoints.cu:26-40): a re-tagging
 # keeps their values where the kernels do not write
 _TAG_CARRIED = ("dist_u_body", "dist_v_body", "uv", "bip_x", "bip_y", "ipp_x", "ipp_y")

@@ -30,18 +30,44 @@
 
 #define EPS 1.e-10
 
-/* foot of the perpendicular from (px,py) onto the line through body points k and l,
- * in the reference's trigonometric form (tagPoints.cu, e.g. :107-117) */
+/* Which form of the body intercept the tagging uses: 0 the reference's trigonometric
+ * form, 1 (the default) its closed form.  Both give the foot of the perpendicular
+ * from (px,py) onto the line through body points k and l at distance b cos(th) from
+ * point k along the segment.  The reference computes th = acos((p^2 + b^2 - o^2) /
+ * (2 p b)), then a = b sin(th) and a / tan(th) (tagPoints.cu, e.g. :107-117): three
+ * transcendental calls whose last bits differ between CUDA's and the C library's
+ * implementations.  a / tan(th) = b cos(th) = (p^2 + b^2 - o^2) / (2 p) (law of
+ * cosines) needs only +, -, x, / and sqrt, which are correctly rounded on both, so
+ * with no fused multiply-add the GPU's intercepts (and every interpolation weight
+ * built from them) equal this restatement's bit for bit.  Form 0 is kept to pin this
+ * restatement against the reference's own kernels (golden fixtures); the two forms
+ * differ by a few ulp of the coordinates. */
+static int intercept_form = 1;
+void or_set_intercept_form(int form) { intercept_form = form; }
+int or_get_intercept_form(void) { return intercept_form; }
+
 static void intercept(const double *bx, const double *by, int k, int l, double px, double py, double *ix,
                       double *iy)
 {
-    double p = sqrt(pow((bx[l] - bx[k]), 2) + pow((by[l] - by[k]), 2));
-    double o = sqrt(pow((bx[l] - px), 2) + pow((by[l] - py), 2));
-    double b = sqrt(pow((px - bx[k]), 2) + pow((py - by[k]), 2));
-    double th = acos((p * p + b * b - o * o) / (2 * p * b));
-    double a = sin(th) * b;
-    *iy = by[k] + (by[l] - by[k]) / p * a / tan(th);
-    *ix = bx[k] + (bx[l] - bx[k]) / p * a / tan(th);
+    if (intercept_form == 0) {
+        double p = sqrt(pow((bx[l] - bx[k]), 2) + pow((by[l] - by[k]), 2));
+        double o = sqrt(pow((bx[l] - px), 2) + pow((by[l] - py), 2));
+        double b = sqrt(pow((px - bx[k]), 2) + pow((py - by[k]), 2));
+        double th = acos((p * p + b * b - o * o) / (2 * p * b));
+        double a = sin(th) * b;
+        *iy = by[k] + (by[l] - by[k]) / p * a / tan(th);
+        *ix = bx[k] + (bx[l] - bx[k]) / p * a / tan(th);
+        return;
+    }
+    const double dxs = bx[l] - bx[k], dys = by[l] - by[k];
+    const double dxo = bx[l] - px, dyo = by[l] - py;
+    const double dxb = px - bx[k], dyb = py - by[k];
+    const double p = sqrt(dxs * dxs + dys * dys);
+    const double o = sqrt(dxo * dxo + dyo * dyo);
+    const double b = sqrt(dxb * dxb + dyb * dyb);
+    const double t = (p * p + b * b - o * o) / (2 * p);
+    *iy = by[k] + (by[l] - by[k]) / p * t;
+    *ix = bx[k] + (bx[l] - bx[k]) / p * t;
 }
 
 /* one velocity node (kind 0 = u, 1 = v) of tag_u_luo / tag_v_luo */

@@ -86,6 +86,10 @@ typedef struct {
     double *q1, *q2, *q3, *q4; /* the corner values the fit used (field or substituted body values) */
 } or_interp;
 
+/* body intercept form of the tagging: 0 the reference's trigonometric form, 1 its
+ * closed form (the default; the GPU's) */
+void or_set_intercept_form(int form);
+int or_get_intercept_form(void);
 void or_tagPoints(or_tags *T, const double *bx, const double *by, const double *uB, const double *vB,
                   const double *xu, const double *yu, const double *xv, const double *yv, int i_start,
                   int j_start, int width, int height, int nx, int ny, int totalPoints, double midX, double midY);

@@ -623,9 +623,12 @@ def recorded_run(ref_root, name, case_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference/src")
+    ap.add_argument("--ref", default=os.environ.get("CUIBM_REF_SRC"),
+                    help="src folder of a cuIBM source tree (default: $CUIBM_REF_SRC)")
     ap.add_argument("--only", default=None, help="generate one group: fadlun, iter, surface, recorded")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref <cuIBM>/src or set CUIBM_REF_SRC")
     if a.only == "recorded":  # data files of the reference tree, no build needed
         recorded_run(os.path.dirname(os.path.abspath(a.ref)), "recorded_osc_static_external",
                      "osc/static/external")

@@ -1,7 +1,7 @@
 """GPU parity of the external (Luo) immersed-boundary path against the oracle,
-through the C ABI: tags bit-exact; interpolation stencils (indices bit-exact,
-weights to RTOL_W); interpolated/blended fields to RTOL_KERNEL; whole steps of
-the impulsively started cylinder to 1e-9 relative L2 and forces to 1e-6."""
+through the C ABI: tags, body intercepts, image points and interpolation stencils
+(indices and weights) bit-exact; interpolated/blended fields to RTOL_KERNEL; whole
+steps of the impulsively started cylinder to 1e-9 relative L2 and forces to 1e-6."""
 import numpy as np
 import pytest
 
@@ -12,9 +12,9 @@ from cuibm_gb300 import cases  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-RTOL_W = 1e-10       # weights: CUDA acos/sin/tan vs the C library differ in the last bits,
-                     # amplified by the cofactor inverse of the 4x4 bilinear fit
-RTOL_KERNEL = 1e-10  # fields built from those weights
+RTOL_W = 0.0         # weights: the intercepts are exact functions of correctly rounded
+                     # operations on both sides (closed form, no fused multiply-add)
+RTOL_KERNEL = 1e-13  # fields built from those weights (sums in the kernels' own order)
 
 
 def rel_max(a, b):
@@ -75,7 +75,10 @@ def test_tags_bit_exact(luo):
         assert np.array_equal(luo.get(mine), ref), mine
     sel = np.nonzero((T.ghostTagsUV > 0) | (T.hybridTagsUV > 0))[0]
     for mine, ref in (("bi_x", T.bi_x), ("bi_y", T.bi_y), ("ip_x", T.ip_x), ("ip_y", T.ip_y)):
-        assert rel_max(luo.get(mine)[sel], ref[sel]) < 1e-13, mine
+        assert np.array_equal(luo.get(mine)[sel], ref[sel]), mine
+    selp = np.nonzero((T.ghostTagsP > 0) | (T.hybridTagsP > 0))[0]
+    for mine, ref in (("bip_x", T.bip_x), ("bip_y", T.bip_y), ("ipp_x", T.ipp_x), ("ipp_y", T.ipp_y)):
+        assert np.array_equal(luo.get(mine)[selp], ref[selp]), mine
 
 
 def test_interpolation_against_oracle(luo):
@@ -93,7 +96,7 @@ def test_interpolation_against_oracle(luo):
     sel = np.nonzero(T.ghostTagsUV > 0)[0]
     for S, part in ((S0, sel[sel < g.nU]), (S1, sel[sel >= g.nU])):
         assert np.array_equal(gi[part].T, S.index[:, part])
-        assert rel_max(gc[part].T, S.coef[:, part]) < RTOL_W
+        assert rel_max(gc[part].T, S.coef[:, part]) <= RTOL_W
     luo.run("hybrid_velocity")
     us = np.zeros(g.nUV)
     us, H0 = oracle.hybrid_velocity(0, ug, us, T, ub, g, bb)
@@ -101,8 +104,10 @@ def test_interpolation_against_oracle(luo):
     sel = np.nonzero(T.hybridTagsUV > 0)[0]
     assert rel_max(luo.get("ustar")[sel], us[sel]) < RTOL_KERNEL
     hi = luo.get("hybrid_uv_index").reshape(-1, 4)
+    hc = luo.get("hybrid_uv_coef").reshape(-1, 4)
     for S, part in ((H0, sel[sel < g.nU]), (H1, sel[sel >= g.nU])):
         assert np.array_equal(hi[part].T, S.index[:, part])
+        assert rel_max(hc[part].T, S.coef[:, part]) <= RTOL_W
     # velocity blend and inside velocity
     uh = 1.0 + 0.2 * rng.standard_normal(g.nUV)
     luo.set("uhat", uh)
@@ -129,7 +134,10 @@ def test_pressure_interpolation_against_oracle(luo):
     gi = luo.get("ghost_p_index").reshape(-1, 4)
     sel = np.nonzero(T.ghostTagsP > 0)[0]
     assert np.array_equal(gi[sel].T, G.index[:, sel])
-    assert rel_max(luo.get("ghost_p_coef").reshape(-1, 4)[sel].T, G.coef[:, sel]) < RTOL_W
+    assert rel_max(luo.get("ghost_p_coef").reshape(-1, 4)[sel].T, G.coef[:, sel]) <= RTOL_W
+    hsel = np.nonzero(T.hybridTagsP > 0)[0]
+    assert np.array_equal(luo.get("hybrid_p_index").reshape(-1, 4)[hsel].T, H.index[:, hsel])
+    assert rel_max(luo.get("hybrid_p_coef").reshape(-1, 4)[hsel].T, H.coef[:, hsel]) <= RTOL_W
     assert dt > 0
 
 

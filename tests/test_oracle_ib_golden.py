@@ -12,6 +12,14 @@ import oracle
 CASES = ["ib_circle48", "ib_circle101"]
 
 
+@pytest.fixture(autouse=True)
+def reference_intercepts():
+    """These fixtures come from the reference's own kernels, which compute the body
+    intercepts in trigonometric form: the oracle tags in that form here."""
+    with oracle.intercept_form(0):
+        yield
+
+
 def bits_equal(a, b):
     a, b = np.asarray(a), np.asarray(b)
     return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
@@ -113,3 +121,45 @@ def test_blend_inside_robin_force(case):
     assert bits_equal(xp, z["xp_robin"])
     fx, fy = oracle.force(z["u_ghost"], z["uold_in"], z["p_in"], T, float(z["nu"]), g, float(z["dt"]), z["bb"])
     assert np.allclose([fx, fy], z["force"], rtol=1e-12, atol=1e-14)
+
+
+ULP_INTERCEPT = 8  # closed form vs the reference's acos/sin/tan form, ulp of the coordinate
+
+
+def test_closed_form_intercepts_follow_the_reference(case):
+    """The closed form b cos(th) = (p^2 + b^2 - o^2) / (2p) that the GPU and the oracle's
+    default use, against the reference's trigonometric form (whose outputs these fixtures
+    hold): the same tags, intercepts and image points within ULP_INTERCEPT ulp of the
+    coordinate, interpolation weights within 1e-9 of the weight scale."""
+    z, g, _ = case
+    with oracle.intercept_form(1):
+        T = oracle.tag_points(g, z["bx"], z["by"], z["uB"], z["vB"], z["bb"], float(z["midX"]), float(z["midY"]))
+    for name in ("ghostTagsUV", "hybridTagsUV", "hybridTagsUV2", "ghostTagsP", "hybridTagsP"):
+        assert np.array_equal(getattr(T, name), z["tag_" + name]), name
+    worst = 0.0
+    for mine, ref in (("bi_x", "body_intercept_x"), ("bi_y", "body_intercept_y"), ("ip_x", "image_point_x"),
+                      ("ip_y", "image_point_y"), ("bip_x", "body_intercept_p_x"), ("bip_y", "body_intercept_p_y"),
+                      ("ipp_x", "image_point_p_x"), ("ipp_y", "image_point_p_y")):
+        a, b = getattr(T, mine), z["tag_" + ref]
+        scale = np.spacing(np.maximum(np.abs(b), 1.0))  # ulp of an O(1) coordinate
+        err = np.max(np.abs(a - b) / scale)
+        worst = max(worst, err)
+        assert err <= ULP_INTERCEPT, (mine, err)
+    assert worst > 0  # the two forms are different computations
+    # stencils: an image point within a few ulp of a grid line lies on the edge of two
+    # cells, and the last bit decides which one the fit uses (in the reference too, whose
+    # GPU and host trigonometry differ there); such ties are left out of the comparison
+    u = z["u_in"]
+    _, S = oracle.ghost_velocity(0, u, T, float(z["uB"][0]), g, z["bb"])
+    sel = _nodes(T.ghostTagsUV)
+    sel = sel[sel < g.nU]
+    ipx, ipy = z["tag_image_point_x"][sel], z["tag_image_point_y"][sel]
+    near = lambda v, lines: np.min(np.abs(v[:, None] - lines[None, :]), axis=1) <= \
+        ULP_INTERCEPT * np.spacing(np.maximum(np.abs(v), 1.0))
+    tie = near(ipx, g.xu) | near(ipy, g.yu)
+    assert tie.sum() <= 2
+    keep = sel[~tie]
+    for k in range(4):
+        assert np.array_equal(S.index[k][keep], z["ghost0_index%d" % (k + 1)][keep])
+        ref = z["ghost0_q%dcoef" % (k + 1)][keep]
+        assert np.max(np.abs(S.coef[k][keep] - ref)) <= 1e-9 * max(1.0, np.max(np.abs(ref)))

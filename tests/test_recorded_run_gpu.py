@@ -11,8 +11,14 @@ above the recording in the first steps and about 11 % off (median over the first
 300 steps where |Fx| > 0.05; up to 80 % next to sign changes) later; the restatement's
 kernels are bit-exact against the reference's own kernel code, so the gap lies in
 what the recording ran (its CUSP solves, whose iterates are not reproducible here,
-or the code version it was made with).  The forces are checked for their sign
-pattern and size only."""
+or the code version it was made with).  The recording itself shows that it came
+from a different build: iterations_init has 2000 rows for 1000 steps, every time
+step written twice (rows "1 2 7", "1 2 7", "2 2 15", "2 2 15", ...), where the
+shipped code writes one row per step - NavierStokesSolver::writeCommon
+(NavierStokesSolver.cu:350) is the only writer, reached once per step through
+luoIBM::writeData -> luoIBM::writeCommon -> luo_base::writeCommon
+(luoIBM.cu:69-89, luo_base.cu:180-182).  The forces are checked for their sign
+pattern and size only; the body motion exactly."""
 import os
 
 import numpy as np

@@ -68,3 +68,14 @@ def test_noalloc_force_rejects_oversized_box():
                                   dummy, None)
     assert st == cb.ERR_BAD_INPUT
     assert b"exceeds the limit" in L.cuibm_case_error()
+
+
+@pytest.mark.parametrize("box", [(10, 10, 20, 89), (10, 10, 89, 20)])
+def test_noalloc_force_rejects_box_at_grid_edge(box):
+    """A box whose north edge reaches row ny - 1 (v has rows 0..ny-2) or whose east edge
+    reaches column nx - 1 (u has columns 0..nx-2) would read past the arrays."""
+    L = cb.library()
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the range check fails first
+    st = L.cuibm_cv_force_noalloc(dummy, dummy, dummy, dummy, dummy, dummy, 100, 100, *box, 0.01, 0.01, dummy, None)
+    assert st == cb.ERR_BAD_INPUT
+    assert b"out of range" in L.cuibm_case_error()
