@@ -1,0 +1,110 @@
+"""Whole runs of the benchmark configurations on the GPU against the FP64 oracle's
+runs of the same configurations (tests/golden/config_*.npz, written by
+tests/golden/make_config_runs.py with both systems solved by sparse LU).
+
+  lid-driven cavity 64 x 64, Re 100, dt 0.01, plain method, Poisson by CG + smoothed
+      aggregation: u and p after 100 and 1000 steps within FIELD_L2 relative L2;
+  impulsively started cylinder Re 40, 270 x 270, 157 points, external method, dt 0.01:
+      C_D and C_L of every one of 2000 steps within COEF, u and p after 500 and 2000
+      steps within FIELD_L2;
+  cylinder Re 550, 922 x 922, 629 points, external method, dt 0.002, both solves at the
+      configuration's relative tolerance 1e-8, plain FP64 and mixed precision (FP32
+      multigrid cycles inside the FP64 Krylov loop): C_D and C_L of steps 1-40 within
+      COEF of the FP64 oracle's, fields on every 8th node within FIELD_MIXED.
+
+For the first two the GPU solves to SOLVE_TOL, so that what is compared is the
+discretisation both sides share, not where each Krylov solve happened to stop."""
+import os
+
+import numpy as np
+import pytest
+
+cb = pytest.importorskip("cuibm_gb300")
+from cuibm_gb300 import cases  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+SOLVE_TOL = 1e-13   # relative residual of both GPU solves in the tightly solved runs
+FIELD_L2 = 1e-9     # relative L2 of u and p against the oracle
+COEF = 1e-6         # drag and lift coefficients, every step
+FIELD_MIXED = 1e-6  # Re 550 at the configuration's solver tolerance 1e-8, relative L2 of the subsample
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def golden(golden_dir, name):
+    path = os.path.join(golden_dir, name + ".npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture %s not generated" % name)
+    return np.load(path)
+
+
+def test_cavity64_1000_steps(tmp_path, golden_dir):
+    z = golden(golden_dir, "config_cavity64")
+    f = cases.cavity(str(tmp_path / "c"), n=64, nu=0.01, dt=0.01, nt=1000, vel_tol=SOLVE_TOL, pois_tol=SOLVE_TOL,
+                     pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG")
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.initialise()
+        done = 0
+        for k in (100, 1000):
+            s.stepTime(k - done)
+            done = k
+            eu, ep = rel_l2(s.get("u"), z["u_%d" % k]), rel_l2(s.get("p"), z["p_%d" % k])
+            assert eu < FIELD_L2 and ep < FIELD_L2, (k, eu, ep)
+
+
+def test_cylinder_re40_2000_steps(tmp_path, golden_dir):
+    z = golden(golden_dir, "config_cylinder_re40")
+    f = cases.cylinder(str(tmp_path / "c"), h=0.02, ratio=1.03, points=157, nu=1.0 / 40, dt=0.01, nt=2000,
+                       vel_tol=SOLVE_TOL, pois_tol=SOLVE_TOL, pois_pc="SMOOTHED_AGGREGATION")
+    cd, cl = [], []
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.initialise()
+        assert (s.info.nx, s.info.ny) == (270, 270)
+        for k in range(1, 2001):
+            s.stepTime(1)
+            fx, fy = s.forces()
+            cd.append(2 * fx)
+            cl.append(2 * fy)
+            if k in (500, 2000):
+                eu, ep = rel_l2(s.get("u"), z["u_%d" % k]), rel_l2(s.get("p"), z["p_%d" % k])
+                assert eu < FIELD_L2 and ep < FIELD_L2, (k, eu, ep)
+    dcd = np.max(np.abs(np.array(cd) - z["cd"]))
+    dcl = np.max(np.abs(np.array(cl) - z["cl"]))
+    assert dcd < COEF and dcl < COEF, (dcd, dcl)
+
+
+def subsample(info, u, p, stride):
+    nx, ny, nU = info.nx, info.ny, info.numU
+    uu = u[:nU].reshape(ny, nx - 1)[::stride, ::stride].ravel()
+    vv = u[nU:].reshape(ny - 1, nx)[::stride, ::stride].ravel()
+    return np.concatenate([uu, vv]), p.reshape(ny, nx)[::stride, ::stride].ravel()
+
+
+@pytest.mark.parametrize("precision", [None, "MIXED"])
+def test_cylinder_re550_40_steps_against_fp64_oracle(tmp_path, golden_dir, precision):
+    z = golden(golden_dir, "config_cylinder_re550")
+    f = cases.cylinder(str(tmp_path / "c"), h=0.005, ratio=1.01, points=629, nu=1.0 / 550, dt=0.002, nt=40,
+                       vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", precision=precision)
+    cd, cl = [], []
+    with cb.NavierStokesSolver(f) as s:
+        s.set_option("write_output", 0)
+        s.initialise()
+        assert (s.info.nx, s.info.ny, s.info.total_points) == (922, 922, 629)
+        for _ in range(40):
+            s.stepTime(1)
+            fx, fy = s.forces()
+            cd.append(2 * fx)
+            cl.append(2 * fy)
+        us, ps = subsample(s.info, s.get("u"), s.get("p"), int(z["stride"]))
+    dcd = np.max(np.abs(np.array(cd) - z["cd"]))
+    dcl = np.max(np.abs(np.array(cl) - z["cl"]))
+    eu, ep = rel_l2(us, z["u_sub"]), rel_l2(ps, z["p_sub"])
+    print("Re 550 %s vs FP64 oracle: max |dC_D| %.2e, max |dC_L| %.2e, u %.2e, p %.2e"
+          % (precision or "FP64", dcd, dcl, eu, ep))
+    assert dcd < COEF and dcl < COEF, (dcd, dcl)
+    assert eu < FIELD_MIXED and ep < FIELD_MIXED, (eu, ep)
