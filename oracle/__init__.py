@@ -671,7 +671,7 @@ class LuoSolver:
     luo_base.cu:255-264.  solve='direct' solves both systems exactly;
     solve='krylov' uses BiCGSTAB with the case's preconditioners and tolerances."""
 
-    def __init__(self, folder, solve="direct"):
+    def __init__(self, folder, solve="direct", vel_offset=None):
         sim, flow, dom, bodies = load_case(folder)
         self.sim = sim[0]
         g = self.g = Grid(dom)
@@ -710,8 +710,12 @@ class LuoSolver:
         xnew, unew = self.motion(0)
         self.bx = np.array([xnew + v for v in self.bdx])
         self.by = Y.copy()
-        self.uB = np.full(n, unew)
-        self.vB = np.zeros(n)
+        # per-point offsets of the body velocity (u, v), added wherever the prescribed motion
+        # sets it (a perturbation for derivative checks; zero in the reference's model)
+        ou, ov = (np.zeros(n), np.zeros(n)) if vel_offset is None else (f64(vel_offset[0]), f64(vel_offset[1]))
+        self.vel_offset = (ou.copy(), ov.copy())
+        self.uB = np.full(n, unew) + ou
+        self.vB = np.zeros(n) + ov
         self.uBk = np.full(n, self.coef["uCoefficient"] * np.cos(
             2 * np.pi * self.coef["xfrequency"] * (0 - self.dt) + self.coef["uPhase"]))
         self.midX, self.midY = xnew, my
@@ -773,7 +777,7 @@ class LuoSolver:
             return
         xnew, unew = self.motion(self.timeStep)
         self.bx = np.array([xnew + v for v in self.bdx])
-        self.uB = np.full(len(self.bx), unew)
+        self.uB = np.full(len(self.bx), unew) + self.vel_offset[0]
         self.midX = xnew
 
     def _update_solver(self):
@@ -960,8 +964,8 @@ class EmbeddedSolver(LuoSolver):
     later steps of the reference reuse its previous sorted COO arrays without clearing
     the LHS1 values, which this restatement does not reproduce)."""
 
-    def __init__(self, folder, solve="direct"):
-        super().__init__(folder, solve="none")
+    def __init__(self, folder, solve="direct", vel_offset=None):
+        super().__init__(folder, solve="none", vel_offset=vel_offset)
         g = self.g
         # luo_iter::initialise (luo_base::initialise) does not set the inside velocity
         f0 = load_case(folder)[1][0]

@@ -5,8 +5,8 @@ tests/golden/make_config_runs.py with both systems solved by sparse LU).
   lid-driven cavity 64 x 64, Re 100, dt 0.01, plain method, Poisson by CG + smoothed
       aggregation: u and p after 100 and 1000 steps within FIELD_L2 relative L2;
   impulsively started cylinder Re 40, 270 x 270, 157 points, external method, dt 0.01:
-      C_D and C_L of every one of 2000 steps within COEF, u and p after 500 and 2000
-      steps within FIELD_L2;
+      C_D and C_L of every one of 2000 steps within COEF, u and p after 2000 steps
+      within FIELD_L2;
   cylinder Re 550, 922 x 922, 629 points, external method, dt 0.002, both solves at the
       configuration's relative tolerance 1e-8, plain FP64 and mixed precision (FP32
       multigrid cycles inside the FP64 Krylov loop): C_D and C_L of steps 1-40 within
@@ -53,6 +53,7 @@ def test_cavity64_1000_steps(tmp_path, golden_dir):
             s.stepTime(k - done)
             done = k
             eu, ep = rel_l2(s.get("u"), z["u_%d" % k]), rel_l2(s.get("p"), z["p_%d" % k])
+            print("cavity 64 step %d vs FP64 oracle: u %.2e, p %.2e" % (k, eu, ep))
             assert eu < FIELD_L2 and ep < FIELD_L2, (k, eu, ep)
 
 
@@ -70,11 +71,12 @@ def test_cylinder_re40_2000_steps(tmp_path, golden_dir):
             fx, fy = s.forces()
             cd.append(2 * fx)
             cl.append(2 * fy)
-            if k in (500, 2000):
+            if k == 2000:
                 eu, ep = rel_l2(s.get("u"), z["u_%d" % k]), rel_l2(s.get("p"), z["p_%d" % k])
-                assert eu < FIELD_L2 and ep < FIELD_L2, (k, eu, ep)
     dcd = np.max(np.abs(np.array(cd) - z["cd"]))
     dcl = np.max(np.abs(np.array(cl) - z["cl"]))
+    print("Re 40 step 2000 vs FP64 oracle: u %.2e, p %.2e, max |dC_D| %.2e, max |dC_L| %.2e" % (eu, ep, dcd, dcl))
+    assert eu < FIELD_L2 and ep < FIELD_L2, (eu, ep)
     assert dcd < COEF and dcl < COEF, (dcd, dcl)
 
 
