@@ -38,7 +38,7 @@ _FIELD_NAMES = [
     "ghost_uv_index", "ghost_uv_coef", "hybrid_uv_index", "hybrid_uv_coef",
     "ghost_p_index", "ghost_p_coef", "hybrid_p_index", "hybrid_p_coef",
     "image_value_uv", "cfl", "work_x", "work_y", "solve_trace", "body_motion",
-    "surface_force", "forces",
+    "surface_force", "forces", "body_velocity_offset",
 ]
 FIELDS = {n: i for i, n in enumerate(_FIELD_NAMES)}
 _INT_FIELDS = {"ghost_tags_uv", "hybrid_tags_uv", "hybrid_tags_uv2", "ghost_tags_p", "hybrid_tags_p",
@@ -49,6 +49,7 @@ _OP_NAMES = [
     "weight_pressure", "project", "project_velocity", "update_body", "apply_lhs1", "apply_lhs2", "tag_points",
     "ghost_velocity_u", "ghost_velocity_uhat", "hybrid_velocity", "hybrid_pressure", "ghost_pressure",
     "set_inside", "robin_boundary", "force", "cfl", "surface_force", "surface_force_corrected",
+    "apply_lhs1_t", "apply_lhs2_t",
 ]
 OPS = {n: i for i, n in enumerate(_OP_NAMES)}
 
@@ -73,6 +74,11 @@ class Info(ctypes.Structure):
                                             "nnz_lhs1", "nnz_lhs2", "velocity_precond", "poisson_precond",
                                             "velocity_krylov", "poisson_krylov", "amg_levels",
                                             "velocity_precision", "poisson_precision", "sa_rebuilds")]
+
+
+class AdjointStats(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double)] + [(n, ctypes.c_longlong) for n in (
+        "forward_steps", "tape_steps", "velocity_iterations", "poisson_iterations")]
 
 
 _lib = None
@@ -114,6 +120,7 @@ def library():
         L.cuibm_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.cuibm_cv_force_noalloc.argtypes = [vp, vp, vp, vp, vp, vp, ip, ip, ip, ip, ip, ip, ctypes.c_double,
                                              ctypes.c_double, vp, vp]
+        L.cuibm_adjoint.argtypes = [vp, ip, ip, dp, dp, dp, dp, ctypes.c_size_t, ctypes.POINTER(AdjointStats)]
         L.cuibm_batch_create.argtypes = [ip, ctypes.POINTER(cp), ip, ctypes.POINTER(cp), ip, ctypes.POINTER(vp)]
         L.cuibm_batch_initialise.argtypes = [vp]
         L.cuibm_batch_step.argtypes = [vp, ip]
@@ -195,6 +202,24 @@ class NavierStokesSolver:
     def __exit__(self, *exc):
         self.close()
 
+    # ---- discrete adjoint (embedded method, prescribed motion) ---------------
+    def adjoint(self, nsteps, wx, wy=None, snapshots=64):
+        """Gradients of J = sum_n wx[n] Fx^n + wy[n] Fy^n over steps 1..nsteps from the
+        initial condition (cuibm_adjoint): returns (J, grad, stats) with grad =
+        [dJ/dnu, dJ/duCoefficient, dJ/d(u offsets of the points)..., dJ/d(v offsets)...]."""
+        nb = self.info.total_points
+        wx = np.ascontiguousarray(np.broadcast_to(np.asarray(wx, np.float64), (nsteps,)))
+        wy = np.ascontiguousarray(np.zeros(nsteps) if wy is None else np.broadcast_to(np.asarray(wy, np.float64),
+                                                                                      (nsteps,)))
+        grad = np.zeros(2 + 2 * nb)
+        J = ctypes.c_double()
+        st = AdjointStats()
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self._L.cuibm_adjoint(self._h, int(nsteps), int(snapshots), wx.ctypes.data_as(dp),
+                                          wy.ctypes.data_as(dp), ctypes.byref(J), grad.ctypes.data_as(dp),
+                                          grad.size, ctypes.byref(st)))
+        return J.value, grad, {k: getattr(st, k) for k, _ in AdjointStats._fields_}
+
     # ---- data access ---------------------------------------------------------
     def get_info(self):
         info = Info()
@@ -208,7 +233,7 @@ class NavierStokesSolver:
                  "x": nx, "dx": nx, "xu": nx - 1, "xv": nx, "y": ny, "dy": ny, "yu": ny, "yv": ny - 1,
                  "body_x": nb, "body_y": nb, "body_uB": nb, "body_vB": nb,
                  "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024,
-                 "body_motion": 12, "surface_force": 3 * nb + 2, "forces": 2}
+                 "body_motion": 12, "surface_force": 3 * nb + 2, "forces": 2, "body_velocity_offset": 2 * nb}
         if name in sizes:
             return sizes[name]
         if name in ("p", "p_old", "rhs2", "ghost_tags_p", "hybrid_tags_p", "bip_x", "bip_y", "ipp_x", "ipp_y",

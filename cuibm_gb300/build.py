@@ -35,6 +35,7 @@ UNITS = {
     "krylov.cu": [],
     "amg.cu": [],
     "fused_solve.cu": [],
+    "adjoint.cu": [],
     "fadlun.cu": ["-fmad=false"],
     "embedded.cu": ["-fmad=false"],
     "ib_kernels.cu": ["-fmad=false"],

@@ -555,4 +555,120 @@ void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z)
     CUIBM_TRY(cudaGetLastError());
 }
 
+// ---- the transposed cycle (discrete adjoint) ----------------------------------------
+// The Galerkin hierarchy of A^T with the same prolongators is the transposed one:
+// P^T A^T P = (P^T A P)^T, so a V-cycle for A^T needs only the transposed level
+// matrices and the transposed coarsest inverse.  They are made from the forward
+// hierarchy the first time the adjoint asks (and again after a rebuild), in blocks that
+// go with the hierarchy.
+static void *sa_block(LinearSystem &S, size_t bytes)
+{
+    void *p = nullptr;
+    CUIBM_TRY(cudaMalloc(&p, std::max<size_t>(1, bytes)));
+    S.sa_blocks.push_back(p);
+    return p;
+}
+
+void ensure_transposed_levels(Context &c, LinearSystem &S)
+{
+    for (size_t l = 0; l < S.amg.size(); ++l) {
+        SaLevel *L = S.amg[l];
+        if (l > 0 && !L->AT.ptr) {
+            HostCsr H;
+            H.n = H.m = L->A.n;
+            H.ptr.resize(H.n + 1);
+            H.col.resize(L->A.nnz);
+            H.val.resize(L->A.nnz);
+            CUIBM_TRY(cudaMemcpyAsync(H.ptr.data(), L->A.ptr, H.ptr.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                      c.stream));
+            if (L->A.nnz) {
+                CUIBM_TRY(cudaMemcpyAsync(H.col.data(), L->A.col, H.col.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                          c.stream));
+                CUIBM_TRY(cudaMemcpyAsync(H.val.data(), L->A.val, H.val.size() * sizeof(double),
+                                          cudaMemcpyDeviceToHost, c.stream));
+            }
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            const HostCsr T = transpose(H);
+            DevCsr D;
+            D.n = T.n;
+            D.nnz = (int)T.col.size();
+            D.ptr = static_cast<int *>(sa_block(S, T.ptr.size() * sizeof(int)));
+            D.col = static_cast<int *>(sa_block(S, T.col.size() * sizeof(int)));
+            D.val = static_cast<double *>(sa_block(S, T.val.size() * sizeof(double)));
+            CUIBM_TRY(cudaMemcpyAsync(D.ptr, T.ptr.data(), T.ptr.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                      c.stream));
+            if (D.nnz) {
+                CUIBM_TRY(cudaMemcpyAsync(D.col, T.col.data(), T.col.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                          c.stream));
+                CUIBM_TRY(cudaMemcpyAsync(D.val, T.val.data(), T.val.size() * sizeof(double),
+                                          cudaMemcpyHostToDevice, c.stream));
+            }
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            L->AT = D;
+        }
+        if (L->coarse_inv && !L->coarse_inv_t) {
+            const size_t n = L->n;
+            std::vector<double> a(n * n), t(n * n);
+            CUIBM_TRY(cudaMemcpyAsync(a.data(), L->coarse_inv, a.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                      c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            for (size_t i = 0; i < n; ++i)
+                for (size_t j = 0; j < n; ++j) t[j * n + i] = a[i * n + j];
+            L->coarse_inv_t = static_cast<double *>(sa_block(S, t.size() * sizeof(double)));
+            CUIBM_TRY(cudaMemcpyAsync(L->coarse_inv_t, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                      c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        }
+    }
+}
+
+struct Lvl0T {
+    int which;
+    Op1T a1;
+    Op2T a2;
+    template <class X>
+    __device__ __forceinline__ double row(int i, const X &x) const
+    {
+        return which == 1 ? a1.row(i, x) : a2.row(i, x);
+    }
+};
+
+// z = the V-cycle of launch_vcycle for A^T: every level operator transposed (level 0: the
+// matrix-free A^T of the transposed lists T).  S holds the forward hierarchy and the
+// gate (the status of the solve it serves).
+void launch_vcycle_transposed(Context &c, LinearSystem &S, const TransposeList &T, const double *r, double *z)
+{
+    const int nl = (int)S.amg.size();
+    const int *gate = &S.ks->status;
+    Lvl0T A0{S.which, Op1T{c.l1, c.g, T}, Op2T{c.l2, c.g, T}};
+    const double *bl = r;
+    for (int l = 0; l < nl - 1; ++l) {
+        SaLevel *L = S.amg[l];
+        if (l == 0)
+            k_sa_down<<<blocks_for(L->n), kBlock, 0, c.stream>>>(A0, L->n, bl, L->dinv, L->omega, L->x, L->r, gate);
+        else
+            k_sa_down<<<blocks_for(L->n), kBlock, 0, c.stream>>>(CsrRow{L->AT}, L->n, bl, L->dinv, L->omega, L->x,
+                                                                 L->r, gate);
+        k_csr_mv<false><<<blocks_for(L->R.n), kBlock, 0, c.stream>>>(L->R, L->r, S.amg[l + 1]->b, gate);
+        bl = S.amg[l + 1]->b;
+    }
+    SaLevel *C = S.amg[nl - 1];
+    double *xc = (nl == 1) ? z : C->x;
+    k_dense_mv<<<(C->n + 7) / 8, 256, 0, c.stream>>>(C->n, C->coarse_inv_t, nl == 1 ? r : C->b, xc, gate);
+    const double *xup = xc;
+    for (int l = nl - 2; l >= 0; --l) {
+        SaLevel *L = S.amg[l];
+        k_csr_mv<true><<<blocks_for(L->P.n), kBlock, 0, c.stream>>>(L->P, xup, L->x, gate);
+        double *out = (l == 0) ? z : L->t;
+        const double *bb = (l == 0) ? r : L->b;
+        if (l == 0)
+            k_sa_up<<<blocks_for(L->n), kBlock, 0, c.stream>>>(A0, L->n, bb, L->dinv, L->omega, L->x, out, gate);
+        else
+            k_sa_up<<<blocks_for(L->n), kBlock, 0, c.stream>>>(CsrRow{L->AT}, L->n, bb, L->dinv, L->omega, L->x, out,
+                                                               gate);
+        xup = out;
+    }
+    CUIBM_TRY(cudaGetLastError());
+}
+
 }  // namespace cuibm

@@ -21,6 +21,10 @@ struct SaLevel {
     // for the persistent cycle (fused_solve.cu), levels with a coarser one:
     double *wd = nullptr;  // omega * D^-1 (the damped-Jacobi weights)
     DevCsr AP;             // A_l P_l: the upward sweep's residual without neighbour values
+    // for the transposed cycle of the discrete adjoint (built on first use): A_l^T on the
+    // levels below the finest, the transposed dense inverse on the coarsest
+    DevCsr AT;
+    double *coarse_inv_t = nullptr;
 };
 
 }  // namespace cuibm

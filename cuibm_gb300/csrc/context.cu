@@ -142,7 +142,7 @@ static bool strong_coupling(const Context &c) { return is_ib(c) && c.P.VIV == 2;
 // first: the step's first pass, which moves N to Nold; the later passes of a strongly
 // coupled step keep Nold and restart from u = uold (luoIBM/intermediateVelocity.cu:33,
 // luo_iter/intermediateVelocity.cu:29; the Fadlun method has no such reset)
-static void phase_generate_rhs1(Context &c, bool first)
+void phase_generate_rhs1(Context &c, bool first)
 {
     PhaseTimer t(c, "Intermediate Velocity Setup");
     if (!first && (is_luo(c) || is_embedded(c))) launch_copy(c, c.u, c.uold, c.g.nUV);
@@ -154,13 +154,13 @@ static void phase_generate_rhs1(Context &c, bool first)
     if (is_fadlun(c)) launch_fadlun_rhs1(c);  // updateRHS1forIBX/Y
 }
 
-static void phase_solve_velocity(Context &c, bool in_graph)
+void phase_solve_velocity(Context &c, bool in_graph)
 {
     PhaseTimer t(c, "Intermediate Velocity Solve");
     launch_solve(c, c.sys1, c.rhs1, c.uhat, in_graph);
 }
 
-static void phase_generate_rhs2(Context &c)
+void phase_generate_rhs2(Context &c)
 {
     PhaseTimer t(c, "Poisson Setup");
     if (is_fadlun(c))
@@ -169,7 +169,7 @@ static void phase_generate_rhs2(Context &c)
         launch_rhs2(c, c.uhat);
 }
 
-static void phase_solve_poisson(Context &c, bool in_graph)
+void phase_solve_poisson(Context &c, bool in_graph)
 {
     PhaseTimer t(c, "Poisson Solve");
     launch_solve(c, c.sys2, c.rhs2, c.p, in_graph);
@@ -569,20 +569,42 @@ static void rebuild_hierarchies(Context &c)
     if (rebuilt && c.use_graph) build_step_graph(c);
 }
 
+}  // extern "C"
+
+namespace cuibm {
+
+// one time step as cuibm_step runs it: the step graph (or the phases one by one), the
+// host's step count, and a rebuilt SA hierarchy when the embedded rows' pattern changed
+void step_once(Context &c)
+{
+    if (c.use_graph && !c.profile_phases && c.step_exec)
+        CUIBM_TRY(cudaGraphLaunch(c.step_exec, c.stream));
+    else
+        record_step(c, false);
+    c.timeStep++;
+    if (c.sa_rebuild) ::rebuild_hierarchies(c);
+}
+
+// the step error word of the steps enqueued so far (0: every solve converged)
+int read_step_error(Context &c)
+{
+    int errw = 0;
+    CUIBM_TRY(cudaMemcpyAsync(&errw, c.err_word, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    return errw;
+}
+
+}  // namespace cuibm
+
+extern "C" {
+
 int cuibm_step(cuibm_ctx *h, int nsteps)
 {
     if (!h || !h->c.initialised) return CUIBM_ERR_STATE;
     if (nsteps < 0) return fail(h, CUIBM_ERR_BAD_INPUT, "nsteps < 0");
     Context &c = h->c;
     CUIBM_GUARD(h, {
-        for (int s = 0; s < nsteps; ++s) {
-            if (c.use_graph && !c.profile_phases)
-                CUIBM_TRY(cudaGraphLaunch(c.step_exec, c.stream));
-            else
-                record_step(c, false);
-            c.timeStep++;
-            if (c.sa_rebuild) rebuild_hierarchies(c);
-        }
+        for (int s = 0; s < nsteps; ++s) step_once(c);
         if (!c.step_sync && nsteps > 0) return CUIBM_OK;  // enqueued only; checked by a later synchronising call
         int errw = 0;
         CUIBM_TRY(cudaMemcpyAsync(&errw, g_err_word_of(c), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -798,6 +820,8 @@ int cuibm_run(cuibm_ctx *h, int op)
         case CUIBM_OP_CFL: launch_cfl(c); break;
         case CUIBM_OP_SURFACE_FORCE: need_ib(); launch_surface_force(c, 1, false); break;
         case CUIBM_OP_SURFACE_FORCE_CORRECTED: need_ib(); launch_surface_force(c, 2, false); break;
+        case CUIBM_OP_APPLY_LHS1_T: apply_transposed(c, 1, c.work_x, c.work_y); break;
+        case CUIBM_OP_APPLY_LHS2_T: apply_transposed(c, 2, c.work_x, c.work_y); break;
         default: return fail(h, CUIBM_ERR_BAD_INPUT, "unknown operation " + std::to_string(op));
         }
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
@@ -883,6 +907,9 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
             c.force_method = m;
             if (c.initialised && c.use_graph) CUIBM_GUARD(h, { build_step_graph(c); });
         }
+    } else if (k == "adjoint_tolerance") {
+        if (!(value > 0 && value < 1)) return fail(h, CUIBM_ERR_BAD_INPUT, "adjoint_tolerance must lie in (0, 1)");
+        c.adjoint_rtol = value;
     } else return fail(h, CUIBM_ERR_BAD_INPUT, "unknown option " + k);
     return CUIBM_OK;
 }
@@ -1074,6 +1101,29 @@ int cuibm_case_array(const char *folder, int argc, const char **argv, int field,
 
 const char *cuibm_case_error(void) { return g_create_error.c_str(); }
 
+int cuibm_adjoint(cuibm_ctx *h, int nsteps, int snapshots, const double *wx, const double *wy, double *J,
+                  double *grad, size_t ngrad, cuibm_adjoint_stats *stats)
+{
+    if (!h || !h->c.initialised) return CUIBM_ERR_STATE;
+    if (!wx || !wy || !grad) return fail(h, CUIBM_ERR_BAD_INPUT, "null weights or gradient array");
+    Context &c = h->c;
+    CUIBM_GUARD(h, {
+        if (!(c.P.solverType == ST_OSC && c.has_body))
+            return fail(h, CUIBM_ERR_UNSUPPORTED,
+                        "the adjoint covers the embedded method (SolverType OSC_CYLINDER) with a body");
+        AdjointStats st{};
+        run_adjoint(c, nsteps, snapshots, wx, wy, J, grad, ngrad, c.adjoint_rtol, &st);
+        if (stats) {
+            stats->ms = st.ms;
+            stats->forward_steps = st.forward_steps;
+            stats->tape_steps = st.tape_steps;
+            stats->velocity_iterations = st.velocity_iterations;
+            stats->poisson_iterations = st.poisson_iterations;
+        }
+    });
+    return CUIBM_OK;
+}
+
 void cuibm_destroy(cuibm_ctx *h)
 {
     if (!h) return;
@@ -1086,6 +1136,7 @@ void cuibm_destroy(cuibm_ctx *h)
     free_sa_hierarchy(c.sys2);
     free_fused(c.sys1);
     free_fused(c.sys2);
+    free_adjoint(c);
     if (c.arena) cudaFree(c.arena);
     if (c.h_scalars) cudaFreeHost(c.h_scalars);
     if (c.ev0) cudaEventDestroy(c.ev0);

@@ -49,6 +49,7 @@ struct EmbGeom {
     const double *dx, *dy;
     const int *gUV, *gP;
     const double *uB, *vB;
+    const int *hUV, *hP;  // hybrid tags: a node tagged both ways takes the hybrid row
 };
 
 // 1/diagonal of the interior LHS1 rows (the ns_rhs of LHS1_mid_iter_X/Y's plain rows),
@@ -117,8 +118,11 @@ __global__ void k_emb_rows(EmbGeom G, IbPlan P, Context::EmbeddedRows E)
     const int nx = G.nx, ny = G.ny, nU = (nx - 1) * ny;
     if (cls == 0) {
         // ghost velocity (LHS1_mid_iter_X/Y ghost branch): 1 at the node, +w at the corners
-        // that are neither ghost nodes nor the node; the others go to interp_rhs
+        // that are neither ghost nodes nor the node; the others go to interp_rhs.  A node
+        // tagged hybrid as well takes the hybrid row (LHS1_mid_iter_X/Y test the hybrid tag
+        // first), so its ghost slot stays unused.
         const int n = P.gvNode[k];
+        if (G.hUV[n] > 0) return;
         int *pc = E.pcol1 + 5 * (size_t)k;
         double *pv = E.pval1 + 5 * (size_t)k;
         int m = 0, in = 0;
@@ -176,6 +180,7 @@ __global__ void k_emb_rows(EmbGeom G, IbPlan P, Context::EmbeddedRows E)
         // are neither ghost nodes nor the node; interp_rhs = dp/dn + sum_l w_l q_l over the
         // ghost corners, q_l = -(n_l . dU/dt), dp/dn = |node - image point| (n . dU/dt)
         const int ip = P.gpNode[k];
+        if (G.hP[ip] > 0) return;  // tagged hybrid as well: the hybrid row (LHS2_mid_iter's order)
         int *pc = E.pcol2 + 5 * (size_t)k;
         double *pv = E.pval2 + 5 * (size_t)k;
         int m = 0;
@@ -303,7 +308,8 @@ void launch_embedded_rows(Context &c)
     const IbPlan &P = ib_plan(c);
     CUIBM_TRY(cudaMemsetAsync(E.pid1, 0xff, c.g.nUV * sizeof(int), c.stream));
     CUIBM_TRY(cudaMemsetAsync(E.pid2, 0xff, c.g.nP * sizeof(int), c.stream));
-    EmbGeom G{c.g.nx, c.g.ny, c.P.dt, c.P.nu, c.dx, c.dy, c.ib.ghostUV, c.ib.ghostP, c.ib.uB, c.ib.vB};
+    EmbGeom G{c.g.nx,  c.g.ny,  c.P.dt,       c.P.nu,        c.dx, c.dy, c.ib.ghostUV, c.ib.ghostP,
+              c.ib.uB, c.ib.vB, c.ib.hybridUV, c.ib.hybridP};
     const int cap = std::max(P.cap_v, P.cap_p);
     k_emb_rows<<<dim3(blocks_for(cap), 4), kBlock, 0, c.stream>>>(G, P, E);
     CUIBM_TRY(cudaGetLastError());

@@ -53,6 +53,7 @@ void *field_pointer(Context &c, int f, size_t *bytes)
     case CUIBM_F_BODY_MOTION: return ret(b.motion, kMotionLen * D);
     case CUIBM_F_SURFACE_FORCE: return ret(b.surf, (3 * nb + 2) * D);
     case CUIBM_F_FORCES: return ret(b.forceOut, 2 * D);
+    case CUIBM_F_BODY_VELOCITY_OFFSET: return ret(b.velOff, 2 * nb * D);
     case CUIBM_F_GHOST_TAGS_UV: return ret(b.ghostUV, UV * I);
     case CUIBM_F_HYBRID_TAGS_UV: return ret(b.hybridUV, UV * I);
     case CUIBM_F_HYBRID_TAGS_UV2: return ret(b.hybrid2UV, UV * I);
@@ -92,6 +93,10 @@ void field_changed(Context &c, int f)
 {
     if (c.has_body && (f == CUIBM_F_BODY_X || f == CUIBM_F_BODY_Y || f == CUIBM_F_BODY_UB || f == CUIBM_F_BODY_VB))
         c.ib_dirty = true;
+    if (c.has_body && f == CUIBM_F_BODY_VELOCITY_OFFSET) {
+        if (!c.initialised) throw InputError("write body_velocity_offset after cuibm_initialise");
+        apply_velocity_offsets(c);
+    }
 }
 
 }  // namespace cuibm

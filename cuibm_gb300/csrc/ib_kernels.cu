@@ -1124,8 +1124,9 @@ __global__ void k_force_box(int nx, int ny, int I, int J, int ncx, int ncy, cons
 
 // prescribed motion (luo_base/move.cu set_movement): x = xnew + offset, uB = unew with
 // xnew, unew taken from a table of the host-evaluated motion indexed by the step
+// (plus the per-point velocity offset off[i], zero unless the caller set one)
 __global__ void k_body_motion(int total, const int *step, int table_len, const double *table, const double *bdx,
-                              double *bx, double *uB, double *motion)
+                              const double *off, double *bx, double *uB, double *motion)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int s = *step;
@@ -1133,7 +1134,7 @@ __global__ void k_body_motion(int total, const int *step, int table_len, const d
     const double xnew = table[2 * s], unew = table[2 * s + 1];
     if (i < total) {
         bx[i] = xnew + bdx[i];
-        uB[i] = unew;
+        uB[i] = unew + off[i];
     }
     if (i == 0) {
         motion[0] = xnew;
@@ -1340,6 +1341,7 @@ void setup_ib(Context &c)
     b.bdx = c.carve<double>(nb);
     b.bdy = c.carve<double>(nb);
     b.motion = c.carve<double>(kMotionLen);
+    b.velOff = c.carve<double>(2 * (size_t)nb);  // zero (the arena starts zeroed)
     b.forceOut = c.carve<double>(8);  // Fx, Fy, then the six partial sums
     b.surf = c.carve<double>(3 * (size_t)nb + 2);
     const int fblocks = 64;
@@ -1696,10 +1698,31 @@ void launch_body_motion(Context &c, double)
         return;
     }
     k_body_motion<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.step_counter_dev, H.table_len,
-                                                                     H.motion_table, c.ib.bdx, c.ib.bx, c.ib.uB,
-                                                                     c.ib.motion);
+                                                                     H.motion_table, c.ib.bdx, c.ib.velOff, c.ib.bx,
+                                                                     c.ib.uB, c.ib.motion);
     CUIBM_TRY(cudaGetLastError());
 }
+
+// the prescribed body velocity with new per-point offsets: uB = unew + offU, vB = offV
+__global__ void k_apply_velocity_offsets(int total, const double *off, const double *motion, double *uB, double *vB)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    uB[i] = motion[2] + off[i];
+    vB[i] = off[total + i];
+}
+
+void apply_velocity_offsets(Context &c)
+{
+    if (c.P.VIV) throw InputError("body velocity offsets apply to prescribed motion only (VIV: 0)");
+    k_apply_velocity_offsets<<<blocks_for(c.body.total), kBlock, 0, c.stream>>>(c.body.total, c.ib.velOff,
+                                                                                c.ib.motion, c.ib.uB, c.ib.vB);
+    CUIBM_TRY(cudaGetLastError());
+    // the embedded method's hybrid rows hold the body velocity in their right-hand side
+    if (c.emb.pid1) launch_embedded_rows(c);
+}
+
+const int *force_box_dev(Context &c) { return hostside(c).bb; }
 
 void launch_body_pre_step(Context &c)
 {

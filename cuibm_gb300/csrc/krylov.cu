@@ -701,4 +701,128 @@ int read_solve_status(Context &c, LinearSystem &S, int *iterations)
     return fs.abort ? KS_TIMEOUT : host.status;
 }
 
+// ---- transposed solves (discrete adjoint) -------------------------------------------
+__global__ void k_apply_op(Op1T A, int n, const double *__restrict__ x, double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = A.row(i, PtrAccess{x});
+}
+__global__ void k_apply_op(Op2T A, int n, const double *__restrict__ x, double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = A.row(i, PtrAccess{x});
+}
+
+// The transposed system S of the forward system F: its own Krylov vectors and scalars,
+// F's Jacobi table (A and A^T share their diagonal) and, for the Poisson system, F's SA
+// hierarchy.  Allocated with cudaMalloc (the context's arena is sized at initialise);
+// the pointers go to allocs for the caller to free.
+void setup_transposed_system(Context &c, const LinearSystem &F, LinearSystem &S, std::vector<void *> &allocs)
+{
+    auto dalloc = [&](size_t bytes) {
+        void *p = nullptr;
+        CUIBM_TRY(cudaMalloc(&p, bytes));
+        allocs.push_back(p);
+        return p;
+    };
+    S.which = F.which;
+    S.n = F.n;
+    S.krylov = KRYLOV_BICGSTAB;
+    S.precond = F.precond == PC_SMOOTHED_AGGREGATION && !F.amg.empty() ? PC_SMOOTHED_AGGREGATION : PC_DIAGONAL;
+    const size_t n = S.n;
+    double *blk = static_cast<double *>(dalloc(8 * n * sizeof(double)));
+    S.r = blk;
+    S.rs = blk + n;
+    S.p = blk + 2 * n;
+    S.Mp = blk + 3 * n;
+    S.AMp = blk + 4 * n;
+    S.s = blk + 5 * n;
+    S.Ms = blk + 6 * n;
+    S.AMs = blk + 7 * n;
+    S.z = S.Ms;
+    S.q = S.AMs;
+    S.dinv = F.dinv;
+    S.w = nullptr;
+    S.partials = static_cast<double *>(dalloc((4 * (size_t)blocks_for(S.n) + 4) * sizeof(double)));
+    S.ks = static_cast<KrylovScalars *>(dalloc(sizeof(KrylovScalars)));
+    KrylovScalars hk{};
+    hk.rtol = S.rtol;
+    hk.maxit = S.maxit;
+    hk.status = KS_CONVERGED;
+    CUIBM_TRY(cudaMemcpy(S.ks, &hk, sizeof(hk), cudaMemcpyHostToDevice));
+    S.amg = F.amg;
+}
+
+template <class Op>
+static void transposed_iterations(Context &c, LinearSystem &S, Op A, const TransposeList &T, const double *b,
+                                  double *x)
+{
+    const int n = S.n, nb = blocks_for(n);
+    const bool sa = S.precond == PC_SMOOTHED_AGGREGATION;
+    auto precond = [&](const double *in, double *out) { launch_vcycle_transposed(c, S, T, in, out); };
+    k_bicg_init<<<nb, kBlock, 0, c.stream>>>(A, n, b, x, S.r, S.rs, S.p, S.partials, S.ks, nullptr, S.which, 0, 0);
+    CUIBM_TRY(cudaGetLastError());
+    KrylovScalars host{};
+    const int chunk = 4;
+    for (int done = 0; done <= S.maxit + chunk; done += chunk) {
+        for (int k = 0; k < chunk; ++k) {
+            if (sa) {
+                precond(S.p, S.Mp);
+                k_bicg_1<Op, 2><<<nb, kBlock, 0, c.stream>>>(A, n, S.p, S.dinv, S.Mp, S.AMp, S.rs, S.partials, S.ks);
+            } else {
+                k_bicg_1<Op, 1><<<nb, kBlock, 0, c.stream>>>(A, n, S.p, S.dinv, S.Mp, S.AMp, S.rs, S.partials, S.ks);
+            }
+            k_bicg_2<<<nb, kBlock, 0, c.stream>>>(n, S.r, S.AMp, S.s, S.partials, S.ks);
+            if (sa) {
+                precond(S.s, S.Ms);
+                k_bicg_3<Op, 2><<<nb, kBlock, 0, c.stream>>>(A, n, S.s, S.dinv, S.Ms, S.AMs, S.partials, S.ks);
+            } else {
+                k_bicg_3<Op, 1><<<nb, kBlock, 0, c.stream>>>(A, n, S.s, S.dinv, S.Ms, S.AMs, S.partials, S.ks);
+            }
+            k_bicg_4<<<nb, kBlock, 0, c.stream>>>(n, x, S.r, S.rs, S.s, S.Mp, S.Ms, S.AMs, S.partials, S.ks,
+                                                  nullptr, S.which, 0, 0);
+            k_bicg_5<<<nb, kBlock, 0, c.stream>>>(n, S.p, S.r, S.AMp, S.ks);
+        }
+        CUIBM_TRY(cudaGetLastError());
+        CUIBM_TRY(cudaMemcpyAsync(&host, S.ks, sizeof(host), cudaMemcpyDeviceToHost, c.stream));
+        CUIBM_TRY(cudaStreamSynchronize(c.stream));
+        if (host.status != KS_RUNNING) break;
+    }
+}
+
+// A^T x = b for system S.which, warm-started from x; returns the KStatus and the
+// iteration count.  The Poisson system's preconditioner is the transposed cycle of the
+// forward SA hierarchy (the same aggregates and prolongators, transposed level matrices).
+int launch_solve_transposed(Context &c, LinearSystem &S, LinearSystem &F, const TransposeList &T, const double *b,
+                            double *x, int *iterations)
+{
+    S.amg = F.amg;  // the forward hierarchy (rebuilt for a moving body between steps)
+    if (S.precond == PC_SMOOTHED_AGGREGATION) ensure_transposed_levels(c, F);
+    KrylovScalars hk{};
+    CUIBM_TRY(cudaMemcpyAsync(&hk, S.ks, sizeof(hk), cudaMemcpyDeviceToHost, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    hk.rtol = S.rtol;
+    hk.maxit = S.maxit;
+    CUIBM_TRY(cudaMemcpyAsync(S.ks, &hk, sizeof(hk), cudaMemcpyHostToDevice, c.stream));
+    if (S.which == 1)
+        transposed_iterations(c, S, Op1T{c.l1, c.g, T}, T, b, x);
+    else
+        transposed_iterations(c, S, Op2T{c.l2, c.g, T}, T, b, x);
+    KrylovScalars host{};
+    CUIBM_TRY(cudaMemcpyAsync(&host, S.ks, sizeof(host), cudaMemcpyDeviceToHost, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+    if (iterations) *iterations = host.it;
+    return host.status;
+}
+
+// y = A^T x (which 1: LHS1, 2: LHS2)
+void launch_apply_transposed(Context &c, int which, const TransposeList &T, const double *x, double *y)
+{
+    if (which == 1)
+        k_apply_op<<<blocks_for(c.g.nUV), kBlock, 0, c.stream>>>(Op1T{c.l1, c.g, T}, c.g.nUV, x, y);
+    else
+        k_apply_op<<<blocks_for(c.g.nP), kBlock, 0, c.stream>>>(Op2T{c.l2, c.g, T}, c.g.nP, x, y);
+    CUIBM_TRY(cudaGetLastError());
+}
+
 }  // namespace cuibm

@@ -86,4 +86,82 @@ __device__ __forceinline__ double lhs2_row(const Lhs2Coef &c, const Grid &g, int
     return lhs2_row_f(c, g, i, PtrAccess{x});
 }
 
+// ---- transposed operators (discrete adjoint) ---------------------------------------
+// Row i of A^T is column i of A: the structured rows j next to i that are not patched
+// contribute their coefficient towards i (times the row scale of LHS1's embedded rows),
+// the diagonal is row i's own, and the patched rows holding column i are listed in
+// TransposeList (built by the adjoint for each tagging).
+struct Op1T {
+    Lhs1Coef c;
+    Grid g;
+    TransposeList T;
+    template <class X>
+    __device__ __forceinline__ double row(int i, const X &x) const
+    {
+        const RowPatch &P = c.patch;
+        auto patched = [&](int j) { return P.pid && P.pid[j] >= 0; };
+        auto rs = [&](int j) { return c.rscale ? c.rscale[j] : 1.0; };
+        const int ki = P.pid ? P.pid[i] : -1;
+        double y;
+        if (i < g.nU) {
+            const int w = g.nx - 1, I = i % w, J = i / w;
+            if (ki >= 0) y = P.pdiag[ki] * x(i);
+            else y = ((((1 + c.uE[I]) + c.uW[I]) + c.uN[J]) + c.uS[J]) * rs(i) * x(i);
+            if (I != 0 && !patched(i - 1)) y -= c.uE[I - 1] * rs(i - 1) * x(i - 1);
+            if (I != g.nx - 2 && !patched(i + 1)) y -= c.uW[I + 1] * rs(i + 1) * x(i + 1);
+            if (J != 0 && !patched(i - w)) y -= c.uN[J - 1] * rs(i - w) * x(i - w);
+            if (J != g.ny - 1 && !patched(i + w)) y -= c.uS[J + 1] * rs(i + w) * x(i + w);
+        } else {
+            const int k = i - g.nU, w = g.nx, I = k % w, J = k / w;
+            if (ki >= 0) y = P.pdiag[ki] * x(i);
+            else y = ((((1 + c.vE[I]) + c.vW[I]) + c.vN[J]) + c.vS[J]) * rs(i) * x(i);
+            if (I != 0 && !patched(i - 1)) y -= c.vE[I - 1] * rs(i - 1) * x(i - 1);
+            if (I != g.nx - 1 && !patched(i + 1)) y -= c.vW[I + 1] * rs(i + 1) * x(i + 1);
+            if (J != 0 && !patched(i - w)) y -= c.vN[J - 1] * rs(i - w) * x(i - w);
+            if (J != g.ny - 2 && !patched(i + w)) y -= c.vS[J + 1] * rs(i + w) * x(i + w);
+        }
+        if (T.cnt) {
+            const int n = T.cnt[i] < T.tmax ? T.cnt[i] : T.tmax;
+            for (int t = 0; t < n; ++t) {
+                const int e = T.ent[(size_t)i * T.tmax + t];
+                y += P.pval[e] * x(T.prow[e / 5]);
+            }
+        }
+        return y;
+    }
+};
+struct Op2T {
+    Lhs2Coef c;
+    Grid g;
+    TransposeList T;
+    template <class X>
+    __device__ __forceinline__ double row(int i, const X &x) const
+    {
+        const RowPatch &P = c.patch;
+        auto patched = [&](int j) { return P.pid && P.pid[j] >= 0; };
+        const int ki = P.pid ? P.pid[i] : -1;
+        const int I = i % g.nx, J = i / g.nx;
+        double y;
+        if (ki >= 0) {
+            y = P.pdiag[ki] * x(i);
+        } else {
+            double d = (((0 + c.E[I]) + c.W[I]) + c.N[J]) + c.S[J];
+            if (i == c.pin0 || i == c.pinc) d += d;
+            y = d * x(i);
+        }
+        if (I != 0 && !patched(i - 1)) y -= c.E[I - 1] * x(i - 1);
+        if (I != g.nx - 1 && !patched(i + 1)) y -= c.W[I + 1] * x(i + 1);
+        if (J != 0 && !patched(i - g.nx)) y -= c.N[J - 1] * x(i - g.nx);
+        if (J != g.ny - 1 && !patched(i + g.nx)) y -= c.S[J + 1] * x(i + g.nx);
+        if (T.cnt) {
+            const int n = T.cnt[i] < T.tmax ? T.cnt[i] : T.tmax;
+            for (int t = 0; t < n; ++t) {
+                const int e = T.ent[(size_t)i * T.tmax + t];
+                y += P.pval[e] * x(T.prow[e / 5]);
+            }
+        }
+        return y;
+    }
+};
+
 }  // namespace cuibm

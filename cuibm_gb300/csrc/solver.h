@@ -52,6 +52,14 @@ struct Lhs1Coef {
     // interior rows, 1 on the boundary rows); null for the other methods
     const double *rscale;
 };
+// The patched rows holding each column (discrete adjoint): column i appears in
+// min(cnt[i], tmax) entries ent[i * tmax + t] of the RowPatch arrays (entry e is slot
+// e / 5, position e % 5), slot k being the row prow[k].  cnt is null where no row is
+// patched.
+struct TransposeList {
+    const int *cnt, *ent, *prow;
+    int tmax;
+};
 struct Lhs2Coef {
     const double *E, *W;  // on I (0..nx-1), zero where the neighbour is missing
     const double *N, *S;  // on J (0..ny-1)
@@ -166,6 +174,7 @@ struct IbArrays {
     double *forcePart;
     double *forceOut;  // [fx, fy]
     double *surf;      // surface force: pressure, du/dn, dv/dn per body point, then Fx, Fy
+    double *velOff;    // 2 * total: per-point offsets of the prescribed body velocity (u, then v)
     double *motion;    // kMotionLen: [midX, midY, centerVelocityU, centerVelocityV, midX0, midY0,
                        //  U0, V0, SCtol, sub-iterations done, continue flag, spare]
 };
@@ -255,6 +264,11 @@ struct Context {
         double *rscale1 = nullptr;                 // numUV
     } emb;
 
+    // discrete adjoint (adjoint.cu): its buffers and snapshots, allocated by the first
+    // cuibm_adjoint call; the relative tolerance of its transposed solves
+    void *adj = nullptr;
+    double adjoint_rtol = 1e-10;
+
     // output files
     FILE *iterationsFile = nullptr, *forceFile = nullptr, *midPositionFile = nullptr;
 
@@ -270,6 +284,15 @@ struct Context {
 };
 
 // ---- entry points between translation units ----------------------------------
+// context.cu: the phases of a step's pass (record_pass runs them in this order), one
+// whole step as cuibm_step runs it, and the step error word
+void phase_generate_rhs1(Context &c, bool first);
+void phase_solve_velocity(Context &c, bool in_graph);
+void phase_generate_rhs2(Context &c);
+void phase_solve_poisson(Context &c, bool in_graph);
+void step_once(Context &c);
+int read_step_error(Context &c);
+
 // ns_kernels.cu
 void upload_ns_tables(Context &c);
 void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val);
@@ -290,6 +313,12 @@ int read_solve_status(Context &c, LinearSystem &S, int *iterations);
 int read_body_runs(Context &c, LinearSystem &S);
 int count_kernel_nodes(cudaGraph_t g);
 void refresh_system_diagonals(Context &c, LinearSystem &S);  // after the operator's rows changed
+
+// krylov.cu: the transposed systems of the discrete adjoint (adjoint.cu)
+void setup_transposed_system(Context &c, const LinearSystem &F, LinearSystem &S, std::vector<void *> &allocs);
+int launch_solve_transposed(Context &c, LinearSystem &S, LinearSystem &F, const TransposeList &T, const double *b,
+                            double *x, int *iterations);
+void launch_apply_transposed(Context &c, int which, const TransposeList &T, const double *x, double *y);
 
 // fused_solve.cu
 void setup_fused(Context &c, LinearSystem &S);
@@ -317,6 +346,9 @@ void build_sa_hierarchy(Context &c, LinearSystem &S);
 void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z);
 void free_sa_hierarchy(LinearSystem &S);
 double sa_vcycle_bytes(const LinearSystem &S);
+// the transposed cycle of the discrete adjoint (its level matrices made on first use)
+void ensure_transposed_levels(Context &c, LinearSystem &S);
+void launch_vcycle_transposed(Context &c, LinearSystem &S, const TransposeList &T, const double *r, double *z);
 int sa_coarsest_size(const LinearSystem &S);
 
 // ib_kernels.cu
@@ -341,6 +373,8 @@ void launch_force(Context &c);
 void launch_surface_force(Context &c, int mode, bool to_step);
 void launch_body_motion(Context &c, double t);
 void launch_body_pre_step(Context &c);
+void apply_velocity_offsets(Context &c);  // after CUIBM_F_BODY_VELOCITY_OFFSET was written
+const int *force_box_dev(Context &c);     // the control-volume box [i0, j0, ncx, ncy] (device)
 bool body_moves(Context &c);
 void launch_body_box(Context &c);
 void launch_step_counter(Context &c);
@@ -352,6 +386,16 @@ void refresh_fused_hierarchy(Context &c, LinearSystem &S);  // after the SA hier
 // embedded.cu: the checksum of the Poisson patched-row pattern (written at every tagging)
 unsigned long long read_rows_key(Context &c);
 void initialise_body(Context &c);
+
+// adjoint.cu: the discrete adjoint of the embedded method's steps (cuibm_adjoint)
+struct AdjointStats {
+    double ms;
+    long long forward_steps, tape_steps, velocity_iterations, poisson_iterations;
+};
+void run_adjoint(Context &c, int nsteps, int snapshots, const double *wx, const double *wy, double *J, double *grad,
+                 size_t ngrad, double adjoint_rtol, AdjointStats *stats);
+void free_adjoint(Context &c);
+void apply_transposed(Context &c, int which, const double *x, double *y);
 
 // io.cpp / fields.cu
 void write_grid_file(Context &c);

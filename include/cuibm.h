@@ -121,6 +121,13 @@ enum {
                                 (written by CUIBM_OP_SURFACE_FORCE*, or each step with the option
                                 "force_method" 1 or 2) */
     CUIBM_F_FORCES,          /* D 2: Fx, Fy of the last step (what cuibm_get_forces reads) */
+    CUIBM_F_BODY_VELOCITY_OFFSET, /* D 2*total_points: per-point offsets of the prescribed body velocity
+                                (u of each point, then v), zero by default; writing them (after
+                                cuibm_initialise) sets uB = unew + offset_u and vB = offset_v at once
+                                and at every later motion update (prescribed motion only).  No
+                                counterpart in the reference, whose motion sets every point's velocity
+                                alike (luo_base/move.cu:11-36); it is the perturbation behind the
+                                per-point gradients of cuibm_adjoint */
     CUIBM_F_COUNT
 };
 
@@ -152,6 +159,8 @@ enum {
     CUIBM_OP_SURFACE_FORCE,    /* surface-integral force on body 0 (luo_base::luoForce, unused by the
                                   reference's step) into CUIBM_F_SURFACE_FORCE, as the reference wrote it */
     CUIBM_OP_SURFACE_FORCE_CORRECTED, /* the same with its two index slips corrected */
+    CUIBM_OP_APPLY_LHS1_T,     /* WORK_Y = LHS1^T WORK_X (embedded method: the adjoint's operator) */
+    CUIBM_OP_APPLY_LHS2_T,     /* WORK_Y = LHS2^T WORK_X */
     CUIBM_OP_COUNT
 };
 
@@ -244,6 +253,37 @@ int cuibm_launch_count(cuibm_ctx *ctx, long long *per_step);
 int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p, const int *ghost_tags_uv,
                            const double *dx, const double *dy, int nx, int ny, int bb_i, int bb_j, int bb_ncx,
                            int bb_ncy, double nu, double dt, double *force_out, void *stream);
+
+/* ---- discrete adjoint ---------------------------------------------------------
+ * Gradients of J = sum_{n=1..nsteps} wx[n-1] Fx^n + wy[n-1] Fy^n, the control-volume
+ * force of each step (period-averaged drag coefficient: wx = 2 / nsteps, wy = 0), for the
+ * embedded method (SolverType OSC_CYLINDER) with a prescribed body motion (VIV: 0) and
+ * the control-volume force (force_method 0).  No counterpart in the reference, whose
+ * step (luo_base::stepTime, luo_base.cu:208-233 with luo_iter's phases) it differentiates.
+ * Runs steps 1..nsteps from the initial condition (call it right after cuibm_initialise)
+ * and the reverse sweep: transposed stencils, transposed ghost-node interpolation with
+ * the tags of the forward step, transposed solves (the Poisson one preconditioned by the
+ * transposed cycle of the forward smoothed-aggregation hierarchy), binomial
+ * checkpointing over `snapshots` stored states (each holds u, uhat, N, p, the x+ boundary
+ * and the body state).  On return the context is back at its initial state.  grad
+ * (ngrad = 2 + 2 * total_points):
+ *   grad[0]                     dJ / d nu
+ *   grad[1]                     dJ / d uCoefficient (the prescribed velocity amplitude of
+ *                               bodies.yaml; the prescribed path xCoefficient held fixed)
+ *   grad[2 + k], grad[2 + np + k]  dJ / d (u, v offset of point k's velocity,
+ *                               CUIBM_F_BODY_VELOCITY_OFFSET); zero for k > 0 because the
+ *                               reference's kernels read point 0's velocity only
+ * *J (may be null) gets J.  The transposed solves stop at the relative residual of the
+ * option "adjoint_tolerance" (default 1e-10).  stats (may be null): device time of the
+ * whole call, forward steps recomputed from snapshots, steps taped, and the transposed
+ * solves' iterations.  The transposed stencils accumulate with atomic adds: results
+ * agree from run to run to rounding, not bit for bit. */
+typedef struct {
+    double ms;
+    long long forward_steps, tape_steps, velocity_iterations, poisson_iterations;
+} cuibm_adjoint_stats;
+int cuibm_adjoint(cuibm_ctx *ctx, int nsteps, int snapshots, const double *wx, const double *wy, double *J,
+                  double *grad, size_t ngrad, cuibm_adjoint_stats *stats);
 
 /* ---- batched instances ------------------------------------------------------
  * Many independent cases advanced together on one GPU.  No counterpart in the

@@ -7,12 +7,14 @@ tests/golden/make_config_runs.py with both systems solved by sparse LU).
   impulsively started cylinder Re 40, 270 x 270, 157 points, external method, dt 0.01:
       C_D and C_L of every one of 2000 steps within COEF, u and p after 2000 steps
       within FIELD_L2;
-  cylinder Re 550, 922 x 922, 629 points, external method, dt 0.002, both solves at the
-      configuration's relative tolerance 1e-8, plain FP64 and mixed precision (FP32
-      multigrid cycles inside the FP64 Krylov loop): C_D and C_L of steps 1-40 within
-      COEF of the FP64 oracle's, fields on every 8th node within FIELD_MIXED.
+  cylinder Re 550, 922 x 922, 629 points, external method, dt 0.002, 40 steps: tightly
+      solved, C_D and C_L within COEF and the fields on every 8th node within FIELD_L2;
+      at the configuration's relative tolerance 1e-8, plain FP64 and mixed precision
+      (FP32 multigrid cycles inside the FP64 Krylov loop), C_D and C_L within COEF_REL of
+      their size at every step and within COEF_LATE over steps 21-40, fields within
+      FIELD_MIXED.
 
-For the first two the GPU solves to SOLVE_TOL, so that what is compared is the
+The tightly solved runs solve to SOLVE_TOL, so that what is compared is the
 discretisation both sides share, not where each Krylov solve happened to stop."""
 import os
 
@@ -27,7 +29,9 @@ pytestmark = pytest.mark.gpu
 SOLVE_TOL = 1e-13   # relative residual of both GPU solves in the tightly solved runs
 FIELD_L2 = 1e-9     # relative L2 of u and p against the oracle
 COEF = 1e-6         # drag and lift coefficients, every step
-FIELD_MIXED = 1e-6  # Re 550 at the configuration's solver tolerance 1e-8, relative L2 of the subsample
+FIELD_MIXED = 1e-5  # Re 550 at the configuration's solver tolerance 1e-8, relative L2 of the subsample
+COEF_REL = 1e-5     # Re 550 at 1e-8: drag and lift relative to their size, every step
+COEF_LATE = 2e-6    # Re 550 at 1e-8: drag and lift over steps 21-40
 
 
 def rel_l2(a, b):
@@ -87,11 +91,9 @@ def subsample(info, u, p, stride):
     return np.concatenate([uu, vv]), p.reshape(ny, nx)[::stride, ::stride].ravel()
 
 
-@pytest.mark.parametrize("precision", [None, "MIXED"])
-def test_cylinder_re550_40_steps_against_fp64_oracle(tmp_path, golden_dir, precision):
-    z = golden(golden_dir, "config_cylinder_re550")
-    f = cases.cylinder(str(tmp_path / "c"), h=0.005, ratio=1.01, points=629, nu=1.0 / 550, dt=0.002, nt=40,
-                       vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", precision=precision)
+def re550_run(folder, tol, precision):
+    f = cases.cylinder(folder, h=0.005, ratio=1.01, points=629, nu=1.0 / 550, dt=0.002, nt=40, vel_tol=tol,
+                       pois_tol=tol, pois_pc="SMOOTHED_AGGREGATION", precision=precision)
     cd, cl = [], []
     with cb.NavierStokesSolver(f) as s:
         s.set_option("write_output", 0)
@@ -102,11 +104,46 @@ def test_cylinder_re550_40_steps_against_fp64_oracle(tmp_path, golden_dir, preci
             fx, fy = s.forces()
             cd.append(2 * fx)
             cl.append(2 * fy)
-        us, ps = subsample(s.info, s.get("u"), s.get("p"), int(z["stride"]))
-    dcd = np.max(np.abs(np.array(cd) - z["cd"]))
-    dcl = np.max(np.abs(np.array(cl) - z["cl"]))
-    eu, ep = rel_l2(us, z["u_sub"]), rel_l2(ps, z["p_sub"])
-    print("Re 550 %s vs FP64 oracle: max |dC_D| %.2e, max |dC_L| %.2e, u %.2e, p %.2e"
-          % (precision or "FP64", dcd, dcl, eu, ep))
+        return np.array(cd), np.array(cl), subsample(s.info, s.get("u"), s.get("p"), 8)
+
+
+def field_errors(us, ps, z):
+    """relative L2 of the velocity and of the pressure with its mean removed (the
+    pressure level is fixed only by one pinned cell of a nearly singular operator)"""
+    eu = rel_l2(us, z["u_sub"])
+    ep = rel_l2(ps - ps.mean(), z["p_sub"] - z["p_sub"].mean())
+    return eu, ep
+
+
+def test_cylinder_re550_40_steps_tightly_solved(tmp_path, golden_dir):
+    """The Re 550 discretisation at full size: both solves to SOLVE_TOL, every step's
+    C_D and C_L within COEF of the FP64 oracle, fields within FIELD_L2."""
+    z = golden(golden_dir, "config_cylinder_re550")
+    assert int(z["stride"]) == 8
+    cd, cl, (us, ps) = re550_run(str(tmp_path / "c"), SOLVE_TOL, None)
+    dcd, dcl = np.max(np.abs(cd - z["cd"])), np.max(np.abs(cl - z["cl"]))
+    eu, ep = field_errors(us, ps, z)
+    print("Re 550 FP64 at %g vs FP64 oracle: max |dC_D| %.2e, max |dC_L| %.2e, u %.2e, p %.2e"
+          % (SOLVE_TOL, dcd, dcl, eu, ep))
     assert dcd < COEF and dcl < COEF, (dcd, dcl)
+    assert eu < FIELD_L2 and ep < FIELD_L2, (eu, ep)
+
+
+@pytest.mark.parametrize("precision", [None, "MIXED"])
+def test_cylinder_re550_40_steps_at_configuration_tolerance(tmp_path, golden_dir, precision):
+    """Both solves at the configuration's relative tolerance 1e-8, plain FP64 and mixed
+    precision, against the FP64 oracle (sparse LU).  The impulsive start's C_D is 405 at
+    step 1 and about 1.1 from step 30 on; the error a 1e-8 solve leaves grows to a few
+    times 1e-6 in the first steps (about 1e-6 of C_D's size there) and settles below
+    1e-6 as the flow does: every step within COEF_REL of |C_D| (and of |C_L| + 1), steps
+    21-40 within COEF_LATE."""
+    z = golden(golden_dir, "config_cylinder_re550")
+    cd, cl, (us, ps) = re550_run(str(tmp_path / "c"), 1e-8, precision)
+    dcd, dcl = np.abs(cd - z["cd"]), np.abs(cl - z["cl"])
+    eu, ep = field_errors(us, ps, z)
+    print("Re 550 %s at 1e-8 vs FP64 oracle: max |dC_D| %.2e (steps 21-40 %.2e), max |dC_L| %.2e (%.2e), "
+          "max relative dC_D %.2e, u %.2e, p %.2e" % (precision or "FP64", dcd.max(), dcd[20:].max(), dcl.max(),
+                                                      dcl[20:].max(), np.max(dcd / np.abs(z["cd"])), eu, ep))
+    assert dcd[20:].max() < COEF_LATE and dcl[20:].max() < COEF_LATE
+    assert np.all(dcd <= COEF_REL * np.abs(z["cd"])) and np.all(dcl <= COEF_REL * (np.abs(z["cl"]) + 1))
     assert eu < FIELD_MIXED and ep < FIELD_MIXED, (eu, ep)
