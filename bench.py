@@ -31,6 +31,7 @@ which is not available, and a GPU build of it cannot be made here).
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -418,6 +419,64 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
     return out
 
 
+def oscillating_case(folder, nt, tol=1e-8):
+    """The oscillating cylinder at KC 10 (Re 200): [-10, 10]^2, h 0.01 in [-2, 2]^2 stretched
+    by 1.02 (686 x 686), 314 points, embedded method, u_B(t) = sin(2 pi t / 10) in fluid at
+    rest, dt 0.0025."""
+    from cuibm_gb300 import cases
+    period, um = 10.0, 1.0
+    w = 2 * math.pi / period
+    motion = {"xCoefficient": um / w, "uCoefficient": um, "xfrequency": 1.0 / period, "xPhase": -math.pi / 2,
+              "uPhase": -math.pi / 2}
+    return cases.cylinder(folder, h=0.01, ratio=1.02, extent=10.0, core=2.0, points=314, nu=1.0 / 200, dt=0.0025,
+                          nt=nt, method="OSC_CYLINDER", quiescent=True, motion=motion, vel_tol=tol, pois_tol=tol)
+
+
+def adjoint_comparison(local, steps=40, snapshots=64, rebuild_interval=0):
+    """The discrete adjoint on the oscillating cylinder at KC 10 (686 x 686, 314 points,
+    embedded method): the gradient of the drag coefficient averaged over the first `steps`
+    steps with respect to nu, the velocity amplitude and the per-point velocity offsets,
+    against the forward run of the same steps (both solves to 1e-8, transposed solves to
+    1e-8).  Times are wall-clock (the SA hierarchy is kept from the initial rows,
+    sa_rebuild_interval 0, as host rebuilds would dominate both)."""
+    import cuibm_gb300 as cb
+    tmp = tempfile.mkdtemp(prefix="cuibm_adj_")
+    f = oscillating_case(os.path.join(tmp, "kc10"), steps)
+
+    def fresh():
+        s = cb.NavierStokesSolver(f, ["-deviceNumber", str(local)])
+        s.set_option("write_output", 0)
+        s.set_option("sa_rebuild_interval", rebuild_interval)
+        s.set_option("adjoint_tolerance", 1e-8)
+        s.initialise()
+        return s
+
+    s = fresh()
+    info = s.info
+    t0 = time.perf_counter()
+    J = 0.0
+    for _ in range(steps):
+        s.stepTime(1)
+        J += 2.0 / steps * s.forces()[0]
+    fwd = time.perf_counter() - t0
+    s.close()
+    out = {"workload": "oscillating cylinder KC 10, Re 200, embedded method, %dx%d, %d points, dt 0.0025"
+                       % (info.nx, info.ny, info.total_points),
+           "steps": steps, "objective": "mean of C_D = 2 Fx over the steps", "J_forward": J,
+           "forward_s": round(fwd, 3), "cells": info.nx * info.ny}
+    for snaps in (snapshots, 8):
+        s = fresh()
+        t0 = time.perf_counter()
+        Ja, grad, st = s.adjoint(steps, 2.0 / steps, snapshots=snaps)
+        el = time.perf_counter() - t0
+        s.close()
+        out["snapshots_%d" % snaps] = {
+            "adjoint_s": round(el, 3), "adjoint_over_forward": round(el / fwd, 3), "J": Ja,
+            "dJ_dnu": grad[0], "dJ_duCoefficient": grad[1], "dJ_doffset_u0": grad[2],
+            "dJ_doffset_v0": grad[2 + info.total_points], "stats": st}
+    return out
+
+
 def profiled_traffic(kernel, workload):
     """DRAM bytes per launch of the kernel as an ncu capture measured them: the line
     'dram_bytes_per_launch <kernel> <workload> <bytes>' of a committed summary under
@@ -479,6 +538,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the Re 550 FP64 / mixed-precision comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances comparison")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the discrete-adjoint measurement")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     rank, world, local, pg = dist_setup(a.gpus)
@@ -511,6 +571,8 @@ def main():
         line["mixed_precision"] = precision_comparison(local)
     if not a.no_batch and world == 1:
         line["batched"] = batch_comparison(local)
+    if not a.no_adjoint and world == 1:
+        line["adjoint"] = adjoint_comparison(local)
     print(json.dumps(line))
 
 

@@ -78,7 +78,7 @@ class Info(ctypes.Structure):
 
 class AdjointStats(ctypes.Structure):
     _fields_ = [("ms", ctypes.c_double)] + [(n, ctypes.c_longlong) for n in (
-        "forward_steps", "tape_steps", "velocity_iterations", "poisson_iterations")]
+        "forward_steps", "tape_steps", "velocity_iterations", "poisson_iterations", "solves_reused")]
 
 
 _lib = None

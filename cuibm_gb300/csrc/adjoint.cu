@@ -671,7 +671,7 @@ struct AdjointState {
     std::vector<void *> allocs;
     std::vector<Snapshot> snaps;
     // statistics of the last run
-    long long forward_steps = 0, tape_steps = 0;
+    long long forward_steps = 0, tape_steps = 0, solves_reused = 0;
     long long it1 = 0, it2 = 0;
 };
 
@@ -797,16 +797,28 @@ struct Runner {
         }
     }
 
-    // the intermediates of step n (1-based) from the state after step n-1
+    // the intermediates of step n (1-based) from the state after step n-1.  Where a
+    // snapshot holds the state after step n, its uhat and p are that step's solutions
+    // (the embedded method changes neither after its solve): they are copied, not solved
+    // again.
     void tape(int n)
     {
         launch_copy(c, c.p_old, c.p, c.g.nP);
         launch_copy(c, c.uold, c.u, c.g.nUV);
         launch_body_pre_step(c);
         phase_generate_rhs1(c, true);  // u := u1 (inside velocity), Nold := N, N, rhs1, x+ boundary
-        phase_solve_velocity(c, false);
-        phase_generate_rhs2(c);
-        phase_solve_poisson(c, false);
+        const Snapshot *done = nullptr;
+        for (const Snapshot &sn : A.snaps)
+            if (sn.holds == n) done = &sn;
+        if (done) {
+            launch_copy(c, c.uhat, done->blk + A.nUV, c.g.nUV);
+            launch_copy(c, c.p, done->blk + 3 * (size_t)A.nUV, c.g.nP);
+            ++A.solves_reused;
+        } else {
+            phase_solve_velocity(c, false);
+            phase_generate_rhs2(c);
+            phase_solve_poisson(c, false);
+        }
         launch_project(c);  // uold := u1, u := u2
         launch_copy(c, A.u2tape, c.u, c.g.nUV);
         launch_ib_after_projection(c);  // u := u4
@@ -928,8 +940,15 @@ struct Runner {
         advance(a, m);
         const int slot_m = save(m);
         reverse(m, b, s - 1, slot_m);
-        A.snaps[slot_m].holds = -1;
-        reverse(a, m, s, slot_a);
+        if (s - 1 >= m - a - 1) {
+            // snapshots to spare: keep the state after step m while reversing a..m, whose
+            // last tape takes step m's solutions from it
+            reverse(a, m, s - 1, slot_a);
+            A.snaps[slot_m].holds = -1;
+        } else {
+            A.snaps[slot_m].holds = -1;
+            reverse(a, m, s, slot_a);
+        }
     }
 };
 
@@ -978,7 +997,7 @@ void run_adjoint(Context &c, int nsteps, int snapshots, const double *wx, const 
     ensure_state(c, nsteps, snapshots);
     AdjointState &A = adj(c);
     A.S1T.rtol = A.S2T.rtol = adjoint_rtol;
-    A.forward_steps = A.tape_steps = A.it1 = A.it2 = 0;
+    A.forward_steps = A.tape_steps = A.solves_reused = A.it1 = A.it2 = 0;
     for (auto &s : A.snaps) s.holds = -1;
     CUIBM_TRY(cudaMemsetAsync(A.scal, 0, (2 + 2 * (size_t)nsteps) * sizeof(double), c.stream));
     CUIBM_TRY(cudaMemsetAsync(A.ubar, 0, A.nUV * sizeof(double), c.stream));
@@ -1037,6 +1056,7 @@ void run_adjoint(Context &c, int nsteps, int snapshots, const double *wx, const 
         stats->ms = ms;
         stats->forward_steps = A.forward_steps;
         stats->tape_steps = A.tape_steps;
+        stats->solves_reused = A.solves_reused;
         stats->velocity_iterations = A.it1;
         stats->poisson_iterations = A.it2;
     }

@@ -1119,6 +1119,7 @@ int cuibm_adjoint(cuibm_ctx *h, int nsteps, int snapshots, const double *wx, con
             stats->tape_steps = st.tape_steps;
             stats->velocity_iterations = st.velocity_iterations;
             stats->poisson_iterations = st.poisson_iterations;
+            stats->solves_reused = st.solves_reused;
         }
     });
     return CUIBM_OK;

@@ -390,7 +390,7 @@ void initialise_body(Context &c);
 // adjoint.cu: the discrete adjoint of the embedded method's steps (cuibm_adjoint)
 struct AdjointStats {
     double ms;
-    long long forward_steps, tape_steps, velocity_iterations, poisson_iterations;
+    long long forward_steps, tape_steps, velocity_iterations, poisson_iterations, solves_reused;
 };
 void run_adjoint(Context &c, int nsteps, int snapshots, const double *wx, const double *wy, double *J, double *grad,
                  size_t ngrad, double adjoint_rtol, AdjointStats *stats);

@@ -275,12 +275,13 @@ int cuibm_cv_force_noalloc(const double *u, const double *uold, const double *p,
  *                               reference's kernels read point 0's velocity only
  * *J (may be null) gets J.  The transposed solves stop at the relative residual of the
  * option "adjoint_tolerance" (default 1e-10).  stats (may be null): device time of the
- * whole call, forward steps recomputed from snapshots, steps taped, and the transposed
- * solves' iterations.  The transposed stencils accumulate with atomic adds: results
+ * whole call, forward steps recomputed from snapshots, steps taped, the transposed
+ * solves' iterations, and the taped steps whose two solves were taken from a snapshot of
+ * the step's end (with snapshots to spare, a taped step solves nothing).  The transposed stencils accumulate with atomic adds: results
  * agree from run to run to rounding, not bit for bit. */
 typedef struct {
     double ms;
-    long long forward_steps, tape_steps, velocity_iterations, poisson_iterations;
+    long long forward_steps, tape_steps, velocity_iterations, poisson_iterations, solves_reused;
 } cuibm_adjoint_stats;
 int cuibm_adjoint(cuibm_ctx *ctx, int nsteps, int snapshots, const double *wx, const double *wy, double *J,
                   double *grad, size_t ngrad, cuibm_adjoint_stats *stats);

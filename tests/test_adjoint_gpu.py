@@ -99,6 +99,9 @@ def test_objective_matches_forward_run(case, adjoint_run):
     J, _, stats = adjoint_run
     assert abs(J - gpu_drag(case)) <= 1e-12 * max(1.0, abs(J))
     assert stats["tape_steps"] == NT
+    # every step's state stored: each taped step but the last takes its solutions from the
+    # snapshot of its end
+    assert stats["solves_reused"] == NT - 1
 
 
 def test_gradient_against_oracle_tangent(case, adjoint_run):
