@@ -256,9 +256,6 @@ static void dense_inverse(const HostCsr &A, std::vector<double> &inv)
     }
 }
 
-// host CSR of the level-0 operator, identical to the device rows (weights applied)
-void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
-                       std::vector<double> &val);
 
 // device memory of the hierarchy: the context's arena, or (a hierarchy that will be
 // rebuilt) allocations of its own, freed with it
@@ -308,7 +305,7 @@ void build_sa_hierarchy(Context &c, LinearSystem &S)
     }
     HostCsr A;
     A.n = A.m = S.n;
-    host_operator_csr(c, S.which, S.w ? wh.data() : nullptr, A.ptr, A.col, A.val);
+    host_operator_csr(c, S.which, S.w ? wh.data() : nullptr, A.ptr, A.col, A.val, S.sa_body_free);
     std::vector<HostCsr> hostA;
     hostA.push_back(A);
     // host buffers are kept alive until the uploads below have been issued and synchronised

@@ -471,12 +471,16 @@ int cuibm_create(const char *case_folder, int argc, const char **argv, cuibm_ctx
                 const LinearSolve &L = S->which == 1 ? c.P.velocity : c.P.poisson;
                 if (L.precond == PC_SMOOTHED_AGGREGATION && L.precision != PRECISION_MIXED) {
                     S->sa_dynamic = true;
+                    S->sa_body_free = true;  // option "sa_body_free" 0: rebuild from the current rows
                     c.sa_rebuild = true;
                 }
             }
         }
         setup_system(c, c.sys1);
         setup_system(c, c.sys2);
+        // a hierarchy without the body's rows smooths level 0 with the current rows
+        for (LinearSystem *S : {&c.sys1, &c.sys2})
+            if (S->sa_body_free) refresh_system_diagonals(c, *S);
         if (c.sa_rebuild) c.sys1.sa_key = c.sys2.sa_key = read_rows_key(c);
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
         const char *ev = getenv("CUIBM_GRAPH");
@@ -550,10 +554,13 @@ int cuibm_initialise(cuibm_ctx *h)
 static void rebuild_hierarchies(Context &c)
 {
     if (c.sa_rebuild_interval <= 0 || c.timeStep - c.sa_last_rebuild < c.sa_rebuild_interval) return;
+    bool any = false;  // hierarchies without the body's rows never need rebuilding
+    for (LinearSystem *S : {&c.sys1, &c.sys2}) any = any || (S->sa_dynamic && !S->sa_body_free);
+    if (!any) return;
     const unsigned long long key = read_rows_key(c);
     bool rebuilt = false;
     for (LinearSystem *S : {&c.sys1, &c.sys2}) {
-        if (!S->sa_dynamic || S->sa_key == key) continue;
+        if (!S->sa_dynamic || S->sa_body_free || S->sa_key == key) continue;
         const auto t0 = std::chrono::steady_clock::now();
         free_sa_hierarchy(*S);
         build_sa_hierarchy(c, *S);
@@ -907,6 +914,25 @@ int cuibm_set_option(cuibm_ctx *h, const char *key, double value)
             c.force_method = m;
             if (c.initialised && c.use_graph) CUIBM_GUARD(h, { build_step_graph(c); });
         }
+    } else if (k == "sa_body_free") {
+        // a moving embedded body's SA hierarchies from the operator without the body's rows
+        // (the level-0 smoother and residual keep the current rows): built once, never
+        // rebuilt as the body moves (the default); 0: rebuilt from the current rows whenever
+        // the set of patched rows changes
+        const bool want = value != 0;
+        CUIBM_GUARD(h, {
+            if (!c.initialised) return fail(h, CUIBM_ERR_STATE, "sa_body_free is set after cuibm_initialise");
+            for (LinearSystem *S : {&c.sys1, &c.sys2}) {
+                if (!S->sa_dynamic || S->sa_body_free == want) continue;
+                S->sa_body_free = want;
+                free_sa_hierarchy(*S);
+                build_sa_hierarchy(c, *S);
+                refresh_fused_hierarchy(c, *S);
+                refresh_system_diagonals(c, *S);  // level 0 smooths with the current rows
+                S->sa_key = read_rows_key(c);
+            }
+            if (c.use_graph) build_step_graph(c);
+        });
     } else if (k == "adjoint_tolerance") {
         if (!(value > 0 && value < 1)) return fail(h, CUIBM_ERR_BAD_INPUT, "adjoint_tolerance must lie in (0, 1)");
         c.adjoint_rtol = value;

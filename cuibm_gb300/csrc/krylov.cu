@@ -608,7 +608,10 @@ struct SolveLauncher {
 void launch_solve(Context &c, LinearSystem &S, const double *b, double *x, bool in_graph)
 {
     int *err = c.err_word;
-    if (c.fused_solve && S.fused_fn) {
+    // a hierarchy without the body's rows (sa_body_free) cycles with the stepwise kernels,
+    // whose level-0 residual is the current operator's (the persistent cycle's stored
+    // A0 P is the hierarchy's own level-0 operator)
+    if (c.fused_solve && S.fused_fn && !S.sa_body_free) {
         launch_fused_solve(c, S, b, x);
         S.body_kernels = 0;
         return;

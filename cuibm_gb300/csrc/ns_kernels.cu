@@ -342,7 +342,8 @@ void upload_ns_tables(Context &c)
 // tables, entries in the reference's order (LHS1.cu / LHS2.cu numE offsets: per
 // row E, W, N, S, centre, rows in increasing order).  The same table values feed
 // the device rows, so this is exactly the operator the solvers apply.
-void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val)
+void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val,
+                     bool body_free)
 {
     const int nx = c.g.nx, ny = c.g.ny;
     const double *t = c.htab.data();
@@ -374,7 +375,8 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
     // the embedded method's patched rows live on the device (rebuilt at every tagging)
     Context::FadlunRows F = c.fadlun;
     const bool emb = c.emb.pid1 != nullptr;
-    if (emb) {
+    if (body_free) F = Context::FadlunRows{};  // no patched rows
+    if (emb && !body_free) {
         auto down = [&](auto &v, const auto *src, size_t n) {
             v.resize(n);
             CUIBM_TRY(cudaMemcpyAsync(v.data(), src, n * sizeof(v[0]), cudaMemcpyDeviceToHost, c.stream));
@@ -491,10 +493,10 @@ void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<i
 
 // CSR of the operator the solver iterates on (row weights w applied when given)
 void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
-                       std::vector<double> &val)
+                       std::vector<double> &val, bool body_free)
 {
     std::vector<int> row;
-    host_matrix_coo(c, which, row, col, val);
+    host_matrix_coo(c, which, row, col, val, body_free);
     const int n = which == 1 ? c.g.nUV : c.g.nP;
     ptr.assign(n + 1, 0);
     for (int r : row) ptr[r + 1]++;

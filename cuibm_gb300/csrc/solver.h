@@ -140,6 +140,9 @@ struct LinearSystem {
     double *diag = nullptr, *winv = nullptr;  // operator diagonal, 1 / w (CG)
     int precision = PRECISION_FP64;
     double strength = 0.0;  // smoothed aggregation's strength threshold
+    // the SA hierarchy built from the operator without the body's patched rows (a moving
+    // embedded body's option "sa_body_free"): it never needs rebuilding as the body moves
+    bool sa_body_free = false;
     // the SA hierarchy in its own allocations (so that it can be rebuilt) and the
     // checksum of the patched-row pattern it was built from
     bool sa_dynamic = false;
@@ -295,9 +298,11 @@ int read_step_error(Context &c);
 
 // ns_kernels.cu
 void upload_ns_tables(Context &c);
-void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val);
+// body_free: every row as if no body patched it (the SA hierarchy of a moving body)
+void host_matrix_coo(Context &c, int which, std::vector<int> &row, std::vector<int> &col, std::vector<double> &val,
+                     bool body_free = false);
 void host_operator_csr(Context &c, int which, const double *w, std::vector<int> &ptr, std::vector<int> &col,
-                       std::vector<double> &val);
+                       std::vector<double> &val, bool body_free = false);
 void launch_rhs1(Context &c, bool debug_terms, bool shift = true);  // shift: Nold = N first
 void launch_rhs2(Context &c, const double *uh);
 void launch_project(Context &c);
