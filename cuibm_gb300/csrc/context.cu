@@ -989,6 +989,13 @@ int cuibm_profile_kernel(cuibm_ctx *h, const char *kernel, int reps, double *avg
             if (avg_ms) *avg_ms = total / reps;
             if (bytes) *bytes = solve_bytes(S, it);
             return CUIBM_OK;
+        } else if (k == "fp64_fma") {
+            // the GPU's FP64 issue rate: *bytes gets the FLOPs of one launch (not bytes)
+            int sms = 0;
+            CUIBM_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+            const int blocks = 8 * sms;  // 8 blocks of 256 threads per SM
+            if ((size_t)blocks * 256 > (size_t)c.g.nUV) return fail(h, CUIBM_ERR_BAD_INPUT, "grid too small for fp64_fma");
+            launch = [&, blocks] { b = launch_fp64_fma(c, blocks, c.work_y); };
         } else if (k == "poisson_vcycle") {
             if (c.sys2.amg.empty()) return fail(h, CUIBM_ERR_BAD_INPUT, "the Poisson system has no SA hierarchy");
             launch = [&] { launch_vcycle(c, c.sys2, c.work_x, c.work_y); };

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_rhs1(RhsCoef c, Grid g, BcPtrs b, const
     const int nx = g.nx, ny = g.ny, nU = g.nU;
     const double hd = 0.5 * dt * nu;
     const double uc = u[t];
-    double Nn, Ln, B1 = 0;
+    double Nn, Lr, B1 = 0;  // Lr: the diffusion term over nu
     if (t < nU) {
         const int I = t % (nx - 1), J = t / (nx - 1), iv = nU + nx * J + I;
         const double ue = (I == nx - 2) ? b.xp[J] : u[t + 1];
@@ -100,15 +100,15 @@ __global__ void __launch_bounds__(256) k_rhs1(RhsCoef c, Grid g, BcPtrs b, const
         const double vn = (J == ny - 1) ? b.yp[nx - 1 + I] : u[iv];
         const double vse = (J == 0) ? b.ym[nx + I] : u[iv - nx + 1];
         const double vs = (J == 0) ? b.ym[nx - 1 + I] : u[iv - nx];
-        const double a = c.uxA[I];
-        const double vbar = ((vne - vn) * a + vn) / 2 + ((vse - vs) * a + vs) / 2;
+        // ((vne - vn) a + vn) / 2 + ((vse - vs) a + vs) / 2, folded
+        const double vbar = c.uhA[I] * (vne + vse) + c.uhB[I] * (vn + vs);
         const double unc = (J == ny - 1) ? 2 * b.yp[I] - uc : un;  // mirrored ghost value
         const double usc = (J == 0) ? 2 * b.ym[I] - uc : us;
         Nn = uc * (ue * c.uxE[I] + uw * c.uxW[I] + uc * c.uxC[I]) +
              vbar * (unc * c.uyN[J] + usc * c.uyS[J] + uc * c.uyC[J]);
         const double unl = (J == ny - 1) ? b.yp[I] : un;
         const double usl = (J == 0) ? b.ym[I] : us;
-        Ln = nu * ((ue - uc) * c.ulE[I] + (uw - uc) * c.ulW[I] + (unl - uc) * c.ulN[J] + (usl - uc) * c.ulS[J]);
+        Lr = (ue - uc) * c.ulE[I] + (uw - uc) * c.ulW[I] + (unl - uc) * c.ulN[J] + (usl - uc) * c.ulS[J];
         if (I == nx - 2) B1 += b.xp[J] * hd * c.ulE[I];
         if (I == 0) B1 += b.xm[J] * hd * c.ulW[I];
         if (J == ny - 1) B1 += (2 * b.yp[I] - uc) * hd * (0.5 * c.ulN[J]);
@@ -123,15 +123,14 @@ __global__ void __launch_bounds__(256) k_rhs1(RhsCoef c, Grid g, BcPtrs b, const
         const double ue = (I == nx - 1) ? b.xp[J] : u[iu];
         const double unw = (I == 0) ? b.xm[J + 1] : u[iu + nx - 2];
         const double uw = (I == 0) ? b.xm[J] : u[iu - 1];
-        const double a = c.vyA[J];
-        const double ubar = ((une - ue) * a + ue) / 2 + ((unw - uw) * a + uw) / 2;
+        const double ubar = c.vhA[J] * (une + unw) + c.vhB[J] * (ue + uw);
         const double vec = (I == nx - 1) ? 2 * b.xp[ny + J] - uc : ve;
         const double vwc = (I == 0) ? 2 * b.xm[ny + J] - uc : vw;
         Nn = ubar * (vec * c.vxE[I] + vwc * c.vxW[I] + uc * c.vxC[I]) +
              uc * (vn * c.vyN[J] + vs * c.vyS[J] + uc * c.vyC[J]);
         const double vel = (I == nx - 1) ? b.xp[ny + J] : ve;
         const double vwl = (I == 0) ? b.xm[ny + J] : vw;
-        Ln = nu * ((vel - uc) * c.vlE[I] + (vwl - uc) * c.vlW[I] + (vn - uc) * c.vlN[J] + (vs - uc) * c.vlS[J]);
+        Lr = (vel - uc) * c.vlE[I] + (vwl - uc) * c.vlW[I] + (vn - uc) * c.vlN[J] + (vs - uc) * c.vlS[J];
         if (I == nx - 1) B1 += (2 * b.xp[ny + J] - uc) * hd * (0.5 * c.vlE[I]);
         if (I == 0) B1 += (2 * b.xm[ny + J] - uc) * hd * (0.5 * c.vlW[I]);
         if (J == ny - 2) B1 += b.yp[nx - 1 + I] * hd * c.vlN[J];
@@ -140,10 +139,11 @@ __global__ void __launch_bounds__(256) k_rhs1(RhsCoef c, Grid g, BcPtrs b, const
     const double Nprev = SHIFT ? N[t] : Nold[t];
     if (SHIFT) Nold[t] = Nprev;
     N[t] = Nn;
-    const double r = uc + dt * (0.5 * Nprev - 1.5 * Nn + 0.5 * Ln) + B1;
+    // uc + dt (0.5 Nold - 1.5 N + 0.5 L) + B1 with L = nu Lr
+    const double r = uc + (0.5 * dt) * Nprev - (1.5 * dt) * Nn + hd * Lr + B1;
     rhs[t] = e.pid ? emb_rhs1(e, t, nU, r, u) : r;
     if (DEBUG) {
-        Lout[t] = Ln;
+        Lout[t] = nu * Lr;
         bc1out[t] = B1;
     }
 }
@@ -159,8 +159,8 @@ struct EmbRhs2 {
     double dt;
 };
 
-// rhs2 = -D uhat with boundary velocities on the domain edges
-__global__ void k_rhs2(Grid g, BcPtrs b, const double *__restrict__ dx, const double *__restrict__ dy,
+// rhs2 = -D uhat with boundary velocities on the domain edges (1/dx, 1/dy tables)
+__global__ void k_rhs2(Grid g, BcPtrs b, const double *__restrict__ rdx, const double *__restrict__ rdy,
                        const double *__restrict__ uh, double *__restrict__ rhs2, EmbRhs2 e)
 {
     const int ip = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,7 +171,8 @@ __global__ void k_rhs2(Grid g, BcPtrs b, const double *__restrict__ dx, const do
     const double uw = (I != 0) ? uh[iu - 1] : b.xm[J];
     const double vn = (J != ny - 1) ? uh[iv] : b.yp[nx - 1 + I];
     const double vs = (J != 0) ? uh[iv - nx] : b.ym[nx - 1 + I];
-    double r = (((0 - ue / dx[I]) + uw / dx[I]) - vn / dy[J]) + vs / dy[J];
+    // -(ue - uw)/dx - (vn - vs)/dy with reciprocal tables (FP64 divides are the slow path)
+    double r = (uw - ue) * rdx[I] + (vs - vn) * rdy[J];
     if (e.pid && ip < (nx - 1) * ny) {
         const int k = e.pid[ip];
         if (k >= 0) {
@@ -229,6 +230,33 @@ __global__ void k_cfl(Grid g, const double *__restrict__ u, const double *__rest
     const int I = ip % g.nx, J = ip / g.nx;
     if (I == g.nx - 1 || J == g.ny - 1) return;
     cfl[ip] = dt * (fabs(u[(g.nx - 1) * J + I]) / dx[I] + fabs(u[g.nU + g.nx * J + I]) / dy[J]);
+}
+
+// FP64 issue peak: 8 independent chains of kFmaIters fused multiply-adds per thread
+// (2 FLOPs each), the result kept live through one store per thread
+constexpr int kFmaIters = 4096;
+__global__ void __launch_bounds__(256) k_fp64_fma(double a, double b, double *out)
+{
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9 + k;
+    for (int it = 0; it < kFmaIters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// one launch of k_fp64_fma over blocks x 256 threads into out (blocks * 256 doubles);
+// returns the FLOPs it performs
+double launch_fp64_fma(Context &c, int blocks, double *out)
+{
+    k_fp64_fma<<<blocks, 256, 0, c.stream>>>(0.999999, 1e-7, out);
+    CUIBM_TRY(cudaGetLastError());
+    return 2.0 * 8 * kFmaIters * 256.0 * blocks;
 }
 
 __global__ void k_copy(double *__restrict__ dst, const double *__restrict__ src, int n)
@@ -295,6 +323,13 @@ void upload_ns_tables(Context &c)
     size_t o_vyA = table(ny - 1, [&](int J) { double cc = dy[J], d = dy[J + 1]; return cc / (cc + d); });
     size_t o_vlN = table(ny - 1, [&](int J) { return 1 / (dy[J + 1] * (dy[J] + dy[J + 1]) * 0.5); });
     size_t o_vlS = table(ny - 1, [&](int J) { return 1 / (dy[J] * (dy[J] + dy[J + 1]) * 0.5); });
+    // folded tables of the fused right-hand side (see RhsCoef)
+    size_t o_uhA = table(nx - 1, [&](int I) { double a = dx[I], b = dx[I + 1]; return 0.5 * (a / (a + b)); });
+    size_t o_uhB = table(nx - 1, [&](int I) { double a = dx[I], b = dx[I + 1]; return 0.5 * (1 - a / (a + b)); });
+    size_t o_vhA = table(ny - 1, [&](int J) { double cc = dy[J], d = dy[J + 1]; return 0.5 * (cc / (cc + d)); });
+    size_t o_vhB = table(ny - 1, [&](int J) { double cc = dy[J], d = dy[J + 1]; return 0.5 * (1 - cc / (cc + d)); });
+    size_t o_rdx = table(nx, [&](int I) { return 1 / dx[I]; });
+    size_t o_rdy = table(ny, [&](int J) { return 1 / dy[J]; });
     // LHS1 (reference LHS1.cu expressions)
     size_t o_1uE = table(nx - 1, [&](int I) { return 0.5 * dt * nu * (1 / (dx[I + 1] * (dx[I + 1] + dx[I]) * 0.5)); });
     size_t o_1uW = table(nx - 1, [&](int I) { return 0.5 * dt * nu * (1 / (dx[I] * (dx[I + 1] + dx[I]) * 0.5)); });
@@ -325,6 +360,9 @@ void upload_ns_tables(Context &c)
     r.vxE = d + o_vxE; r.vxW = d + o_vxW; r.vxC = d + o_vxC; r.vlE = d + o_vlE; r.vlW = d + o_vlW;
     r.vyN = d + o_vyN; r.vyS = d + o_vyS; r.vyC = d + o_vyC; r.vyA = d + o_vyA; r.vlN = d + o_vlN; r.vlS = d + o_vlS;
     r.dx = c.dx; r.dy = c.dy;
+    r.uhA = d + o_uhA; r.uhB = d + o_uhB;
+    r.vhA = d + o_vhA; r.vhB = d + o_vhB;
+    r.rdx = d + o_rdx; r.rdy = d + o_rdy;
     c.l1.uE = d + o_1uE; c.l1.uW = d + o_1uW; c.l1.uN = d + o_1uN; c.l1.uS = d + o_1uS;
     c.l1.vE = d + o_1vE; c.l1.vW = d + o_1vW; c.l1.vN = d + o_1vN; c.l1.vS = d + o_1vS;
     c.l2.E = d + o_2E; c.l2.W = d + o_2W; c.l2.N = d + o_2N; c.l2.S = d + o_2S;
@@ -538,7 +576,7 @@ void launch_rhs2(Context &c, const double *uh)
     const auto &E = c.emb;
     const EmbRhs2 e = E.pid2 ? EmbRhs2{E.pid2, E.pns2, E.pAu2, E.pAv2, c.ib.uB, c.ib.uBk, c.ib.vB, c.ib.vBk, c.P.dt}
                              : EmbRhs2{};
-    k_rhs2<<<blocks_for(c.g.nP), kBlock, 0, c.stream>>>(c.g, bc_ptrs(c), c.dx, c.dy, uh, c.rhs2, e);
+    k_rhs2<<<blocks_for(c.g.nP), kBlock, 0, c.stream>>>(c.g, bc_ptrs(c), c.rc.rdx, c.rc.rdy, uh, c.rhs2, e);
     CUIBM_TRY(cudaGetLastError());
 }
 

@@ -85,6 +85,12 @@ struct RhsCoef {
     const double *vyN, *vyS, *vyC, *vyA;   // v-bar weight c/(c+d) for u at v nodes
     const double *vlN, *vlS;
     const double *dx, *dy;
+    // folded forms for fewer FP64 operations (the kernel is FP64-issue bound):
+    // v-bar = uhA (vne + vse) + uhB (vn + vs) with uhA = a/2, uhB = (1 - a)/2 (u nodes, per I);
+    // u-bar likewise with vhA, vhB (v nodes, per J); 1/dx, 1/dy for the divergence
+    const double *uhA, *uhB;
+    const double *vhA, *vhB;
+    const double *rdx, *rdy;
 };
 
 // ---- Krylov state living in device memory -------------------------------------
@@ -310,6 +316,7 @@ void launch_initial_velocity(Context &c);
 void launch_apply(Context &c, int which, const double *xin, double *yout);
 void launch_cfl(Context &c);
 void launch_copy(Context &c, double *dst, const double *src, int n);
+double launch_fp64_fma(Context &c, int blocks, double *out);  // FP64 issue peak probe; returns FLOPs
 
 // krylov.cu
 void setup_system(Context &c, LinearSystem &S);

@@ -217,7 +217,9 @@ int cuibm_set_option(cuibm_ctx *ctx, const char *key, double value);
  * back-to-back launches on the current state; *avg_ms is the mean launch time
  * and *bytes the kernel's algorithmic DRAM bytes per launch (unique inputs read
  * plus outputs written).  Names: "rhs1", "rhs2", "project", "apply_lhs1",
- * "apply_lhs2", "poisson_vcycle". */
+ * "apply_lhs2", "poisson_vcycle", "poisson_solve", "velocity_solve", and "fp64_fma" (a
+ * throughput probe of the GPU's FP64 fused multiply-add issue: *bytes then gets the
+ * FLOPs of one launch). */
 int cuibm_profile_kernel(cuibm_ctx *ctx, const char *kernel, int reps, double *avg_ms, double *bytes);
 
 /* Kernels of this library launched by the last time step: the kernel nodes of
