@@ -250,6 +250,7 @@ def run_ours(a, rank, world, local, pg):
             "other_kernels": {k: {"ms": round(v[0], 5), "GB/s": round(v[1] / (v[0] * 1e-3) / 1e9, 1)}
                               for k, v in prof.items()}}
     roof["traffic"], roof["traffic_source"] = profiled_traffic(dom, a.workload)
+    roof["fp64_issue"] = fp64_issue_roofline(s, prof, a.workload)
     s.close()
 
     # end to end through the public API with host buffers, on a fresh instance over
@@ -419,52 +420,59 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
     return out
 
 
-def oscillating_case(folder, nt, tol=1e-8):
+def oscillating_case(folder, nt, tol=1e-8, nu=None, ucoef=None):
     """The oscillating cylinder at KC 10 (Re 200): [-10, 10]^2, h 0.01 in [-2, 2]^2 stretched
     by 1.02 (686 x 686), 314 points, embedded method, u_B(t) = sin(2 pi t / 10) in fluid at
-    rest, dt 0.0025."""
+    rest, dt 0.0025.  nu and the velocity amplitude uCoefficient can be changed (the path
+    amplitude stays that of Um = 1)."""
     from cuibm_gb300 import cases
     period, um = 10.0, 1.0
     w = 2 * math.pi / period
-    motion = {"xCoefficient": um / w, "uCoefficient": um, "xfrequency": 1.0 / period, "xPhase": -math.pi / 2,
-              "uPhase": -math.pi / 2}
-    return cases.cylinder(folder, h=0.01, ratio=1.02, extent=10.0, core=2.0, points=314, nu=1.0 / 200, dt=0.0025,
-                          nt=nt, method="OSC_CYLINDER", quiescent=True, motion=motion, vel_tol=tol, pois_tol=tol)
+    motion = {"xCoefficient": um / w, "uCoefficient": um if ucoef is None else ucoef, "xfrequency": 1.0 / period,
+              "xPhase": -math.pi / 2, "uPhase": -math.pi / 2}
+    return cases.cylinder(folder, h=0.01, ratio=1.02, extent=10.0, core=2.0, points=314,
+                          nu=1.0 / 200 if nu is None else nu, dt=0.0025, nt=nt, method="OSC_CYLINDER", quiescent=True,
+                          motion=motion, vel_tol=tol, pois_tol=tol)
 
 
-def adjoint_comparison(local, steps=40, snapshots=64, rebuild_interval=0):
+def adjoint_comparison(local, steps=40, snapshots=64, tol=1e-8, fd=False, also_snapshots=(8,)):
     """The discrete adjoint on the oscillating cylinder at KC 10 (686 x 686, 314 points,
     embedded method): the gradient of the drag coefficient averaged over the first `steps`
     steps with respect to nu, the velocity amplitude and the per-point velocity offsets,
-    against the forward run of the same steps (both solves to 1e-8, transposed solves to
-    1e-8).  Times are wall-clock (the SA hierarchy is kept from the initial rows,
-    sa_rebuild_interval 0, as host rebuilds would dominate both)."""
+    against the forward run of the same steps (forward and transposed solves to tol).
+    Times are wall-clock.  With fd, central differences (relative step 1e-6) of the
+    forward run for nu and uCoefficient beside the gradient."""
     import cuibm_gb300 as cb
     tmp = tempfile.mkdtemp(prefix="cuibm_adj_")
-    f = oscillating_case(os.path.join(tmp, "kc10"), steps)
 
-    def fresh():
+    def fresh(nu=None, ucoef=None, name="kc10"):
+        f = oscillating_case(os.path.join(tmp, name), steps, tol=tol, nu=nu, ucoef=ucoef)
         s = cb.NavierStokesSolver(f, ["-deviceNumber", str(local)])
         s.set_option("write_output", 0)
-        s.set_option("sa_rebuild_interval", rebuild_interval)
-        s.set_option("adjoint_tolerance", 1e-8)
+        s.set_option("adjoint_tolerance", tol)
         s.initialise()
         return s
 
+    def forward(**kw):
+        s = fresh(**kw)
+        t0 = time.perf_counter()
+        J = 0.0
+        for _ in range(steps):
+            s.stepTime(1)
+            J += 2.0 / steps * s.forces()[0]
+        el = time.perf_counter() - t0
+        s.close()
+        return J, el
+
     s = fresh()
     info = s.info
-    t0 = time.perf_counter()
-    J = 0.0
-    for _ in range(steps):
-        s.stepTime(1)
-        J += 2.0 / steps * s.forces()[0]
-    fwd = time.perf_counter() - t0
     s.close()
+    J, fwd = forward()
     out = {"workload": "oscillating cylinder KC 10, Re 200, embedded method, %dx%d, %d points, dt 0.0025"
                        % (info.nx, info.ny, info.total_points),
-           "steps": steps, "objective": "mean of C_D = 2 Fx over the steps", "J_forward": J,
+           "steps": steps, "tolerance": tol, "objective": "mean of C_D = 2 Fx over the steps", "J_forward": J,
            "forward_s": round(fwd, 3), "cells": info.nx * info.ny}
-    for snaps in (snapshots, 8):
+    for snaps in (snapshots,) + tuple(also_snapshots):
         s = fresh()
         t0 = time.perf_counter()
         Ja, grad, st = s.adjoint(steps, 2.0 / steps, snapshots=snaps)
@@ -474,15 +482,42 @@ def adjoint_comparison(local, steps=40, snapshots=64, rebuild_interval=0):
             "adjoint_s": round(el, 3), "adjoint_over_forward": round(el / fwd, 3), "J": Ja,
             "dJ_dnu": grad[0], "dJ_duCoefficient": grad[1], "dJ_doffset_u0": grad[2],
             "dJ_doffset_v0": grad[2 + info.total_points], "stats": st}
+    if fd:
+        h, nu0 = 1e-6, 1.0 / 200
+        g = out["snapshots_%d" % snapshots]
+        fd_nu = (forward(nu=nu0 * (1 + h), name="nup")[0] - forward(nu=nu0 * (1 - h), name="num")[0]) / (2 * h * nu0)
+        fd_uc = (forward(ucoef=1 + h, name="ucp")[0] - forward(ucoef=1 - h, name="ucm")[0]) / (2 * h)
+        out["central_differences"] = {"relative_step": h, "dJ_dnu": fd_nu, "dJ_duCoefficient": fd_uc,
+                                      "rel_err_nu": abs(g["dJ_dnu"] - fd_nu) / abs(fd_nu),
+                                      "rel_err_uCoefficient": abs(g["dJ_duCoefficient"] - fd_uc) / abs(fd_uc)}
     return out
 
 
-def profiled_traffic(kernel, workload):
-    """DRAM bytes per launch of the kernel as an ncu capture measured them: the line
-    'dram_bytes_per_launch <kernel> <workload> <bytes>' of a committed summary under
-    profiles/.  This run does not measure DRAM traffic (that needs ncu); the number is
-    returned with the summary it comes from, which names the captured launch.  (None,
-    None) where no summary has one for this kernel and workload."""
+def fp64_issue_roofline(s, prof, workload, kernel="rhs1"):
+    """The FP64-issue bound beside the HBM one.  GB300 issues about two FP64 thread
+    instructions per clock per SM; the peak is measured here, in this run, by the
+    library's own FP64 FMA loop (profile_kernel "fp64_fma": independent FMA chains,
+    flops per launch / CUDA-event time).  The explicit right-hand-side kernel's FP64
+    instruction count per launch (DADD + DMUL + DFMA thread instructions) is an ncu
+    count, taken from the committed summary that holds it (a kernel's instruction
+    count does not depend on the clock or the cache, only on the workload); divided
+    by this run's event time it gives the achieved issue rate."""
+    ms, flops = s.profile_kernel("fp64_fma", reps=3)
+    peak_instr = flops / 2 / (ms * 1e-3)  # one FMA = two flops, one instruction
+    out = {"peak_tflops": round(flops / (ms * 1e-3) / 1e12, 4), "peak_ginstr_per_s": round(peak_instr / 1e9, 1),
+           "peak_source": "fp64_fma loop timed in this run (%.3f ms, %.4g flops)" % (ms, flops), "kernel": kernel}
+    instr, src = profiled_value("fp64_instr_per_launch", kernel, workload)
+    if instr is not None and kernel in prof:
+        kms = prof[kernel][0]
+        achieved = instr / (kms * 1e-3)
+        out.update({"instr_per_launch": instr, "instr_source": src, "ms_per_launch": round(kms, 5),
+                    "achieved_ginstr_per_s": round(achieved / 1e9, 1), "frac": round(achieved / peak_instr, 4)})
+    return out
+
+
+def profiled_value(key, kernel, workload):
+    """The number on the line '<key> <kernel> <workload> <value>' of a committed ncu
+    summary under profiles/, with the summary's name; (None, None) where none has it."""
     here = os.path.dirname(os.path.abspath(__file__))
     d = os.path.join(here, "profiles")
     if not os.path.isdir(d):
@@ -492,9 +527,18 @@ def profiled_traffic(kernel, workload):
             continue
         for line in open(os.path.join(d, fn)):
             f = line.strip().strip("`").split()
-            if len(f) == 4 and f[0] == "dram_bytes_per_launch" and f[1] == kernel and f[2] == workload:
+            if len(f) == 4 and f[0] == key and f[1] == kernel and f[2] == workload:
                 return int(f[3]), "ncu capture summarised in profiles/" + fn + " (not measured by this run)"
     return None, None
+
+
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of the kernel as an ncu capture measured them: the line
+    'dram_bytes_per_launch <kernel> <workload> <bytes>' of a committed summary under
+    profiles/.  This run does not measure DRAM traffic (that needs ncu); the number is
+    returned with the summary it comes from, which names the captured launch.  (None,
+    None) where no summary has one for this kernel and workload."""
+    return profiled_value("dram_bytes_per_launch", kernel, workload)
 
 
 def cpu_baseline(workload, budget_s=15.0, warmup=1, max_steps=200):
@@ -526,6 +570,27 @@ def cpu_baseline(workload, budget_s=15.0, warmup=1, max_steps=200):
                       % (max(1, warmup) + 1, max(1, warmup) + steps, steps, el), "steps_timed": steps}
 
 
+def kernel_timings(a):
+    """Each named kernel launched alone three times on the workload after its warm-up
+    steps, timed with CUDA events on the solver's stream (profile_kernel): ms per
+    launch and its algorithmic bytes (flops for fp64_fma)."""
+    import torch
+
+    import cuibm_gb300 as cb
+    with tempfile.TemporaryDirectory() as tmp:
+        folder, _ = make_case(a.workload, os.path.join(tmp, "case"))
+        s = cb.NavierStokesSolver(folder)
+        s.set_option("write_output", 0)
+        s.initialise()
+        s.stepTime(a.warmup)
+        torch.cuda.synchronize()
+        for k in a.kernel_timings.split(","):
+            ms, b = s.profile_kernel(k, reps=3)
+            print(json.dumps({"workload": a.workload, "kernel": k, "ms_per_launch": round(ms, 5),
+                              "bytes_or_flops": b}), flush=True)
+        s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -539,8 +604,23 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the Re 550 FP64 / mixed-precision comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-instances comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the discrete-adjoint measurement")
+    ap.add_argument("--adjoint-period", type=int, default=0, metavar="STEPS",
+                    help="only the discrete-adjoint comparison over STEPS steps of the KC 10 case (4000: the "
+                         "whole period), solves to --adjoint-tol, with central differences if --adjoint-fd")
+    ap.add_argument("--adjoint-tol", type=float, default=1e-10)
+    ap.add_argument("--adjoint-fd", action="store_true")
+    ap.add_argument("--kernel-timings", default=None, metavar="K1,K2,...",
+                    help="only time these kernels (profile_kernel names) after the warm-up steps of the "
+                         "workload, one JSON line each (the command the per-kernel ncu summaries capture)")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
+    if a.kernel_timings:
+        kernel_timings(a)
+        return
+    if a.adjoint_period:
+        print(json.dumps(adjoint_comparison(0, steps=a.adjoint_period, tol=a.adjoint_tol, fd=a.adjoint_fd,
+                                            also_snapshots=())))
+        return
     rank, world, local, pg = dist_setup(a.gpus)
     cfg = workload_config(a.workload)
     cfg.update({"l2": "flushed before every timed step (256 MB write)", "parallelism": "replicas" if world > 1

@@ -49,7 +49,7 @@ _OP_NAMES = [
     "weight_pressure", "project", "project_velocity", "update_body", "apply_lhs1", "apply_lhs2", "tag_points",
     "ghost_velocity_u", "ghost_velocity_uhat", "hybrid_velocity", "hybrid_pressure", "ghost_pressure",
     "set_inside", "robin_boundary", "force", "cfl", "surface_force", "surface_force_corrected",
-    "apply_lhs1_t", "apply_lhs2_t",
+    "apply_lhs1_t", "apply_lhs2_t", "precondition_poisson",
 ]
 OPS = {n: i for i, n in enumerate(_OP_NAMES)}
 
@@ -73,7 +73,8 @@ class Info(ctypes.Structure):
                [(n, ctypes.c_int) for n in ("total_points", "bb_start_i", "bb_start_j", "bb_ncx", "bb_ncy",
                                             "nnz_lhs1", "nnz_lhs2", "velocity_precond", "poisson_precond",
                                             "velocity_krylov", "poisson_krylov", "amg_levels",
-                                            "velocity_precision", "poisson_precision", "sa_rebuilds")]
+                                            "velocity_precision", "poisson_precision", "sa_rebuilds",
+                                            "sa_structured")]
 
 
 class AdjointStats(ctypes.Structure):

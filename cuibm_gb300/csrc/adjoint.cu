@@ -670,6 +670,11 @@ struct AdjointState {
     LinearSystem S1T, S2T;
     std::vector<void *> allocs;
     std::vector<Snapshot> snaps;
+    // two stashes of one step's solutions (uhat, then p) with the step they belong to
+    // (-1 none): the solutions of a checkpoint step whose snapshot was released, or of
+    // the last step of an advance, kept for the tape that comes next
+    double *stash[2] = {nullptr, nullptr};
+    int stash_step[2] = {-1, -1};
     // statistics of the last run
     long long forward_steps = 0, tape_steps = 0, solves_reused = 0;
     long long it1 = 0, it2 = 0;
@@ -720,6 +725,7 @@ void ensure_state(Context &c, int nsteps, int snapshots)
         A.prow2 = static_cast<int *>(dalloc(A, 2 * (size_t)c.emb.cap2 * sizeof(int) + 4));
         A.overflow = static_cast<int *>(dalloc(A, sizeof(int)));
         CUIBM_TRY(cudaMemset(A.overflow, 0, sizeof(int)));
+        for (double *&st : A.stash) st = static_cast<double *>(dalloc(A, (UV + P) * sizeof(double)));
         A.S1T.rtol = A.S2T.rtol = 1e-10;
         A.S1T.maxit = c.sys1.maxit;
         A.S2T.maxit = c.sys2.maxit;
@@ -797,22 +803,41 @@ struct Runner {
         }
     }
 
+    // keep the solutions of step n (uhat at src_uhat, p at src_p) in the stash the
+    // next tape does not need (that one holds step keep)
+    void stash_solutions(int n, const double *src_uhat, const double *src_p, int keep)
+    {
+        const int k = A.stash_step[0] == keep ? 1 : 0;
+        launch_copy(c, A.stash[k], src_uhat, c.g.nUV);
+        launch_copy(c, A.stash[k] + A.nUV, src_p, c.g.nP);
+        A.stash_step[k] = n;
+    }
+
     // the intermediates of step n (1-based) from the state after step n-1.  Where a
-    // snapshot holds the state after step n, its uhat and p are that step's solutions
-    // (the embedded method changes neither after its solve): they are copied, not solved
-    // again.
+    // snapshot holds the state after step n, or a stash that step's solutions, its uhat
+    // and p are that step's solutions (the embedded method changes neither after its
+    // solve): they are copied, not solved again.
     void tape(int n)
     {
         launch_copy(c, c.p_old, c.p, c.g.nP);
         launch_copy(c, c.uold, c.u, c.g.nUV);
         launch_body_pre_step(c);
         phase_generate_rhs1(c, true);  // u := u1 (inside velocity), Nold := N, N, rhs1, x+ boundary
-        const Snapshot *done = nullptr;
+        const double *done_uhat = nullptr, *done_p = nullptr;
         for (const Snapshot &sn : A.snaps)
-            if (sn.holds == n) done = &sn;
-        if (done) {
-            launch_copy(c, c.uhat, done->blk + A.nUV, c.g.nUV);
-            launch_copy(c, c.p, done->blk + 3 * (size_t)A.nUV, c.g.nP);
+            if (sn.holds == n) {
+                done_uhat = sn.blk + A.nUV;
+                done_p = sn.blk + 3 * (size_t)A.nUV;
+            }
+        for (int k = 0; k < 2 && !done_uhat; ++k)
+            if (A.stash_step[k] == n) {
+                done_uhat = A.stash[k];
+                done_p = A.stash[k] + A.nUV;
+                A.stash_step[k] = -1;
+            }
+        if (done_uhat) {
+            launch_copy(c, c.uhat, done_uhat, c.g.nUV);
+            launch_copy(c, c.p, done_p, c.g.nP);
             ++A.solves_reused;
         } else {
             phase_solve_velocity(c, false);
@@ -904,7 +929,8 @@ struct Runner {
     }
 
     static double beta(int s, int r)
-    {  // C(s + r, s), saturated
+    {  // C(s + r, s), saturated; 0 for r < 0
+        if (r < 0) return 0;
         double b = 1;
         for (int k = 1; k <= s; ++k) {
             b = b * (r + k) / k;
@@ -913,7 +939,13 @@ struct Runner {
         return b;
     }
 
-    // Reverse steps a+1..b; the state after step a is in snapshot slot_a; s more slots free.
+    // Reverse steps a+1..b; the state after step a is in snapshot slot_a; s more slots
+    // free.  Binomial checkpointing (Griewank and Walther, "Algorithm 799: revolve", ACM
+    // TOMS 26, 2000): with r the least repetition count for which beta(s, r) >= t = b - a
+    // steps can be reversed, the checkpoint goes after m - a steps with m - a in
+    //   [max(beta(s, r-2), t - beta(s-1, r)), min(beta(s, r-1), t - beta(s-1, r-1))],
+    // the range where the right part (s - 1 free slots) and the left part (s slots)
+    // together advance the fewest steps, r t - beta(s+1, r-1) in all.
     void reverse(int a, int b, int s, int slot_a)
     {
         if (b - a == 1) {
@@ -926,6 +958,8 @@ struct Runner {
             for (int k = b; k > a; --k) {
                 restore(slot_a);
                 advance(a, k - 1);
+                // the advance's last step is the one the next tape recomputes
+                if (k - 1 > a) stash_solutions(k - 1, c.uhat, c.p, k);
                 tape(k);
                 reverse_step(k);
             }
@@ -934,21 +968,17 @@ struct Runner {
         const int t = b - a;
         int r = 1;
         while (beta(s, r) < t) ++r;
-        int m = a + std::max(1, t - (int)std::min<double>(beta(s - 1, r), 1e9));
-        m = std::min(m, b - 1);
+        const double lo = std::max(beta(s, r - 2), t - beta(s - 1, r));
+        const int m = a + (int)std::min<double>(std::max(1.0, lo), t - 1);
         restore(slot_a);
         advance(a, m);
         const int slot_m = save(m);
         reverse(m, b, s - 1, slot_m);
-        if (s - 1 >= m - a - 1) {
-            // snapshots to spare: keep the state after step m while reversing a..m, whose
-            // last tape takes step m's solutions from it
-            reverse(a, m, s - 1, slot_a);
-            A.snaps[slot_m].holds = -1;
-        } else {
-            A.snaps[slot_m].holds = -1;
-            reverse(a, m, s, slot_a);
-        }
+        // the left part's first tape is step m: its solutions go to a stash, the slot is free
+        Snapshot &sm = A.snaps[slot_m];
+        stash_solutions(m, sm.blk + A.nUV, sm.blk + 3 * (size_t)A.nUV, -2);
+        sm.holds = -1;
+        reverse(a, m, s, slot_a);
     }
 };
 
@@ -999,6 +1029,7 @@ void run_adjoint(Context &c, int nsteps, int snapshots, const double *wx, const 
     A.S1T.rtol = A.S2T.rtol = adjoint_rtol;
     A.forward_steps = A.tape_steps = A.solves_reused = A.it1 = A.it2 = 0;
     for (auto &s : A.snaps) s.holds = -1;
+    A.stash_step[0] = A.stash_step[1] = -1;
     CUIBM_TRY(cudaMemsetAsync(A.scal, 0, (2 + 2 * (size_t)nsteps) * sizeof(double), c.stream));
     CUIBM_TRY(cudaMemsetAsync(A.ubar, 0, A.nUV * sizeof(double), c.stream));
     CUIBM_TRY(cudaMemsetAsync(A.Nbar, 0, A.nUV * sizeof(double), c.stream));

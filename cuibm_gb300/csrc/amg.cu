@@ -22,6 +22,7 @@
 #include "amg.h"
 #include "operators.cuh"
 #include "solver.h"
+#include "structured.cuh"
 
 namespace cuibm {
 
@@ -295,8 +296,16 @@ static DevCsr upload(Context &c, LinearSystem &S, const HostCsr &H)
     return D;
 }
 
+static bool structured_applies(const Context &c, const LinearSystem &S);
+static void build_structured_hierarchy(Context &c, LinearSystem &S);
+
 void build_sa_hierarchy(Context &c, LinearSystem &S)
 {
+    S.sa_structured = structured_applies(c, S);
+    if (S.sa_structured) {
+        build_structured_hierarchy(c, S);
+        return;
+    }
     std::vector<double> wh;
     if (S.w) {
         wh.resize(S.n);
@@ -413,6 +422,24 @@ double sa_vcycle_bytes(const LinearSystem &S)
     auto csr = [](const DevCsr &M) { return 12.0 * M.nnz + 4.0 * (M.n + 1); };
     const int nl = (int)S.amg.size();
     double b = 0;
+    if (S.sa_structured) {
+        // the structured cycle: below level 0 the operator is nine coefficients a node,
+        // the prolongator four weights a node (read by the restriction and the prolongation)
+        for (int l = 0; l < nl; ++l) {
+            const SaLevel *L = S.amg[l];
+            const double n = L->n;
+            if (l + 1 == nl) {
+                b += 16.0 * n;
+                break;
+            }
+            const double nc = S.amg[l + 1]->n, a = l > 0 ? 72.0 * n : 0.0;
+            b += 32.0 * n + a;              // down: b, dinv in; x, r out
+            b += 8.0 * n + 32.0 * n + 8.0 * nc;  // restriction: r and the weights in, coarse b out
+            b += 8.0 * nc + 32.0 * n + 16.0 * n;  // prolongation into x
+            b += 32.0 * n + a;              // up
+        }
+        return b;
+    }
     for (int l = 0; l < nl; ++l) {
         const SaLevel *L = S.amg[l];
         const double n = L->n;
@@ -514,12 +541,312 @@ __global__ void k_dense_mv(int n, const double *__restrict__ inv, const double *
     if (lane == 0) x[row] = s;
 }
 
+// ---------------------------------------------------------------------------
+// structured hierarchy (structured.cuh): set-up on the device
+// ---------------------------------------------------------------------------
+// A coarse level's 9-point operator
+struct Row9 {
+    int nx, ny;
+    const double *c9;
+    template <class X>
+    __device__ __forceinline__ double row(int i, const X &x) const
+    {
+        return st_row9(nx, ny, c9, i, x);
+    }
+};
+
+// the Poisson system of the plain and external methods: its operator is the 5-point
+// QTBNQ on the pressure grid at every row (pins change diagonals only), and it is fixed
+static bool structured_applies(const Context &c, const LinearSystem &S)
+{
+    return c.P.saStructured && S.which == 2 && S.precond == PC_SMOOTHED_AGGREGATION && !S.sa_dynamic &&
+           (c.P.solverType == ST_NAVIERSTOKES || c.P.solverType == ST_LUO) && !c.l2.patch.pid &&
+           S.n == c.g.nx * c.g.ny && S.n > kCoarse;
+}
+
+// diagonal of a level operator (row i against the unit vector e_i) and its inverse
+template <class Op>
+__global__ void k_st_diag(Op A, int n, double *__restrict__ dinv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = A.row(i, [i](int j) { return j == i ? 1.0 : 0.0; });
+    if (d == 0) d = 1.0;
+    dinv[i] = 1.0 / d;
+}
+
+// power iteration for rho(D^-1 A): y = D^-1 A x and the block sums of y^2 (summed in a
+// fixed order by k_st_sum, so the estimate is the same on every run)
+template <class Op>
+__global__ void k_st_rho_apply(Op A, int n, const double *__restrict__ dinv, const double *__restrict__ x,
+                               double *__restrict__ y, double *__restrict__ part)
+{
+    __shared__ double sh[kBlock / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0;
+    if (i < n) {
+        v = dinv[i] * A.row(i, PtrAccess{x});
+        y[i] = v;
+    }
+    v *= v;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < (int)blockDim.x / 32; ++k) t += sh[k];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_st_sum(int nb, const double *__restrict__ part, double *__restrict__ out)
+{
+    __shared__ double sh[kBlock];
+    double t = 0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) t += part[k];
+    sh[threadIdx.x] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int k = 0; k < (int)blockDim.x; ++k) s += sh[k];
+        *out = s;
+    }
+}
+
+__global__ void k_st_normalise(int n, const double *__restrict__ y, const double *__restrict__ sq,
+                               double *__restrict__ x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = y[i] / sqrt(*sq);
+}
+
+__global__ void k_st_scale(int n, const double *__restrict__ a, double s, double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = s * a[i];
+}
+
+// the prolongator's weights: P_iJ = [i in J] - w D^-1_i (A 1_J)_i for J the aggregates
+// around node i, (A 1_J)_i being row i against the indicator of aggregate J
+template <class Op>
+__global__ void k_st_weights(Op A, int nx, int ny, int cnx, int cny, const double *__restrict__ dinv, double omega,
+                             double *__restrict__ pw)
+{
+    const int n = nx * ny;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int iy = i / nx, ix = i - iy * nx;
+    const StAxis ax = st_axis(ix, nx, cnx), ay = st_axis(iy, ny, cny);
+    const double wdi = omega * dinv[i];
+    auto weight = [&](int jx, int jy) {
+        const double a = A.row(i, [&](int k) {
+            const int ky = k / nx, kx = k - ky * nx;
+            return st_axis(kx, nx, cnx).a == jx && st_axis(ky, ny, cny).a == jy ? 1.0 : 0.0;
+        });
+        return (ax.a == jx && ay.a == jy ? 1.0 : 0.0) - wdi * a;
+    };
+    pw[i] = weight(ax.a, ay.a);
+    pw[n + i] = ax.s ? weight(ax.a + ax.s, ay.a) : 0.0;
+    pw[2 * n + i] = ay.s ? weight(ax.a, ay.a + ay.s) : 0.0;
+    pw[3 * n + i] = ax.s && ay.s ? weight(ax.a + ax.s, ay.a + ay.s) : 0.0;
+}
+
+// Galerkin product by probing: with the coarse nodes coloured (Jx mod 3, Jy mod 3),
+// (P^T A P e_c)_J for the indicator e_c of one colour is the one entry of row J of the
+// 9-point coarse operator whose neighbour has that colour
+__global__ void k_st_probe_prolong(int nx, int ny, int cnx, int cny, const double *__restrict__ pw, int cx, int cy,
+                                   double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx * ny) return;
+    y[i] = st_prolong(nx, ny, cnx, cny, pw, i, [&](int J) {
+        const int Jy = J / cnx, Jx = J - Jy * cnx;
+        return Jx % 3 == cx && Jy % 3 == cy ? 1.0 : 0.0;
+    });
+}
+
+template <class Op>
+__global__ void k_st_apply(Op A, int n, const double *__restrict__ x, double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = A.row(i, PtrAccess{x});
+}
+
+__global__ void k_st_probe_restrict(int nx, int ny, int cnx, int cny, const double *__restrict__ pw, int cx, int cy,
+                                    const double *__restrict__ w, double *__restrict__ c9)
+{
+    const int nc = cnx * cny;
+    const int J = blockIdx.x * blockDim.x + threadIdx.x;
+    if (J >= nc) return;
+    const double v = st_restrict(nx, ny, cnx, cny, pw, J, PtrAccess{w});
+    const int Jy = J / cnx, Jx = J - Jy * cnx;
+    int dx = (cx - Jx % 3 + 3) % 3, dy = (cy - Jy % 3 + 3) % 3;
+    if (dx == 2) dx = -1;
+    if (dy == 2) dy = -1;
+    const bool inside = Jx + dx >= 0 && Jx + dx < cnx && Jy + dy >= 0 && Jy + dy < cny;
+    c9[(3 * (dy + 1) + dx + 1) * nc + J] = inside ? v : 0.0;
+}
+
+// prolongation added to the level's iterate: x += P xc
+__global__ void k_st_prolong_add(int nx, int ny, int cnx, int cny, const double *__restrict__ pw,
+                                 const double *__restrict__ xc, double *__restrict__ x, const int *gate)
+{
+    if (gate && *gate != KS_RUNNING) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nx * ny) x[i] += st_prolong(nx, ny, cnx, cny, pw, i, PtrAccess{xc});
+}
+
+// restriction: bc = P^T r
+__global__ void k_st_restrict(int nx, int ny, int cnx, int cny, const double *__restrict__ pw,
+                              const double *__restrict__ r, double *__restrict__ bc, const int *gate)
+{
+    if (gate && *gate != KS_RUNNING) return;
+    const int J = blockIdx.x * blockDim.x + threadIdx.x;
+    if (J < cnx * cny) bc[J] = st_restrict(nx, ny, cnx, cny, pw, J, PtrAccess{r});
+}
+
+// One level of the structured set-up: Jacobi tables, rho(D^-1 A) by 20 power
+// iterations (from the graph set-up's start vector), the prolongator's weights and the
+// next level's 9-point operator (nine probes).  Returns the next level's coefficients.
+template <class Op>
+static double *st_level(Context &c, LinearSystem &S, const Op &A, SaLevel *L, double *scratch)
+{
+    const int n = L->n, nx = L->nx, ny = L->ny, nb = blocks_for(n);
+    k_st_diag<<<nb, kBlock, 0, c.stream>>>(A, n, L->dinv);
+    double *xv = scratch, *yv = scratch + n, *wv = scratch + 2 * (size_t)n, *part = scratch + 3 * (size_t)n;
+    double *acc = part + nb;
+    std::vector<double> x0(n);
+    double nrm = 0;
+    for (int i = 0; i < n; ++i) {
+        x0[i] = 1.0 + 0.25 * std::sin(0.37 * i);
+        nrm += x0[i] * x0[i];
+    }
+    nrm = std::sqrt(nrm);
+    for (double &v : x0) v /= nrm;
+    CUIBM_TRY(cudaMemcpyAsync(xv, x0.data(), n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    constexpr int kIts = 20;
+    for (int it = 0; it < kIts; ++it) {
+        k_st_rho_apply<<<nb, kBlock, 0, c.stream>>>(A, n, L->dinv, xv, yv, part);
+        k_st_sum<<<1, kBlock, 0, c.stream>>>(nb, part, acc + it);
+        k_st_normalise<<<nb, kBlock, 0, c.stream>>>(n, yv, acc + it, xv);
+    }
+    double sq = 0;
+    CUIBM_TRY(cudaMemcpyAsync(&sq, acc + kIts - 1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));  // x0 and sq
+    const double rho = std::sqrt(sq);
+    if (!(rho > 0) || !std::isfinite(rho)) throw CudaError("structured smoothed aggregation: no spectral radius");
+    L->omega = 4.0 / (3.0 * rho);
+    L->wd = sa_alloc<double>(c, S, n);
+    k_st_scale<<<nb, kBlock, 0, c.stream>>>(n, L->dinv, L->omega, L->wd);
+    const int cnx = st_coarse(nx), cny = st_coarse(ny), nc = cnx * cny;
+    L->pw = sa_alloc<double>(c, S, 4 * (size_t)n);
+    k_st_weights<<<nb, kBlock, 0, c.stream>>>(A, nx, ny, cnx, cny, L->dinv, L->omega, L->pw);
+    double *c9 = sa_alloc<double>(c, S, 9 * (size_t)nc);
+    for (int cy = 0; cy < 3; ++cy)
+        for (int cx = 0; cx < 3; ++cx) {
+            k_st_probe_prolong<<<nb, kBlock, 0, c.stream>>>(nx, ny, cnx, cny, L->pw, cx, cy, yv);
+            k_st_apply<<<nb, kBlock, 0, c.stream>>>(A, n, yv, wv);
+            k_st_probe_restrict<<<blocks_for(nc), kBlock, 0, c.stream>>>(nx, ny, cnx, cny, L->pw, cx, cy, wv, c9);
+        }
+    CUIBM_TRY(cudaGetLastError());
+    return c9;
+}
+
+static void build_structured_hierarchy(Context &c, LinearSystem &S)
+{
+    Lvl0 A0{S.which, c.l1, c.l2, c.g, S.w};
+    const int n0 = S.n;
+    double *scratch = c.carve<double>(4 * (size_t)n0 + blocks_for(n0) + 64);
+    int nx = c.g.nx, ny = c.g.ny;
+    const double *c9 = nullptr;  // the current level's operator (levels below 0)
+    for (int lev = 0; lev < 25; ++lev) {
+        SaLevel *L = new SaLevel();
+        L->n = nx * ny;
+        L->nx = nx;
+        L->ny = ny;
+        L->c9 = const_cast<double *>(c9);
+        L->dinv = sa_alloc<double>(c, S, L->n);
+        L->x = sa_alloc<double>(c, S, L->n);
+        L->b = sa_alloc<double>(c, S, L->n);
+        L->r = sa_alloc<double>(c, S, L->n);
+        L->t = sa_alloc<double>(c, S, L->n);
+        const bool coarsest = lev > 0 && (L->n <= kCoarse || lev == 24);
+        if (coarsest) {
+            // the 9-point operator to the host, its dense inverse back
+            std::vector<double> h(9 * (size_t)L->n);
+            CUIBM_TRY(cudaMemcpyAsync(h.data(), c9, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            HostCsr H;
+            H.n = H.m = L->n;
+            H.ptr.assign(L->n + 1, 0);
+            for (int i = 0; i < L->n; ++i) {
+                const int iy = i / nx, ix = i - iy * nx;
+                for (int k = 0; k < 9; ++k) {
+                    const int dy = k / 3 - 1, dx = k % 3 - 1;
+                    const double v = h[(size_t)k * L->n + i];
+                    if (v == 0 || ix + dx < 0 || ix + dx >= nx || iy + dy < 0 || iy + dy >= ny) continue;
+                    H.col.push_back(i + dy * nx + dx);
+                    H.val.push_back(v);
+                }
+                H.ptr[i + 1] = (int)H.col.size();
+            }
+            k_st_diag<<<blocks_for(L->n), kBlock, 0, c.stream>>>(Row9{nx, ny, c9}, L->n, L->dinv);
+            std::vector<double> inv;
+            dense_inverse(H, inv);
+            L->coarse_inv = sa_alloc<double>(c, S, inv.size());
+            CUIBM_TRY(cudaMemcpyAsync(L->coarse_inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                      c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            S.amg.push_back(L);
+            break;
+        }
+        c9 = lev == 0 ? st_level(c, S, A0, L, scratch) : st_level(c, S, Row9{nx, ny, c9}, L, scratch);
+        S.amg.push_back(L);
+        nx = st_coarse(nx);
+        ny = st_coarse(ny);
+    }
+    CUIBM_TRY(cudaStreamSynchronize(c.stream));
+}
+
 // z = V(r): r on level 0 is the Krylov residual, z the preconditioned vector
 void launch_vcycle(Context &c, LinearSystem &S, const double *r, double *z)
 {
     const int nl = (int)S.amg.size();
     const int *gate = &S.ks->status;
     Lvl0 A0{S.which, c.l1, c.l2, c.g, S.w};
+    if (S.sa_structured) {
+        const double *bl = r;
+        for (int l = 0; l < nl - 1; ++l) {
+            SaLevel *L = S.amg[l], *C = S.amg[l + 1];
+            if (l == 0)
+                k_sa_down<<<blocks_for(L->n), kBlock, 0, c.stream>>>(A0, L->n, bl, L->dinv, L->omega, L->x, L->r,
+                                                                     gate);
+            else
+                k_sa_down<<<blocks_for(L->n), kBlock, 0, c.stream>>>(Row9{L->nx, L->ny, L->c9}, L->n, bl, L->dinv,
+                                                                     L->omega, L->x, L->r, gate);
+            k_st_restrict<<<blocks_for(C->n), kBlock, 0, c.stream>>>(L->nx, L->ny, C->nx, C->ny, L->pw, L->r, C->b,
+                                                                      gate);
+            bl = C->b;
+        }
+        SaLevel *C = S.amg[nl - 1];
+        k_dense_mv<<<(C->n + 7) / 8, 256, 0, c.stream>>>(C->n, C->coarse_inv, C->b, C->x, gate);
+        const double *xup = C->x;
+        for (int l = nl - 2; l >= 0; --l) {
+            SaLevel *L = S.amg[l], *Cl = S.amg[l + 1];
+            k_st_prolong_add<<<blocks_for(L->n), kBlock, 0, c.stream>>>(L->nx, L->ny, Cl->nx, Cl->ny, L->pw, xup,
+                                                                         L->x, gate);
+            double *out = (l == 0) ? z : L->t;
+            const double *bb = (l == 0) ? r : L->b;
+            if (l == 0)
+                k_sa_up<<<blocks_for(L->n), kBlock, 0, c.stream>>>(A0, L->n, bb, L->dinv, L->omega, L->x, out, gate);
+            else
+                k_sa_up<<<blocks_for(L->n), kBlock, 0, c.stream>>>(Row9{L->nx, L->ny, L->c9}, L->n, bb, L->dinv,
+                                                                   L->omega, L->x, out, gate);
+            xup = out;
+        }
+        CUIBM_TRY(cudaGetLastError());
+        return;
+    }
     // downward
     const double *bl = r;
     for (int l = 0; l < nl - 1; ++l) {
@@ -568,6 +895,8 @@ static void *sa_block(LinearSystem &S, size_t bytes)
 
 void ensure_transposed_levels(Context &c, LinearSystem &S)
 {
+    if (S.sa_structured)
+        throw InputError("the transposed cycle takes the graph-aggregated hierarchy (-saStructured 0)");
     for (size_t l = 0; l < S.amg.size(); ++l) {
         SaLevel *L = S.amg[l];
         if (l > 0 && !L->AT.ptr) {

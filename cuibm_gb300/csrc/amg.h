@@ -25,6 +25,11 @@ struct SaLevel {
     // levels below the finest, the transposed dense inverse on the coarsest
     DevCsr AT;
     double *coarse_inv_t = nullptr;
+    // structured hierarchy (structured.cuh): the level's grid (nx = 0: CSR level), its
+    // 9-point operator below level 0 and its prolongator's four weights a node
+    int nx = 0, ny = 0;
+    double *c9 = nullptr;
+    double *pw = nullptr;
 };
 
 }  // namespace cuibm

@@ -696,6 +696,7 @@ int cuibm_get_info(const cuibm_ctx *h, cuibm_info *info)
     info->velocity_precision = c.P.velocity.precision;
     info->poisson_precision = c.P.poisson.precision;
     info->sa_rebuilds = c.sa_rebuilds;
+    info->sa_structured = c.sys2.sa_structured ? 1 : 0;
     info->amg_levels = (int)c.sys2.amg.size();
     return CUIBM_OK;
 }
@@ -829,6 +830,18 @@ int cuibm_run(cuibm_ctx *h, int op)
         case CUIBM_OP_SURFACE_FORCE_CORRECTED: need_ib(); launch_surface_force(c, 2, false); break;
         case CUIBM_OP_APPLY_LHS1_T: apply_transposed(c, 1, c.work_x, c.work_y); break;
         case CUIBM_OP_APPLY_LHS2_T: apply_transposed(c, 2, c.work_x, c.work_y); break;
+        case CUIBM_OP_PRECONDITION_POISSON: {
+            LinearSystem &S = c.sys2;
+            if (S.amg.empty()) throw InputError("the Poisson system has no smoothed-aggregation preconditioner");
+            // the cycle's kernels run while the system's status word says a solve runs
+            int saved = 0, running = KS_RUNNING;
+            CUIBM_TRY(cudaMemcpyAsync(&saved, &S.ks->status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            CUIBM_TRY(cudaStreamSynchronize(c.stream));
+            CUIBM_TRY(cudaMemcpyAsync(&S.ks->status, &running, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+            launch_vcycle(c, S, c.work_x, c.work_y);
+            CUIBM_TRY(cudaMemcpyAsync(&S.ks->status, &saved, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+            break;
+        }
         default: return fail(h, CUIBM_ERR_BAD_INPUT, "unknown operation " + std::to_string(op));
         }
         CUIBM_TRY(cudaStreamSynchronize(c.stream));
@@ -994,7 +1007,6 @@ int cuibm_profile_kernel(cuibm_ctx *h, const char *kernel, int reps, double *avg
             int sms = 0;
             CUIBM_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
             const int blocks = 8 * sms;  // 8 blocks of 256 threads per SM
-            if ((size_t)blocks * 256 > (size_t)c.g.nUV) return fail(h, CUIBM_ERR_BAD_INPUT, "grid too small for fp64_fma");
             launch = [&, blocks] { b = launch_fp64_fma(c, blocks, c.work_y); };
         } else if (k == "poisson_vcycle") {
             if (c.sys2.amg.empty()) return fail(h, CUIBM_ERR_BAD_INPUT, "the Poisson system has no SA hierarchy");

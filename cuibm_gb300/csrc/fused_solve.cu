@@ -66,6 +66,7 @@
 
 #include "amg.h"
 #include "operators.cuh"
+#include "structured.cuh"
 #include "solver.h"
 
 namespace cuibm {
@@ -90,6 +91,10 @@ struct FLevel {
     const T *wd;  // omega D^-1
     T *x, *b, *r, *t;
     const double *inv;  // coarsest level: dense inverse, FP64 in every precision (dense_solve)
+    // structured hierarchy (structured.cuh): the level's grid, its 9-point operator
+    // (below level 0) and its prolongator's weights
+    int nx, ny;
+    const T *c9, *pw;
 };
 
 // Everything a solve needs except its right-hand side and solution, built once
@@ -107,6 +112,7 @@ struct FArgs {
     int *err;
     int which;
     int nlev;
+    int st;  // the hierarchy is the structured one
     FLevel<T> lev[kMaxLevels];
     // mixed precision, float side: the FP32 cycle's input (SA) or the inner system's
     // right-hand side and solution (refinement)
@@ -493,6 +499,146 @@ __device__ __forceinline__ void dense_solve(const FLevel<T> &C, const T *b, T *x
     }
 }
 
+// The end of a cycle on level l = 0: out = x + w D^-1 (b - A x) written to zout, with
+// b0 . out (dot) or wdot . out reduced, or a plain barrier
+template <class T>
+__device__ __forceinline__ bool cycle_end(const FArgs<T> &a, T v0, double vw, bool dot, const double *wdot,
+                                          double rho_prev, double &rz, double &beta, int &parity, double *wz)
+{
+    if (dot) {
+        T v[1] = {v0};
+        double vd[1], q[2];
+        to_double(v, vd);
+        if (!grid_reduce<1, 2>(vd, a, parity, [&](const double (&t)[1], double (&o)[2]) {
+                o[0] = t[0];
+                o[1] = t[0] / rho_prev;
+            }, q))
+            return false;
+        rz = q[0];
+        beta = q[1];
+    } else if (wdot) {
+        double vd[1] = {vw}, q[1];
+        if (!grid_reduce<1, 1>(vd, a, parity, [&](const double (&t)[1], double (&o)[1]) { o[0] = t[0]; }, q))
+            return false;
+        *wz = q[0];
+    } else if (!grid_sync(a.sync, a.trace)) {
+        return false;
+    }
+    return true;
+}
+
+// x_l = w D^-1 b_l + P x_l+1 at node k of level l, from the coarse values xc
+template <class T>
+struct StUp {
+    const FLevel<T> &V;
+    int cnx, cny;
+    const T *b, *xc;
+    __device__ __forceinline__ T operator()(int k) const
+    {
+        return V.wd[k] * __ldcg(b + k) + st_prolong(V.nx, V.ny, cnx, cny, V.pw, k, acc(xc));
+    }
+};
+// r_l = b_l - A_l (w D^-1 b_l) at node k of a level below 0
+template <class T>
+struct StRes {
+    const FLevel<T> &V;
+    __device__ __forceinline__ T operator()(int k) const
+    {
+        return __ldcg(V.b + k) - st_row9(V.nx, V.ny, V.c9, k, scaled(acc(V.b), V.wd));
+    }
+};
+
+// The structured hierarchy's cycle after its first phase: the same cycle as below
+// (one damped-Jacobi sweep from zero down, one up, R = P^T), with the prolongator as
+// four weights a node and 9-point coarse operators, so that no phase loads a column
+// index.  FP64: up, x_l = w D^-1 b_l + P x_l+1 is stored (one phase), then out_l = x_l +
+// w D^-1 (b_l - A_l x_l) (the next); down, r_l then its restriction.  FP32 (the mixed
+// solver's cycle): each pair is one phase, the stored value recomputed where the
+// second needs it - a few dozen FP32 operations a node, against FP64 issue at 1/64 of
+// the FP32 rate, which is why the FP64 cycle stores it instead.
+template <class Op, class T, class TO>
+__device__ __forceinline__ bool vcycle_rest_st(const Op &A, const FArgs<T> &a, const T *b0, TO *zout, bool dot,
+                                               double rho_prev, double &rz, double &beta, int &parity,
+                                               const double *wdot, double *wz)
+{
+    constexpr bool kFuse = sizeof(T) == 4;
+    const int L = a.nlev;
+    for (int l = 0; l < L - 1; ++l) {
+        const FLevel<T> &V = a.lev[l];
+        const FLevel<T> &C = a.lev[l + 1];
+        if (kFuse && l > 0) {
+            FOR_ROWS(J, C.n) C.b[J] = st_restrict(V.nx, V.ny, C.nx, C.ny, V.pw, J, StRes<T>{V});
+            if (!grid_sync(a.sync, a.trace)) return false;
+            continue;
+        }
+        if (l > 0) {
+            FOR_ROWS(i, V.n) V.r[i] = __ldcg(V.b + i) - st_row9(V.nx, V.ny, V.c9, i, scaled(acc(V.b), V.wd));
+            if (!grid_sync(a.sync, a.trace)) return false;
+        }
+        FOR_ROWS(J, C.n) C.b[J] = st_restrict(V.nx, V.ny, C.nx, C.ny, V.pw, J, acc(V.r));
+        if (!grid_sync(a.sync, a.trace)) return false;
+    }
+    const FLevel<T> &C = a.lev[L - 1];
+    dense_solve(C, C.b, C.x);
+    if (!grid_sync(a.sync, a.trace)) return false;
+    const T *xc = C.x;
+    for (int l = L - 2; l >= 0; --l) {
+        const FLevel<T> &V = a.lev[l];
+        const FLevel<T> &Cn = a.lev[l + 1];
+        const T *bb = l == 0 ? b0 : V.b;
+        if (kFuse) {
+            const StUp<T> up{V, Cn.nx, Cn.ny, bb, xc};
+            T v0 = 0;
+            double vw = 0;
+            if (l == 0) {
+                FOR_ROWS(i, V.n)
+                {
+                    const T xi = up(i);
+                    const T o = xi + V.wd[i] * (__ldcg(bb + i) - A.row_x(i, xi, up));
+                    zout[i] = (TO)o;
+                    if (dot) v0 += __ldcg(b0 + i) * o;
+                    if (wdot) vw += wdot[i] * (double)o;
+                }
+                if (!cycle_end(a, v0, vw, dot, wdot, rho_prev, rz, beta, parity, wz)) return false;
+            } else {
+                FOR_ROWS(i, V.n)
+                {
+                    const T xi = up(i);
+                    V.t[i] = xi + V.wd[i] * (__ldcg(bb + i) - st_row9(V.nx, V.ny, V.c9, i, up));
+                }
+                if (!grid_sync(a.sync, a.trace)) return false;
+            }
+            xc = V.t;
+            continue;
+        }
+        FOR_ROWS(i, V.n)
+        V.x[i] = V.wd[i] * __ldcg(bb + i) + st_prolong(V.nx, V.ny, Cn.nx, Cn.ny, V.pw, i, acc(xc));
+        if (!grid_sync(a.sync, a.trace)) return false;
+        if (l == 0) {
+            T v0 = 0;
+            double vw = 0;
+            FOR_ROWS(i, V.n)
+            {
+                const T xi = __ldcg(V.x + i);
+                const T o = xi + V.wd[i] * (__ldcg(bb + i) - A.row_x(i, xi, acc((const T *)V.x)));
+                zout[i] = (TO)o;
+                if (dot) v0 += __ldcg(b0 + i) * o;
+                if (wdot) vw += wdot[i] * (double)o;
+            }
+            if (!cycle_end(a, v0, vw, dot, wdot, rho_prev, rz, beta, parity, wz)) return false;
+        } else {
+            FOR_ROWS(i, V.n)
+            {
+                const T xi = __ldcg(V.x + i);
+                V.t[i] = xi + V.wd[i] * (__ldcg(bb + i) - st_row9(V.nx, V.ny, V.c9, i, acc((const T *)V.x)));
+            }
+            if (!grid_sync(a.sync, a.trace)) return false;
+        }
+        xc = V.t;
+    }
+    return true;
+}
+
 // The cycle after its first phase (r_0 written, barrier passed).  b0 is the
 // cycle's input (stored); the output zout may have another precision.  With dot,
 // returns b0 . z; with wdot (and no dot), returns wdot . z in *wz.
@@ -501,6 +647,7 @@ __device__ __forceinline__ bool vcycle_rest(const Op &A, const FArgs<T> &a, cons
                                             double rho_prev, double &rz, double &beta, int &parity,
                                             const double *wdot = nullptr, double *wz = nullptr)
 {
+    if (a.st) return vcycle_rest_st(A, a, b0, zout, dot, rho_prev, rz, beta, parity, wdot, wz);
     const int L = a.nlev;
     for (int l = 0; l < L - 1; ++l) {
         const FLevel<T> &V = a.lev[l];
@@ -1476,7 +1623,12 @@ static void upload_fargs(Context &c, LinearSystem &S)
         F.r = L->r;
         F.t = L->t;
         F.inv = L->coarse_inv;
+        F.nx = L->nx;
+        F.ny = L->ny;
+        F.c9 = L->c9;
+        F.pw = L->pw;
     }
+    a.st = S.sa_structured;
     a.ym = S.ym;
     a.wdef = S.wdef;
     a.Edef = S.Edef;
@@ -1554,7 +1706,12 @@ static void setup_mixed(Context &c, LinearSystem &S)
         F.r = c.carve<float>(L->n);
         F.t = c.carve<float>(L->n);
         F.inv = L->coarse_inv;  // shared: the coarse solve runs in FP64
+        F.nx = L->nx;
+        F.ny = L->ny;
+        F.c9 = L->c9 ? to_float(c, L->c9, 9 * (size_t)L->n) : nullptr;
+        F.pw = L->pw ? to_float(c, L->pw, 4 * (size_t)L->n) : nullptr;
     }
+    f.st = S.sa_structured;
     m->dev = c.carve<FArgs<float>>(1);
     CUIBM_TRY(cudaMemcpyAsync(m->dev, &f, sizeof(f), cudaMemcpyHostToDevice, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
@@ -1648,6 +1805,19 @@ double solve_bytes(const LinearSystem &S, int it)
     // choice, not algorithmic: solve_dense_bytes reports it apart
     if (L == 1) {
         vc = 2 * DL * S.amg[0]->n;
+    } else if (L > 1 && S.sa_structured) {
+        // the structured cycle: the prolongator is four weights a node (read by the
+        // restriction and the prolongation), a coarse operator nine coefficients a node;
+        // the level-0 operator is the matrix-free one (its diagonal a value a node)
+        vc += 2 * DL * n;
+        for (int l = 0; l < L - 1; ++l) {
+            const double m = S.amg[l]->n, mc = S.amg[l + 1]->n, a9 = l > 0 ? 9 * DL * m : DL * m;
+            if (l > 0) vc += 3 * DL * m + a9;          // residual
+            vc += DL * m + 4 * DL * m + DL * mc;        // restriction
+            vc += 7 * DL * m + DL * mc;                 // x_l = w D^-1 b_l + P x_l+1
+            vc += 4 * DL * m + a9;                      // out_l = x_l + w D^-1 (b_l - A_l x_l)
+        }
+        vc += 2 * DL * S.amg[L - 1]->n;
     } else if (L > 1) {
         vc += 2 * DL * n;  // first sweep: omega D^-1 and r_0 (its input is counted by the caller)
         for (int l = 0; l < L - 1; ++l) {

@@ -28,7 +28,7 @@ struct InputError {
 };
 
 constexpr int kBlock = 256;
-constexpr int kTraceLen = 1024;  // timestamps kept per persistent solve (diagnostic trace)
+constexpr int kTraceLen = 4096;  // timestamps kept per persistent solve (diagnostic trace)
 inline int blocks_for(long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
 
 // ---- structured operators --------------------------------------------------
@@ -149,6 +149,9 @@ struct LinearSystem {
     // the SA hierarchy built from the operator without the body's patched rows (a moving
     // embedded body's option "sa_body_free"): it never needs rebuilding as the body moves
     bool sa_body_free = false;
+    // the hierarchy is the structured one (3 x 3 aggregates of the pressure grid, 9-point
+    // coarse operators, set up on the device; structured.cuh)
+    bool sa_structured = false;
     // the SA hierarchy in its own allocations (so that it can be rebuilt) and the
     // checksum of the patched-row pattern it was built from
     bool sa_dynamic = false;

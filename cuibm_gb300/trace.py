@@ -7,7 +7,7 @@ phase that ended at the second barrier (its work, its wait for the slowest block
 and the barrier itself), so summing by call site shows where a solve spends its
 time without a profiler.
 
-    python -m cuibm_gb300.trace CASE_FOLDER [--warm 20] [--system poisson]
+    python -m cuibm_gb300.trace CASE_FOLDER [--warm 20] [--system poisson] [--flags "-saStructured 0"]
 
 runs the case for --warm steps, traces the next step and prints, per barrier site
 of csrc/fused_solve.cu, the count, total and mean phase time.
@@ -22,7 +22,7 @@ SRC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "fused_so
 
 
 def phases(trace):
-    """(site line, microseconds) of every phase of one solve's trace (1024 entries)."""
+    """(site line, microseconds) of every phase of one solve's trace."""
     k = int(trace[0])
     e = np.asarray(trace[1:k + 1], dtype=np.uint64)
     ts = (e & np.uint64(0xFFFFFFFFFFFF)).astype(np.int64)
@@ -47,9 +47,10 @@ def main(argv=None):
     ap.add_argument("case")
     ap.add_argument("--warm", type=int, default=20)
     ap.add_argument("--system", choices=["velocity", "poisson", "both"], default="both")
+    ap.add_argument("--flags", default="", help="the solver's command-line flags, e.g. \"-saStructured 0\"")
     a = ap.parse_args(argv)
     src = open(SRC).read().split("\n") if os.path.exists(SRC) else []
-    with cb.NavierStokesSolver(a.case) as s:
+    with cb.NavierStokesSolver(a.case, a.flags.split()) as s:
         s.set_option("write_output", 0)
         s.initialise()
         s.stepTime(a.warm)
@@ -61,7 +62,8 @@ def main(argv=None):
         i = s.info
         print("case %s: %d x %d, SA levels %d, iterations (velocity, Poisson) %s at step %d" % (
             a.case, i.nx, i.ny, i.amg_levels, it, s.timeStep - 1))
-        for name, t in (("velocity", tr[:1024]), ("poisson", tr[1024:])):
+        half = len(tr) // 2
+        for name, t in (("velocity", tr[:half]), ("poisson", tr[half:])):
             if a.system not in (name, "both"):
                 continue
             ph = phases(t)

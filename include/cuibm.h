@@ -63,6 +63,9 @@ typedef struct {
     int amg_levels;                   /* levels of the Poisson SA hierarchy (0 if none) */
     int velocity_precision, poisson_precision; /* 0 FP64, 1 MIXED (simParams.yaml `precision`) */
     int sa_rebuilds;                  /* SA hierarchies rebuilt for a moving embedded body so far */
+    int sa_structured;                /* 1: the Poisson SA hierarchy is the structured one (3 x 3
+                                         aggregates of the pressure grid, 9-point coarse operators,
+                                         set up on the device; -saStructured 0 turns it off) */
 } cuibm_info;
 
 /* Fields readable/writable through cuibm_get_field / cuibm_set_field.
@@ -109,8 +112,8 @@ enum {
     CUIBM_F_CFL,             /* D P  */
     CUIBM_F_WORK_X,          /* D max(UV,P) operator test input  */
     CUIBM_F_WORK_Y,          /* D max(UV,P) operator test output */
-    CUIBM_F_SOLVE_TRACE,     /* uint64 2*1024: per-barrier timestamps (ns) of the last persistent
-                                velocity (first 1024) and Poisson solve: [count, start, ...], each
+    CUIBM_F_SOLVE_TRACE,     /* uint64 2*4096: per-barrier timestamps (ns) of the last persistent
+                                velocity (first 4096) and Poisson solve: [count, start, ...], each
                                 entry the timer's low 48 bits with the barrier's source line of
                                 fused_solve.cu in the top 16; written only while the option
                                 "trace_solve" is 1 */
@@ -161,6 +164,8 @@ enum {
     CUIBM_OP_SURFACE_FORCE_CORRECTED, /* the same with its two index slips corrected */
     CUIBM_OP_APPLY_LHS1_T,     /* WORK_Y = LHS1^T WORK_X (embedded method: the adjoint's operator) */
     CUIBM_OP_APPLY_LHS2_T,     /* WORK_Y = LHS2^T WORK_X */
+    CUIBM_OP_PRECONDITION_POISSON, /* WORK_Y = M WORK_X: one V-cycle of the Poisson system's
+                                      smoothed-aggregation preconditioner (stepwise kernels) */
     CUIBM_OP_COUNT
 };
 

@@ -10,8 +10,8 @@ grid and a few steps):
     against the oracle's FP64 tangent-linear model (oracle/tangent.py, the restated step
     on dual numbers) and against central finite differences of the GPU's own forward
     run (relative step 1e-6);
-  * binomial checkpointing with few snapshots gives the gradient of the stored-every-step
-    schedule;
+  * binomial checkpointing with few snapshots advances the fewest steps the schedule
+    allows and gives the gradient of the stored-every-step schedule;
   * a torch.autograd.Function (this file only) whose backward is cuibm_adjoint.
 Forward solves run to 1e-12 and the adjoint's transposed solves to 1e-12 here, so that
 the comparisons see the linearisation, not the Krylov stopping points."""
@@ -140,11 +140,25 @@ def test_gradient_against_finite_differences(case, adjoint_run, tmp_path):
     assert abs(grad[2] - fd_off) <= RTOL_FD * abs(fd_off)
 
 
+def binomial_advances(t, snapshots):
+    """The fewest forward steps that reverse t steps with the given snapshots, one of
+    them holding the initial state (Griewank and Walther, revolve): r t - C(s + r, r - 1)
+    with s = snapshots - 1 free slots and r the least count with C(s + r, s) >= t."""
+    from math import comb
+    s, r = snapshots - 1, 1
+    while comb(s + r, s) < t:
+        r += 1
+    return r * t - comb(s + r, r - 1)
+
+
 def test_checkpointing_schedule_does_not_change_the_gradient(case, adjoint_run):
     _, grad, stats_all = adjoint_run
     with solver(case) as s:
         J, g2, stats = s.adjoint(NT, 2.0 / NT, snapshots=3)
-    assert stats["forward_steps"] > stats_all["forward_steps"]  # recomputation from fewer snapshots
+    assert stats_all["forward_steps"] == binomial_advances(NT, NT) == NT - 1
+    assert stats["forward_steps"] == binomial_advances(NT, 3) == 28  # the fewest with 3 snapshots
+    # every taped step but the last takes its solutions from a snapshot or the stash
+    assert stats["solves_reused"] == NT - 1
     assert np.allclose(g2, grad, rtol=1e-8, atol=1e-12)
 
 
