@@ -296,57 +296,70 @@ def precision_comparison(local, warm=20, steps=20):
     """The Re 550 cylinder (922 x 922, 629 body points, dt 0.002, both solves to 1e-8),
     plain FP64 against precision MIXED on the same steps: steps warm+1 .. warm+steps of
     the impulsive start, timed with CUDA events on the solver's stream (the working set,
-    several hundred MB, is larger than L2).  C_D of both runs at the last step is
-    reported beside the times; at these tolerances both are within 1e-6 of a tightly
-    solved FP64 run.  Each precision also runs with the smoothed aggregation's
-    strengthThreshold at 0.05 (the reference's CUSP default is 0)."""
+    several hundred MB, is larger than L2).  Each precision runs with the structured
+    smoothed-aggregation hierarchy (the default at this size) and with the graph
+    aggregation (-saStructured 0).  Every run's C_D at each timed step is compared with
+    the FP64 oracle's (tests/golden/config_cylinder_re550.npz: the oracle's run of the
+    same configuration, both systems solved by sparse LU, steps 1-40)."""
+    import numpy as np
     import torch
 
     import cuibm_gb300 as cb
+    gold = os.path.join(ROOT, "tests", "golden", "config_cylinder_re550.npz")
+    cd_oracle = np.load(gold)["cd"] if os.path.exists(gold) else None
     out = {"workload": "impulsively started cylinder Re 550, external (Luo) method, 922x922, 629 points, "
                        "dt 0.002, BiCGSTAB + diagonal / smoothed aggregation, rtol 1e-8 both",
-           "steps_timed": "%d-%d" % (warm + 1, warm + steps)}
-    for prec, strength, key in (("FP64", None, "fp64"), ("MIXED", None, "mixed"),
-                                ("FP64", 0.05, "fp64_strength_0.05"), ("MIXED", 0.05, "mixed_strength_0.05")):
+           "steps_timed": "%d-%d" % (warm + 1, warm + steps),
+           "cd_reference": "FP64 oracle run (sparse LU solves), tests/golden/config_cylinder_re550.npz"}
+    for prec, flags, key in (("FP64", [], "fp64"), ("MIXED", [], "mixed"),
+                             ("FP64", ["-saStructured", "0"], "fp64_graph"),
+                             ("MIXED", ["-saStructured", "0"], "mixed_graph")):
         with tempfile.TemporaryDirectory() as tmp:
-            folder, cells = make_case("cylinder_re550", os.path.join(tmp, "case"), precision=prec,
-                                      strength=strength)
-            s = cb.NavierStokesSolver(folder, ["-deviceNumber", str(local)])
+            folder, cells = make_case("cylinder_re550", os.path.join(tmp, "case"), precision=prec)
+            s = cb.NavierStokesSolver(folder, ["-deviceNumber", str(local)] + flags)
             s.set_option("write_output", 0)
             s.initialise()
             s.stepTime(warm)
             stream = torch.cuda.ExternalStream(s.stream())
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(steps)]
+            cds = []
             torch.cuda.synchronize()
-            s.set_option("step_sync", 0)
-            e0.record(stream)
-            s.stepTime(steps)
-            e1.record(stream)
+            for k in range(steps):
+                # each step bracketed by its own events (the step's forces are read between
+                # steps, outside them)
+                ev[k][0].record(stream)
+                s.stepTime(1)
+                ev[k][1].record(stream)
+                cds.append(2 * s.forces()[0])
             torch.cuda.synchronize()
-            s.set_option("step_sync", 1)
-            s.stepTime(0)  # raises if a solve failed
-            ms = e0.elapsed_time(e1) / steps
-            fx, _ = s.forces()
-            out[key] = {"ms_per_step": round(ms, 4), "value": round(cells / ms / 1e3, 3), "unit": METRIC,
-                        "iterations_last_step": list(s.iterations()), "cd_last_step": 2 * fx}
+            ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / steps
+            rec = {"ms_per_step": round(ms, 4), "value": round(cells / ms / 1e3, 3), "unit": METRIC,
+                   "iterations_last_step": list(s.iterations()), "cd_last_step": cds[-1],
+                   "sa_structured": s.info.sa_structured}
+            if cd_oracle is not None and warm + steps <= len(cd_oracle):
+                err = np.abs(np.array(cds) - cd_oracle[warm:warm + steps])
+                rec["cd_error_vs_fp64_oracle_max"] = float(err.max())
+            out[key] = rec
             s.close()
     base = out["fp64"]
+    best64 = min(out["fp64"]["ms_per_step"], out["fp64_graph"]["ms_per_step"])
     out["speedup_mixed_over_fp64"] = round(base["ms_per_step"] / out["mixed"]["ms_per_step"], 3)
-    out["cd_difference"] = abs(base["cd_last_step"] - out["mixed"]["cd_last_step"])
-    best = out["mixed_strength_0.05"]
-    out["speedup_mixed_strength_over_fp64"] = round(base["ms_per_step"] / best["ms_per_step"], 3)
-    out["cd_difference_mixed_strength"] = abs(base["cd_last_step"] - best["cd_last_step"])
+    out["speedup_mixed_over_fastest_fp64"] = round(best64 / out["mixed"]["ms_per_step"], 3)
+    out["speedup_mixed_graph_over_fp64_graph"] = round(out["fp64_graph"]["ms_per_step"] /
+                                                       out["mixed_graph"]["ms_per_step"], 3)
     return out
 
 
-def batch_cases(tmp, n=64, seed=0):
+def batch_cases(tmp, n=64, seed=0, precision=None):
     """The batched workload: n instances drawn with numpy's default_rng(seed) - half
     lid-driven cavities (N from {96, 128, ..., 512}, Re log-uniform in [100, 1000]),
     half impulsively started cylinders (external method, the Re 40 case's stretching
     rule with core h from {0.04, 0.03, 0.02}, round(pi/h) body points made even, Re
     log-uniform in [40, 300], dt 0.005).  The cavities' dt is 0.01 x 64/N (CFL 0.64,
     as at 64 x 64): at dt 0.01 the finer cavities are unstable (CFL up to 5) and
-    overflow within a few dozen steps."""
+    overflow within a few dozen steps.  precision MIXED: both systems of every
+    instance in mixed precision (the same draws)."""
     import numpy as np
     from cuibm_gb300 import cases
     rng = np.random.default_rng(seed)
@@ -356,14 +369,15 @@ def batch_cases(tmp, n=64, seed=0):
             N = int(rng.choice(np.arange(96, 513, 32)))
             Re = float(np.exp(rng.uniform(np.log(100), np.log(1000))))
             f = cases.cavity(os.path.join(tmp, "cav%02d" % k), n=N, nu=1.0 / Re, dt=0.01 * 64 / N, nt=1000000,
-                             vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG")
+                             vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG",
+                             precision=precision)
         else:
             h = float(rng.choice([0.04, 0.03, 0.02]))
             Re = float(np.exp(rng.uniform(np.log(40), np.log(300))))
             pts = int(round(np.pi / h))
             pts += pts % 2
             f = cases.cylinder(os.path.join(tmp, "cyl%02d" % k), h=h, ratio=1.03, points=pts, nu=1.0 / Re, dt=0.005,
-                               nt=1000000)
+                               nt=1000000, precision=precision)
         out.append(f)
     return out
 
@@ -371,35 +385,37 @@ def batch_cases(tmp, n=64, seed=0):
 def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
     """The batched workload run as one batch (cuibm_batch_*: every instance on its own
     stream, the persistent solves' block count picked by the batch autotuner during
-    warm-up) and one instance after another (each with the whole GPU), both plain
-    FP64, timed over the same steps with wall-clock time around synchronised GPU work.
-    Aggregate Mcell-steps/s."""
+    warm-up), in plain FP64 and in mixed precision (the configuration's), and one
+    instance after another in plain FP64 (each with the whole GPU), timed over the same
+    steps with wall-clock time around synchronised GPU work.  Aggregate Mcell-steps/s."""
     import time as _time
 
     import torch
 
     import cuibm_gb300 as cb
     out = {"workload": "%d instances (seed 0): half lid-driven cavities N 96-512, half cylinders h 0.04-0.02, "
-                       "external method, FP64" % n}
+                       "external method" % n}
     with tempfile.TemporaryDirectory() as tmp:
-        folders = batch_cases(tmp, n)
-        b = cb.Batch(folders, ["-deviceNumber", str(local)])
-        for s in b.instances:
-            s.set_option("write_output", 0)
-        b.initialise()
-        b.stepTime(warm)
-        blocks = b.autotune(tune_steps)  # advances every instance by up to 10 x tune_steps
-        warm_all = b.instances[0].timeStep
-        cells = sum(s.info.numP for s in b.instances)
-        torch.cuda.synchronize()
-        t0 = _time.perf_counter()
-        b.stepTime(steps)
-        torch.cuda.synchronize()
-        el = _time.perf_counter() - t0
-        b.close()
-        out["steps_timed"] = "%d-%d" % (warm_all + 1, warm_all + steps)
-        out["batched"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC,
-                          "solver_blocks": blocks}
+        for prec, key in ((None, "batched"), ("MIXED", "batched_mixed")):
+            folders = batch_cases(os.path.join(tmp, key), n, precision=prec)
+            b = cb.Batch(folders, ["-deviceNumber", str(local)])
+            for s in b.instances:
+                s.set_option("write_output", 0)
+            b.initialise()
+            b.stepTime(warm)
+            blocks = b.autotune(tune_steps)  # advances every instance by up to 10 x tune_steps
+            warm_all = b.instances[0].timeStep
+            cells = sum(s.info.numP for s in b.instances)
+            torch.cuda.synchronize()
+            t0 = _time.perf_counter()
+            b.stepTime(steps)
+            torch.cuda.synchronize()
+            el = _time.perf_counter() - t0
+            b.close()
+            out["steps_timed"] = "%d-%d" % (warm_all + 1, warm_all + steps)
+            out[key] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC,
+                        "solver_blocks": blocks, "precision": prec or "FP64"}
+        folders = batch_cases(os.path.join(tmp, "sequential"), n)
         el = 0.0
         for f in folders:  # one after another, the same steps: each instance alone on the GPU
             s = cb.NavierStokesSolver(f, ["-deviceNumber", str(local)])
@@ -417,6 +433,7 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
             s.close()
         out["sequential"] = {"s": round(el, 4), "value": round(cells * steps / el / 1e6, 3), "unit": METRIC}
     out["speedup_batched_over_sequential"] = round(out["sequential"]["s"] / out["batched"]["s"], 3)
+    out["speedup_batched_mixed_over_sequential_fp64"] = round(out["sequential"]["s"] / out["batched_mixed"]["s"], 3)
     return out
 
 

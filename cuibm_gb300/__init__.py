@@ -233,7 +233,7 @@ class NavierStokesSolver:
         sizes = {"bc_xminus": 2 * ny - 1, "bc_xplus": 2 * ny - 1, "bc_yminus": 2 * nx - 1, "bc_yplus": 2 * nx - 1,
                  "x": nx, "dx": nx, "xu": nx - 1, "xv": nx, "y": ny, "dy": ny, "yu": ny, "yv": ny - 1,
                  "body_x": nb, "body_y": nb, "body_uB": nb, "body_vB": nb,
-                 "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 1024,
+                 "work_x": max(UV, P), "work_y": max(UV, P), "solve_trace": 2 * 4096,
                  "body_motion": 12, "surface_force": 3 * nb + 2, "forces": 2, "body_velocity_offset": 2 * nb}
         if name in sizes:
             return sizes[name]

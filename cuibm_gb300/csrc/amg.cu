@@ -555,11 +555,17 @@ struct Row9 {
     }
 };
 
-// the Poisson system of the plain and external methods: its operator is the 5-point
-// QTBNQ on the pressure grid at every row (pins change diagonals only), and it is fixed
+// The Poisson system of the plain and external methods: its operator is the 5-point
+// QTBNQ on the pressure grid at every row (pins change diagonals only), and it is
+// fixed.  By default from kStructuredMin unknowns: below, the graph aggregation's
+// smaller aggregates take fewer iterations (the Re 40 cylinder's steady state: 4
+// against 9) and the solve is bound by its phase count, not by the cycle's loads.
+constexpr int kStructuredMin = 200000;
+
 static bool structured_applies(const Context &c, const LinearSystem &S)
 {
-    return c.P.saStructured && S.which == 2 && S.precond == PC_SMOOTHED_AGGREGATION && !S.sa_dynamic &&
+    const bool want = c.P.saStructured == 1 || (c.P.saStructured == -1 && S.n >= kStructuredMin);
+    return want && S.which == 2 && S.precond == PC_SMOOTHED_AGGREGATION && !S.sa_dynamic &&
            (c.P.solverType == ST_NAVIERSTOKES || c.P.solverType == ST_LUO) && !c.l2.patch.pid &&
            S.n == c.g.nx * c.g.ny && S.n > kCoarse;
 }

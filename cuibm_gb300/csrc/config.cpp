@@ -524,7 +524,7 @@ std::string load_case(const std::string &folder_in, int argc, const char **argv,
         else if (!strcmp(a, "-solverPack"))
             ok = cli_value(argv[++i], P.solverPack) && (P.solverPack == 1 || P.solverPack == 2);
         else if (!strcmp(a, "-saStructured"))
-            ok = cli_value(argv[++i], P.saStructured) && (P.saStructured == 0 || P.saStructured == 1);
+            ok = cli_value(argv[++i], P.saStructured) && P.saStructured >= -1 && P.saStructured <= 1;
         else if (!strcmp(a, "-solverThreads"))
             ok = cli_value(argv[++i], P.solverThreads) && P.solverThreads >= 0 && P.solverThreads <= 512 &&
                  P.solverThreads % 32 == 0;

@@ -61,8 +61,8 @@ struct Params {
     int solverThreads = 0;  // -solverThreads: their block size (0: 512)
     int solverPack = 1;     // -solverPack 2: FP64 persistent solves built for two blocks per SM
                             // (64 registers a thread), so two solves can share an SM
-    int saStructured = 1;   // -saStructured 0: the Poisson system's smoothed aggregation by the
-                            // graph aggregation (host set-up) where the structured one applies
+    int saStructured = -1;  // -saStructured 1 / 0: the Poisson system's structured smoothed
+                            // aggregation wherever it applies / never (-1: from 200k unknowns)
     // flow
     double nu = 0.01, uInitial = 1.0, vInitial = 0.0, uPerturb = 0.0, vPerturb = 0.0;
     BC bc[4][2];

@@ -95,6 +95,7 @@ struct FLevel {
     // (below level 0) and its prolongator's weights
     int nx, ny;
     const T *c9, *pw;
+    int fz;  // structured: prolongation and smoothing sweep in one phase
 };
 
 // Everything a solve needs except its right-hand side and solution, built once
@@ -113,6 +114,11 @@ struct FArgs {
     int which;
     int nlev;
     int st;  // the hierarchy is the structured one
+    // the level-0 first sweep of the BiCGSTAB cycles in a phase of its own, from the
+    // stored direction or half step, instead of recomputing them at its stencil points
+    // inside the phase that writes them (large FP64 systems: the recomputation costs
+    // more FP64 issue than the extra barrier)
+    int split0;
     FLevel<T> lev[kMaxLevels];
     // mixed precision, float side: the FP32 cycle's input (SA) or the inner system's
     // right-hand side and solution (refinement)
@@ -538,39 +544,26 @@ struct StUp {
         return V.wd[k] * __ldcg(b + k) + st_prolong(V.nx, V.ny, cnx, cny, V.pw, k, acc(xc));
     }
 };
-// r_l = b_l - A_l (w D^-1 b_l) at node k of a level below 0
-template <class T>
-struct StRes {
-    const FLevel<T> &V;
-    __device__ __forceinline__ T operator()(int k) const
-    {
-        return __ldcg(V.b + k) - st_row9(V.nx, V.ny, V.c9, k, scaled(acc(V.b), V.wd));
-    }
-};
 
 // The structured hierarchy's cycle after its first phase: the same cycle as below
 // (one damped-Jacobi sweep from zero down, one up, R = P^T), with the prolongator as
 // four weights a node and 9-point coarse operators, so that no phase loads a column
-// index.  FP64: up, x_l = w D^-1 b_l + P x_l+1 is stored (one phase), then out_l = x_l +
-// w D^-1 (b_l - A_l x_l) (the next); down, r_l then its restriction.  FP32 (the mixed
-// solver's cycle): each pair is one phase, the stored value recomputed where the
-// second needs it - a few dozen FP32 operations a node, against FP64 issue at 1/64 of
-// the FP32 rate, which is why the FP64 cycle stores it instead.
+// index.  Down, r_l then its restriction (a coarse node's sum over the 5 x 5 nodes
+// around its aggregate: recomputing r_l there, 9 points each, would leave a few
+// thousand threads with hundreds of loads apiece).  Up, x_l = w D^-1 b_l + P x_l+1 is
+// stored (one phase), then out_l = x_l + w D^-1 (b_l - A_l x_l) (the next); on a level
+// with fz set the two are one phase, x_l recomputed at the sweep's stencil points: a
+// few dozen operations a node, which FP32 (the mixed solver's cycle, every level)
+// affords, and FP64 - issued at 1/64 of the FP32 rate - on the small levels only.
 template <class Op, class T, class TO>
 __device__ __forceinline__ bool vcycle_rest_st(const Op &A, const FArgs<T> &a, const T *b0, TO *zout, bool dot,
                                                double rho_prev, double &rz, double &beta, int &parity,
                                                const double *wdot, double *wz)
 {
-    constexpr bool kFuse = sizeof(T) == 4;
     const int L = a.nlev;
     for (int l = 0; l < L - 1; ++l) {
         const FLevel<T> &V = a.lev[l];
         const FLevel<T> &C = a.lev[l + 1];
-        if (kFuse && l > 0) {
-            FOR_ROWS(J, C.n) C.b[J] = st_restrict(V.nx, V.ny, C.nx, C.ny, V.pw, J, StRes<T>{V});
-            if (!grid_sync(a.sync, a.trace)) return false;
-            continue;
-        }
         if (l > 0) {
             FOR_ROWS(i, V.n) V.r[i] = __ldcg(V.b + i) - st_row9(V.nx, V.ny, V.c9, i, scaled(acc(V.b), V.wd));
             if (!grid_sync(a.sync, a.trace)) return false;
@@ -586,7 +579,7 @@ __device__ __forceinline__ bool vcycle_rest_st(const Op &A, const FArgs<T> &a, c
         const FLevel<T> &V = a.lev[l];
         const FLevel<T> &Cn = a.lev[l + 1];
         const T *bb = l == 0 ? b0 : V.b;
-        if (kFuse) {
+        if (V.fz) {
             const StUp<T> up{V, Cn.nx, Cn.ny, bb, xc};
             T v0 = 0;
             double vw = 0;
@@ -720,6 +713,14 @@ __device__ __forceinline__ bool vcycle_rest(const Op &A, const FArgs<T> &a, cons
         xc = out;
     }
     return true;
+}
+
+// The cycle's first phase for a stored input b: r_0 = b - A (w D^-1 b), then the barrier
+template <class Op, class T>
+__device__ __forceinline__ bool first_sweep(const Op &A, const FArgs<T> &a, const T *b)
+{
+    FOR_ROWS(i, a.lev[0].n) vcycle_residual0_row(A, a.lev[0], i, acc(b), __ldcg(b + i));
+    return grid_sync(a.sync, a.trace);
 }
 
 // z = V(b) for a stored input; with dot also rz = b . z and beta = rz / rho_prev.
@@ -1019,11 +1020,11 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                     T pi;
                     if (first) {
                         pi = __ldcg(p + i);
-                        vcycle_residual0_row(A, a.lev[0], i, acc((const T *)p), pi);
+                        if (!a.split0) vcycle_residual0_row(A, a.lev[0], i, acc((const T *)p), pi);
                     } else {
                         pi = dir(i);
                         pn[i] = pi;
-                        vcycle_residual0_row(A, a.lev[0], i, dir, pi);
+                        if (!a.split0) vcycle_residual0_row(A, a.lev[0], i, dir, pi);
                     }
                     ve[0] += pi;
                 }
@@ -1042,6 +1043,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                     p = pn;
                     pn = tmp;
                 }
+                if (a.split0 && !first_sweep(A, a, (const T *)p)) return false;
                 if (defl) {
                     double wy = 0;
                     if (!vcycle_rest(A, a, (const T *)p, a.ym, false, 1.0, dummy, dummy2, parity, a.wdef, &wy))
@@ -1134,7 +1136,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                     a.s[i] = si;
                     v2[0] += si * si;
                     v2[1] += si;
-                    vcycle_residual0_row(A, a.lev[0], i, snew, si);
+                    if (!a.split0) vcycle_residual0_row(A, a.lev[0], i, snew, si);
                 }
             } else {
                 FOR_ROWS(i, a.n)
@@ -1158,6 +1160,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                 status = KS_CONVERGED;
                 break;
             }
+            if (sa_multi && !MX && a.split0 && !first_sweep(A, a, (const T *)a.s)) return false;
             if (MX) {
                 if (!vcycle_mixed(*A32, *f, f->bin, a.ym, a.wdef, a.Edef, o2[1], cmx, parity)) return false;
             } else if (defl) {
@@ -1580,6 +1583,12 @@ static void launch_fused_mixed(Context &c, LinearSystem &S, Op64 A, Op32 A32, co
     CUIBM_TRY(cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(S.fused_fn), A, A32, args, fargs, b, x));
 }
 
+// From this many unknowns on, the FP64 BiCGSTAB cycles' first sweep is a phase of its
+// own (FArgs::split0; CUIBM_SPLIT0=0 keeps it folded)
+constexpr int kSplitMin = 200000;
+// FP64 structured levels below level 0 up to this size fold prolongation and sweep (FLevel::fz)
+constexpr int kFuseMax64 = 40000;
+
 // Upload the solver's arguments (after the SA hierarchy exists).
 static void upload_fargs(Context &c, LinearSystem &S)
 {
@@ -1627,8 +1636,10 @@ static void upload_fargs(Context &c, LinearSystem &S)
         F.ny = L->ny;
         F.c9 = L->c9;
         F.pw = L->pw;
+        F.fz = l > 0 && L->n <= kFuseMax64;
     }
     a.st = S.sa_structured;
+    a.split0 = S.n >= kSplitMin && !(getenv("CUIBM_SPLIT0") && getenv("CUIBM_SPLIT0")[0] == '0');
     a.ym = S.ym;
     a.wdef = S.wdef;
     a.Edef = S.Edef;
@@ -1710,6 +1721,7 @@ static void setup_mixed(Context &c, LinearSystem &S)
         F.ny = L->ny;
         F.c9 = L->c9 ? to_float(c, L->c9, 9 * (size_t)L->n) : nullptr;
         F.pw = L->pw ? to_float(c, L->pw, 4 * (size_t)L->n) : nullptr;
+        F.fz = 1;
     }
     f.st = S.sa_structured;
     m->dev = c.carve<FArgs<float>>(1);

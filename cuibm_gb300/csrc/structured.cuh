@@ -62,6 +62,23 @@ __device__ __forceinline__ T st_restrict(int nx, int ny, int cnx, int cny, const
 {
     const int n = nx * ny;
     const int Jy = J / cnx, Jx = J - Jy * cnx;
+    if (Jx >= 1 && Jx <= cnx - 2 && Jy >= 1 && Jy <= cny - 2) {
+        // an interior aggregate (3 x 3, with 3-wide aggregates or the last one around):
+        // its 5 x 5 region, the ring's weights on the side slots, every load independent
+        const int base = (3 * Jy - 1) * nx + 3 * Jx - 1;
+        T s = 0;
+#pragma unroll
+        for (int dy = 0; dy < 5; ++dy) {
+            const int ky = dy == 0 || dy == 4 ? 2 : 0;
+#pragma unroll
+            for (int dx = 0; dx < 5; ++dx) {
+                const int kx = dx == 0 || dx == 4 ? 1 : 0;
+                const int i = base + dy * nx + dx;
+                s += pw[(kx + ky) * n + i] * r(i);
+            }
+        }
+        return s;
+    }
     const int x0 = 3 * Jx, x1 = Jx == cnx - 1 ? nx - 1 : 3 * Jx + 2;
     const int y0 = 3 * Jy, y1 = Jy == cny - 1 ? ny - 1 : 3 * Jy + 2;
     const int xa = x0 > 0 ? x0 - 1 : 0, xb = x1 < nx - 1 ? x1 + 1 : nx - 1;

@@ -48,6 +48,8 @@ def main(argv=None):
     ap.add_argument("--warm", type=int, default=20)
     ap.add_argument("--system", choices=["velocity", "poisson", "both"], default="both")
     ap.add_argument("--flags", default="", help="the solver's command-line flags, e.g. \"-saStructured 0\"")
+    ap.add_argument("--sequence", type=int, default=0, metavar="N",
+                    help="also list the solve's phases N to 2N in order (one iteration's worth)")
     a = ap.parse_args(argv)
     src = open(SRC).read().split("\n") if os.path.exists(SRC) else []
     with cb.NavierStokesSolver(a.case, a.flags.split()) as s:
@@ -73,6 +75,10 @@ def main(argv=None):
                 text = src[line - 1].strip()[:60] if 0 < line <= len(src) else ""
                 print("  line %5d  n %4d  total %9.1f us  mean %7.2f us  %5.1f %%  %s" % (
                     line, n, us, us / n, 100 * us / max(total, 1e-9), text))
+            if a.sequence:
+                print("  phases %d-%d in order:" % (a.sequence, 2 * a.sequence - 1))
+                for k, (line, us) in enumerate(ph[a.sequence:2 * a.sequence]):
+                    print("    %4d  line %5d  %7.2f us" % (a.sequence + k, line, us))
 
 
 if __name__ == "__main__":

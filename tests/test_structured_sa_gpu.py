@@ -2,11 +2,12 @@
 Jacobi tables, power iteration, prolongator weights, Galerkin operators by probing)
 against tests/structured_sa_ref.py, the same construction in scipy: one V-cycle of
 the Poisson preconditioner (CUIBM_OP_PRECONDITION_POISSON, stepwise kernels) on the
-Re 40 cylinder's pressure operator (270 x 270, external method) and on the Re 550
-cylinder's (922 x 922, four levels), from the GPU's own matrix.  Whole runs with the
-structured hierarchy (the default, in the persistent solver) are checked against the
-FP64 oracle by the configuration tests; here a tightly solved run with it and one
-with the graph aggregation (-saStructured 0) give the same fields."""
+Re 40 cylinder's pressure operator (270 x 270, external method; -saStructured 1, as
+the default takes it from 200k unknowns) and on the Re 550 cylinder's (922 x 922, four
+levels, the default), from the GPU's own matrix.  Whole runs with the structured
+hierarchy (in the persistent solver) are checked against the FP64 oracle by the Re 550
+configuration tests; here a tightly solved run with it and one with the graph
+aggregation (-saStructured 0) give the same fields."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -30,7 +31,7 @@ def cylinder(folder, fine, **kw):
 @pytest.mark.parametrize("fine,levels", [(False, [72900, 8100, 900]), (True, [850084, 94249, 10404, 1156])])
 def test_vcycle_matches_scipy_statement(tmp_path, fine, levels):
     f = cylinder(str(tmp_path / "c"), fine, pois_pc="SMOOTHED_AGGREGATION")
-    with cb.NavierStokesSolver(f) as s:
+    with cb.NavierStokesSolver(f, [] if fine else ["-saStructured", "1"]) as s:
         s.set_option("write_output", 0)
         s.initialise()
         i = s.info
