@@ -96,6 +96,7 @@ struct FLevel {
     int nx, ny;
     const T *c9, *pw;
     int fz;  // structured: prolongation and smoothing sweep in one phase
+    int rg;  // structured: the restriction into this level's coarser one, 8 lanes a coarse node
 };
 
 // Everything a solve needs except its right-hand side and solution, built once
@@ -127,6 +128,7 @@ struct FArgs {
     // correction (wdef = A^T e, Edef = e^T A e; wdef null: no correction)
     double *ym;
     const double *wdef;
+    const double *aedef;  // A e: A (y + c e) = A y + c A e, without adding c at every stencil point
     double Edef;
 };
 
@@ -316,6 +318,34 @@ __device__ __forceinline__ T csr_row_g(const CsrV<T> &M, int i, const X &x)
 }
 
 #define FOR_ROWS(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+// The rows of a grid-stride loop U at a time: ld(i) gathers and computes row i's values
+// without storing (so the U rows' loads are in flight together - a store between them
+// would keep the next row's loads behind it, the compiler not knowing that the arrays do
+// not overlap), st(i, v) stores and accumulates.  Rows are taken in the order FOR_ROWS
+// takes them, so per-thread sums are the same.
+template <int U = 2, class Ld, class St>
+__device__ __forceinline__ void rows2(int n, const Ld &ld, const St &st)
+{
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < n; i += U * stride) {
+        decltype(ld(i)) u[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) u[k] = ld(i + k * stride);
+#pragma unroll
+        for (int k = 0; k < U; ++k) st(i + k * stride, u[k]);
+    }
+    for (; i < n; i += stride) st(i, ld(i));
+}
+template <class T>
+struct V2 {
+    T a, b;
+};
+template <class T>
+struct V3 {
+    T a, b, c;
+};
 #define FOR_GROUP_ROWS(G, i, n) \
     for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); i < (n); i += (int)((gridDim.x * blockDim.x) / G))
 
@@ -533,28 +563,71 @@ __device__ __forceinline__ bool cycle_end(const FArgs<T> &a, T v0, double vw, bo
     return true;
 }
 
-// x_l = w D^-1 b_l + P x_l+1 at node k of level l, from the coarse values xc
+// The folded up-sweep works on tiles of kTW x kTH fine nodes with a halo of one node:
+// x_l = w D^-1 b_l + P x_l+1 on the tile and its halo goes to shared memory, then
+// out_l = x_l + w D^-1 (b_l - A_l x_l) reads its stencil values from there.
+constexpr int kTW = 32, kTH = 16, kTP = kTW + 2;
+
+// a tile's x_l as the stencil of node i (tile slot li) sees it: neighbours j = i + dy nx
+// + dx with |dx|, |dy| <= 1 (nx >= 3 on every level with a coarser one)
 template <class T>
-struct StUp {
-    const FLevel<T> &V;
-    int cnx, cny;
-    const T *b, *xc;
-    __device__ __forceinline__ T operator()(int k) const
+struct TileAcc {
+    const T *xs;
+    int li, i, nx;
+    __device__ __forceinline__ T operator()(int j) const
     {
-        return V.wd[k] * __ldcg(b + k) + st_prolong(V.nx, V.ny, cnx, cny, V.pw, k, acc(xc));
+        const int d = j - i;
+        const int dy = d >= nx - 1 ? 1 : (d <= 1 - nx ? -1 : 0);
+        return xs[li + dy * kTP + (d - dy * nx)];
     }
 };
+
+// The level's up-sweep in one phase (no barrier inside; the caller ends the phase):
+// row(i, x_i, acc) applies A_l, out(i, o) takes out_l at node i
+template <class T, class RowFn, class OutFn>
+__device__ __forceinline__ void st_up_tiles(const FLevel<T> &V, int cnx, int cny, const T *bb, const T *xc,
+                                            const RowFn &row, const OutFn &out)
+{
+    __shared__ T xs[(kTH + 2) * kTP];
+    const int nx = V.nx, ny = V.ny;
+    const int tx = (nx + kTW - 1) / kTW, ty = (ny + kTH - 1) / kTH;
+    for (int t = blockIdx.x; t < tx * ty; t += gridDim.x) {
+        const int x0 = (t % tx) * kTW, y0 = (t / tx) * kTH;
+        for (int k = threadIdx.x; k < (kTH + 2) * kTP; k += blockDim.x) {
+            const int hy = k / kTP, hx = k - hy * kTP;
+            const int ix = x0 - 1 + hx, iy = y0 - 1 + hy;
+            T v = 0;
+            if (ix >= 0 && ix < nx && iy >= 0 && iy < ny) {
+                const int i = iy * nx + ix;
+                v = V.wd[i] * __ldcg(bb + i) + st_prolong_xy(nx, ny, cnx, cny, V.pw, ix, iy, acc(xc));
+            }
+            xs[k] = v;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < kTH * kTW; k += blockDim.x) {
+            const int ly = k / kTW, lx = k - ly * kTW;
+            const int ix = x0 + lx, iy = y0 + ly;
+            if (ix < nx && iy < ny) {
+                const int i = iy * nx + ix, li = (ly + 1) * kTP + lx + 1;
+                const T xi = xs[li];
+                out(i, xi + V.wd[i] * (__ldcg(bb + i) - row(i, xi, TileAcc<T>{xs, li, i, nx})));
+            }
+        }
+        __syncthreads();
+    }
+}
 
 // The structured hierarchy's cycle after its first phase: the same cycle as below
 // (one damped-Jacobi sweep from zero down, one up, R = P^T), with the prolongator as
 // four weights a node and 9-point coarse operators, so that no phase loads a column
 // index.  Down, r_l then its restriction (a coarse node's sum over the 5 x 5 nodes
 // around its aggregate: recomputing r_l there, 9 points each, would leave a few
-// thousand threads with hundreds of loads apiece).  Up, x_l = w D^-1 b_l + P x_l+1 is
-// stored (one phase), then out_l = x_l + w D^-1 (b_l - A_l x_l) (the next); on a level
-// with fz set the two are one phase, x_l recomputed at the sweep's stencil points: a
-// few dozen operations a node, which FP32 (the mixed solver's cycle, every level)
-// affords, and FP64 - issued at 1/64 of the FP32 rate - on the small levels only.
+// thousand threads with hundreds of loads apiece).  Up, on the levels below 0 (fz set),
+// one phase over shared-memory tiles (st_up_tiles: x_l computed once a node, a halo row
+// and column twice); on level 0, x_l = w D^-1 b_l + P x_l+1 stored (one phase), then
+// out_l (the next) - there the tiles' two dependent stages per tile, one tile after
+// another in each block, cost more than the barrier they save (52 against 33 us at
+// 850k unknowns in FP64, 33 against about 20 in FP32).
 template <class Op, class T, class TO>
 __device__ __forceinline__ bool vcycle_rest_st(const Op &A, const FArgs<T> &a, const T *b0, TO *zout, bool dot,
                                                double rho_prev, double &rz, double &beta, int &parity,
@@ -568,7 +641,19 @@ __device__ __forceinline__ bool vcycle_rest_st(const Op &A, const FArgs<T> &a, c
             FOR_ROWS(i, V.n) V.r[i] = __ldcg(V.b + i) - st_row9(V.nx, V.ny, V.c9, i, scaled(acc(V.b), V.wd));
             if (!grid_sync(a.sync, a.trace)) return false;
         }
-        FOR_ROWS(J, C.n) C.b[J] = st_restrict(V.nx, V.ny, C.nx, C.ny, V.pw, J, acc(V.r));
+        if (V.rg) {
+            // a small coarse level: a coarse node's region rows over 8 lanes (rows 0-6), so
+            // that a few thousand nodes do not leave each thread a long chain of loads
+            FOR_GROUP_ROWS(8, J, C.n)
+            {
+                T v = st_restrict_row(V.nx, V.ny, C.nx, C.ny, V.pw, J, acc(V.r), threadIdx.x & 7);
+#pragma unroll
+                for (int o = 4; o > 0; o >>= 1) v += __shfl_xor_sync(group_mask<8>(), v, o);
+                if ((threadIdx.x & 7) == 0) C.b[J] = v;
+            }
+        } else {
+            FOR_ROWS(J, C.n) C.b[J] = st_restrict(V.nx, V.ny, C.nx, C.ny, V.pw, J, acc(V.r));
+        }
         if (!grid_sync(a.sync, a.trace)) return false;
     }
     const FLevel<T> &C = a.lev[L - 1];
@@ -580,44 +665,48 @@ __device__ __forceinline__ bool vcycle_rest_st(const Op &A, const FArgs<T> &a, c
         const FLevel<T> &Cn = a.lev[l + 1];
         const T *bb = l == 0 ? b0 : V.b;
         if (V.fz) {
-            const StUp<T> up{V, Cn.nx, Cn.ny, bb, xc};
             T v0 = 0;
             double vw = 0;
             if (l == 0) {
-                FOR_ROWS(i, V.n)
-                {
-                    const T xi = up(i);
-                    const T o = xi + V.wd[i] * (__ldcg(bb + i) - A.row_x(i, xi, up));
-                    zout[i] = (TO)o;
-                    if (dot) v0 += __ldcg(b0 + i) * o;
-                    if (wdot) vw += wdot[i] * (double)o;
-                }
+                st_up_tiles(
+                    V, Cn.nx, Cn.ny, bb, xc,
+                    [&](int i, T xi, const TileAcc<T> &x) { return A.row_x(i, xi, x); },
+                    [&](int i, T o) {
+                        zout[i] = (TO)o;
+                        if (dot) v0 += __ldcg(b0 + i) * o;
+                        if (wdot) vw += wdot[i] * (double)o;
+                    });
                 if (!cycle_end(a, v0, vw, dot, wdot, rho_prev, rz, beta, parity, wz)) return false;
             } else {
-                FOR_ROWS(i, V.n)
-                {
-                    const T xi = up(i);
-                    V.t[i] = xi + V.wd[i] * (__ldcg(bb + i) - st_row9(V.nx, V.ny, V.c9, i, up));
-                }
+                st_up_tiles(
+                    V, Cn.nx, Cn.ny, bb, xc,
+                    [&](int i, T, const TileAcc<T> &x) { return st_row9(V.nx, V.ny, V.c9, i, x); },
+                    [&](int i, T o) { V.t[i] = o; });
                 if (!grid_sync(a.sync, a.trace)) return false;
             }
             xc = V.t;
             continue;
         }
-        FOR_ROWS(i, V.n)
-        V.x[i] = V.wd[i] * __ldcg(bb + i) + st_prolong(V.nx, V.ny, Cn.nx, Cn.ny, V.pw, i, acc(xc));
+        rows2<4>(
+            V.n,
+            [&](int i) { return V.wd[i] * __ldcg(bb + i) + st_prolong(V.nx, V.ny, Cn.nx, Cn.ny, V.pw, i, acc(xc)); },
+            [&](int i, T xi) { V.x[i] = xi; });
         if (!grid_sync(a.sync, a.trace)) return false;
         if (l == 0) {
             T v0 = 0;
             double vw = 0;
-            FOR_ROWS(i, V.n)
-            {
-                const T xi = __ldcg(V.x + i);
-                const T o = xi + V.wd[i] * (__ldcg(bb + i) - A.row_x(i, xi, acc((const T *)V.x)));
-                zout[i] = (TO)o;
-                if (dot) v0 += __ldcg(b0 + i) * o;
-                if (wdot) vw += wdot[i] * (double)o;
-            }
+            rows2(
+                V.n,
+                [&](int i) {
+                    const T xi = __ldcg(V.x + i);
+                    const T o = xi + V.wd[i] * (__ldcg(bb + i) - A.row_x(i, xi, acc((const T *)V.x)));
+                    return V3<double>{(double)o, dot ? (double)__ldcg(b0 + i) : 0.0, wdot ? wdot[i] : 0.0};
+                },
+                [&](int i, const V3<double> &u) {
+                    zout[i] = (TO)u.a;
+                    if (dot) v0 += (T)u.b * (T)u.a;
+                    if (wdot) vw += u.c * u.a;
+                });
             if (!cycle_end(a, v0, vw, dot, wdot, rho_prev, rz, beta, parity, wz)) return false;
         } else {
             FOR_ROWS(i, V.n)
@@ -715,11 +804,28 @@ __device__ __forceinline__ bool vcycle_rest(const Op &A, const FArgs<T> &a, cons
     return true;
 }
 
+// (A (y + c e))_i for the cycle's output y and its constant-mode shift c: A y + c A e
+// where A e is stored (five FP64 additions a row fewer), else with c added at every
+// stencil point
+template <class Op, class T>
+__device__ __forceinline__ T shifted_row(const Op &A, const FArgs<T> &a, int i, double yi, double c)
+{
+    if (a.aedef) return A.row_x(i, (T)yi, acc((const T *)a.ym)) + (T)(c * a.aedef[i]);
+    return A.row_x(i, (T)(yi + c), LdShift{a.ym, c});
+}
+
 // The cycle's first phase for a stored input b: r_0 = b - A (w D^-1 b), then the barrier
 template <class Op, class T>
 __device__ __forceinline__ bool first_sweep(const Op &A, const FArgs<T> &a, const T *b)
 {
-    FOR_ROWS(i, a.lev[0].n) vcycle_residual0_row(A, a.lev[0], i, acc(b), __ldcg(b + i));
+    const FLevel<T> &V = a.lev[0];
+    rows2<4>(
+        V.n,
+        [&](int i) {
+            const T bi = __ldcg(b + i);
+            return bi - A.row_x(i, V.wd[i] * bi, scaled(acc(b), V.wd));
+        },
+        [&](int i, T r) { V.r[i] = r; });
     return grid_sync(a.sync, a.trace);
 }
 
@@ -759,8 +865,7 @@ template <class Op32>
 __device__ __forceinline__ bool vcycle_mixed(const Op32 &A32, const FArgs<float> &f, const float *b32, double *y,
                                              const double *wdef, double Edef, double eb, double &c, int &parity)
 {
-    FOR_ROWS(i, f.lev[0].n) vcycle_residual0_row(A32, f.lev[0], i, acc(b32), __ldcg(b32 + i));
-    if (!grid_sync(f.sync, f.trace)) return false;
+    if (!first_sweep(A32, f, b32)) return false;
     double d0 = 0, d1 = 0, wy = 0;
     if (!vcycle_rest(A32, f, b32, y, false, 1.0, d0, d1, parity, wdef, &wy)) return false;
     c = wdef ? (eb - wy) / Edef : 0.0;
@@ -990,18 +1095,13 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
         if (PC == 2) {
             if (MX) {
                 T ve[1] = {0};
-                FOR_ROWS(i, a.n)
-                {
-                    T pi;
-                    if (first) {
-                        pi = __ldcg(p + i);
-                    } else {
-                        pi = dir(i);
-                        pn[i] = pi;
-                    }
-                    f->bin[i] = (float)pi;
-                    ve[0] += pi;
-                }
+                rows2(
+                    a.n, [&](int i) { return first ? __ldcg(p + i) : dir(i); },
+                    [&](int i, T pi) {
+                        if (!first) pn[i] = pi;
+                        f->bin[i] = (float)pi;
+                        ve[0] += pi;
+                    });
                 double ved[1], eb[1];
                 to_double(ve, ved);
                 if (!grid_reduce<1, 1>(ved, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = t[0]; },
@@ -1079,20 +1179,25 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
             }
             if (!grid_sync(a.sync, a.trace)) return false;
         }
-        FOR_ROWS(i, a.n)
-        {
-            T ai;
-            if (PC != 2) {
-                ai = A.row(i, acc((const T *)a.Mp));
-            } else if (PC == 2 && (MX || defl)) {
-                const double mi = __ldcg(a.ym + i) + cmx;
-                a.Mp[i] = (T)mi;
-                ai = A.row_x(i, (T)mi, LdShift{a.ym, cmx});
-            } else {
-                ai = A.row(i, acc((const T *)a.Mp));
-            }
-            ampn[i] = ai;
-            v1[0] += __ldcg(a.rs + i) * ai;
+        if (PC == 2 && (MX || defl)) {
+            rows2(
+                a.n,
+                [&](int i) {
+                    const double yi = __ldcg(a.ym + i);
+                    return V3<T>{(T)(yi + cmx), shifted_row(A, a, i, yi, cmx), __ldcg(a.rs + i)};
+                },
+                [&](int i, const V3<T> &u) {
+                    a.Mp[i] = u.a;
+                    ampn[i] = u.b;
+                    v1[0] += u.c * u.b;
+                });
+        } else {
+            rows2(
+                a.n, [&](int i) { return V2<T>{A.row(i, acc((const T *)a.Mp)), __ldcg(a.rs + i)}; },
+                [&](int i, const V2<T> &u) {
+                    ampn[i] = u.a;
+                    v1[0] += u.b * u.a;
+                });
         }
         to_double(v1, v1d);
         if (!grid_reduce<1, 1>(v1d, a, parity, [&](const double (&t)[1], double (&q)[1]) { q[0] = rho / t[0]; }, o1))
@@ -1121,14 +1226,14 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
             T v2[2] = {0, 0};
             double v2d[2], o2[2];
             if (MX) {
-                FOR_ROWS(i, a.n)
-                {
-                    const T si = snew(i);
-                    a.s[i] = si;
-                    v2[0] += si * si;
-                    v2[1] += si;
-                    f->bin[i] = (float)si;
-                }
+                rows2(
+                    a.n, [&](int i) { return snew(i); },
+                    [&](int i, T si) {
+                        a.s[i] = si;
+                        v2[0] += si * si;
+                        v2[1] += si;
+                        f->bin[i] = (float)si;
+                    });
             } else if (sa_multi) {
                 FOR_ROWS(i, a.n)
                 {
@@ -1175,20 +1280,27 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
             }
             T v3[2] = {0, 0};
             double v3d[2], o4[1];
-            FOR_ROWS(i, a.n)
-            {
-                T ai;
-                if (MX || defl) {
-                    const double mi = __ldcg(a.ym + i) + cmx;
-                    a.Ms[i] = (T)mi;
-                    ai = A.row_x(i, (T)mi, LdShift{a.ym, cmx});
-                } else {
-                    ai = A.row(i, acc((const T *)a.Ms));
-                }
-                a.AMs[i] = ai;
-                const T si = __ldcg(a.s + i);
-                v3[0] += ai * si;
-                v3[1] += ai * ai;
+            if (MX || defl) {
+                rows2(
+                    a.n,
+                    [&](int i) {
+                        const double yi = __ldcg(a.ym + i);
+                        return V3<T>{(T)(yi + cmx), shifted_row(A, a, i, yi, cmx), __ldcg(a.s + i)};
+                    },
+                    [&](int i, const V3<T> &u) {
+                        a.Ms[i] = u.a;
+                        a.AMs[i] = u.b;
+                        v3[0] += u.b * u.c;
+                        v3[1] += u.b * u.b;
+                    });
+            } else {
+                rows2(
+                    a.n, [&](int i) { return V2<T>{A.row(i, acc((const T *)a.Ms)), __ldcg(a.s + i)}; },
+                    [&](int i, const V2<T> &u) {
+                        a.AMs[i] = u.a;
+                        v3[0] += u.a * u.b;
+                        v3[1] += u.a * u.a;
+                    });
             }
             to_double(v3, v3d);
             if (!grid_reduce<2, 1>(v3d, a, parity, [&](const double (&t)[2], double (&q)[1]) { q[0] = t[0] / t[1]; },
@@ -1239,14 +1351,18 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
         // ---- x, r and the dots that give beta
         T v4[2] = {0, 0};
         double v4d[2], o5[4];
-        FOR_ROWS(i, a.n)
-        {
-            x[i] = __ldcg(x + i) + (at * __ldcg(a.Mp + i) + ot * __ldcg(a.Ms + i));
-            const T ri = __ldcg(a.s + i) - ot * __ldcg(a.AMs + i);
-            a.r[i] = ri;
-            v4[0] += __ldcg(a.rs + i) * ri;
-            v4[1] += ri * ri;
-        }
+        rows2<4>(
+            a.n,
+            [&](int i) {
+                return V3<T>{__ldcg(x + i) + (at * __ldcg(a.Mp + i) + ot * __ldcg(a.Ms + i)),
+                             __ldcg(a.s + i) - ot * __ldcg(a.AMs + i), __ldcg(a.rs + i)};
+            },
+            [&](int i, const V3<T> &u) {
+                x[i] = u.a;
+                a.r[i] = u.b;
+                v4[0] += u.c * u.b;
+                v4[1] += u.b * u.b;
+            });
         to_double(v4, v4d);
         if (!grid_reduce<2, 4>(v4d, a, parity, [&](const double (&t)[2], double (&q)[4]) {
                 q[0] = (t[0] / rho) * (alpha / omega);
@@ -1583,11 +1699,12 @@ static void launch_fused_mixed(Context &c, LinearSystem &S, Op64 A, Op32 A32, co
     CUIBM_TRY(cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(S.fused_fn), A, A32, args, fargs, b, x));
 }
 
+// Structured restrictions into coarse levels up to this size take 8 lanes a coarse node
+constexpr int kRestrictGroupMax = 20000;
+
 // From this many unknowns on, the FP64 BiCGSTAB cycles' first sweep is a phase of its
 // own (FArgs::split0; CUIBM_SPLIT0=0 keeps it folded)
 constexpr int kSplitMin = 200000;
-// FP64 structured levels below level 0 up to this size fold prolongation and sweep (FLevel::fz)
-constexpr int kFuseMax64 = 40000;
 
 // Upload the solver's arguments (after the SA hierarchy exists).
 static void upload_fargs(Context &c, LinearSystem &S)
@@ -1636,12 +1753,14 @@ static void upload_fargs(Context &c, LinearSystem &S)
         F.ny = L->ny;
         F.c9 = L->c9;
         F.pw = L->pw;
-        F.fz = l > 0 && L->n <= kFuseMax64;
+        F.fz = l > 0 && L->nx > 0;
+        F.rg = L->nx > 0 && l + 1 < a.nlev && S.amg[l + 1]->n <= kRestrictGroupMax;
     }
     a.st = S.sa_structured;
     a.split0 = S.n >= kSplitMin && !(getenv("CUIBM_SPLIT0") && getenv("CUIBM_SPLIT0")[0] == '0');
     a.ym = S.ym;
     a.wdef = S.wdef;
+    a.aedef = S.aedef;
     a.Edef = S.Edef;
     MixedState *m = static_cast<MixedState *>(S.mixed);
     FArgs<double> *d = S.fargs ? static_cast<FArgs<double> *>(S.fargs) : c.carve<FArgs<double>>(1);
@@ -1721,7 +1840,8 @@ static void setup_mixed(Context &c, LinearSystem &S)
         F.ny = L->ny;
         F.c9 = L->c9 ? to_float(c, L->c9, 9 * (size_t)L->n) : nullptr;
         F.pw = L->pw ? to_float(c, L->pw, 4 * (size_t)L->n) : nullptr;
-        F.fz = 1;
+        F.fz = l > 0;
+        F.rg = L->nx > 0 && l + 1 < f.nlev && S.amg[l + 1]->n <= kRestrictGroupMax;
     }
     f.st = S.sa_structured;
     m->dev = c.carve<FArgs<float>>(1);
@@ -1754,15 +1874,19 @@ static void setup_deflation(Context &c, LinearSystem &S)
     if (e && (e[0] == '0' || e[0] == '1')) on = e[0] == '1';
     if (!mixed && !on) return;
     std::vector<int> ptr, col;
-    std::vector<double> val, w(S.n, 0.0);
+    std::vector<double> val, w(S.n, 0.0), ae(S.n, 0.0);
     host_operator_csr(c, 2, nullptr, ptr, col, val);
     for (size_t k = 0; k < col.size(); ++k) w[col[k]] += val[k];
+    for (int i = 0; i < S.n; ++i)
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k) ae[i] += val[k];
     double E = 0;
     for (double v : w) E += v;
     if (!(E != 0)) return;  // no pinned cell: the operator is singular, leave the cycle alone
     S.wdef = c.carve<double>(S.n);
+    S.aedef = c.carve<double>(S.n);
     S.Edef = E;
     CUIBM_TRY(cudaMemcpyAsync(S.wdef, w.data(), S.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CUIBM_TRY(cudaMemcpyAsync(S.aedef, ae.data(), S.n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
 }
 

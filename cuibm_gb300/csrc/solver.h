@@ -158,6 +158,7 @@ struct LinearSystem {
     std::vector<void *> sa_blocks;
     unsigned long long sa_key = 0;
     void *mixed = nullptr;  // mixed precision: the float tables (fused_solve.cu)
+    double *aedef = nullptr;                // A e (the operator's row sums), with wdef
     double *ym = nullptr, *wdef = nullptr;  // constant-mode correction of the SA cycle (Poisson):
     double Edef = 0;                        // cycle output, A^T e, e^T A e
     FusedSyncState *fsync = nullptr;

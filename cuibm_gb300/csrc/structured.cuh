@@ -38,6 +38,21 @@ __host__ __device__ __forceinline__ StAxis st_axis(int x, int n, int cn)
 
 __host__ __device__ __forceinline__ int st_coarse(int n) { return n / 3 > 1 ? n / 3 : 1; }
 
+// (P xc)_i for the fine node (ix, iy), i = iy nx + ix
+template <class T, class X>
+__device__ __forceinline__ T st_prolong_xy(int nx, int ny, int cnx, int cny, const T *__restrict__ pw, int ix,
+                                           int iy, const X &xc)
+{
+    const int n = nx * ny, i = iy * nx + ix;
+    const StAxis ax = st_axis(ix, nx, cnx), ay = st_axis(iy, ny, cny);
+    const int J = ay.a * cnx + ax.a;
+    T y = pw[i] * xc(J);
+    if (ax.s) y += pw[n + i] * xc(J + ax.s);
+    if (ay.s) y += pw[2 * n + i] * xc(J + ay.s * cnx);
+    if (ax.s && ay.s) y += pw[3 * n + i] * xc(J + ax.s + ay.s * cnx);
+    return y;
+}
+
 // (P xc)_i: the four weights of fine node i against the coarse values around it
 template <class T, class X>
 __device__ __forceinline__ T st_prolong(int nx, int ny, int cnx, int cny, const T *__restrict__ pw, int i,
@@ -54,19 +69,62 @@ __device__ __forceinline__ T st_prolong(int nx, int ny, int cnx, int cny, const 
     return y;
 }
 
-// (P^T r)_J: the fine nodes of aggregate J and the ring around it, each with the
-// weight of its row of P that refers to J
+// One row of (P^T r)_J: row dy (0..6) of the region of aggregate J - its fine nodes and
+// the ring around them - each node weighted by its row of P's weight that refers to J.
+// An interior aggregate (3 x 3, with 3-wide aggregates or the last one around it) has a
+// 5 x 5 region whose slots are fixed (the ring on the side slots); an aggregate on the
+// grid's edge (up to 5 wide) has up to 7 x 7, its slots worked out first and then all
+// the loads issued on a clamped index, weighted 0 or 1, so that no load waits for the
+// one before it.
+template <class T, class X>
+__device__ __forceinline__ T st_restrict_row(int nx, int ny, int cnx, int cny, const T *__restrict__ pw, int J,
+                                             const X &r, int dy)
+{
+    const int n = nx * ny;
+    const int Jy = J / cnx, Jx = J - Jy * cnx;
+    const int x0 = 3 * Jx, iy = 3 * Jy - 1 + dy;
+    T s = 0;
+    if (Jx >= 1 && Jx <= cnx - 2 && Jy >= 1 && Jy <= cny - 2) {
+        if (dy >= 5) return s;
+        const int base = iy * nx + x0 - 1, ky = dy == 0 || dy == 4 ? 2 : 0;
+#pragma unroll
+        for (int dx = 0; dx < 5; ++dx) {
+            const int kx = dx == 0 || dx == 4 ? 1 : 0;
+            s += pw[(kx + ky) * n + base + dx] * r(base + dx);
+        }
+        return s;
+    }
+    if (dy >= 7 || iy < 0 || iy >= ny) return s;
+    const StAxis ay = st_axis(iy, ny, cny);
+    const int ky = ay.a == Jy ? 0 : (ay.s && ay.a + ay.s == Jy ? 2 : -1);
+    if (ky < 0) return s;
+#pragma unroll
+    for (int dx = 0; dx < 7; ++dx) {
+        const int ix = x0 - 1 + dx;
+        int kx = -1;
+        if (ix >= 0 && ix < nx) {
+            const StAxis ax = st_axis(ix, nx, cnx);
+            kx = ax.a == Jx ? 0 : (ax.s && ax.a + ax.s == Jx ? 1 : -1);
+        }
+        const bool on = kx >= 0;
+        const int i = on ? iy * nx + ix : 0;
+        const T w = pw[(on ? kx + ky : 0) * n + i];
+        const T v = r(i);
+        if (on) s += w * v;
+    }
+    return s;
+}
+
+// (P^T r)_J: the interior 5 x 5 region in one unrolled sum, an edge aggregate row by row
 template <class T, class X>
 __device__ __forceinline__ T st_restrict(int nx, int ny, int cnx, int cny, const T *__restrict__ pw, int J,
                                          const X &r)
 {
     const int n = nx * ny;
     const int Jy = J / cnx, Jx = J - Jy * cnx;
+    T s = 0;
     if (Jx >= 1 && Jx <= cnx - 2 && Jy >= 1 && Jy <= cny - 2) {
-        // an interior aggregate (3 x 3, with 3-wide aggregates or the last one around):
-        // its 5 x 5 region, the ring's weights on the side slots, every load independent
         const int base = (3 * Jy - 1) * nx + 3 * Jx - 1;
-        T s = 0;
 #pragma unroll
         for (int dy = 0; dy < 5; ++dy) {
             const int ky = dy == 0 || dy == 4 ? 2 : 0;
@@ -79,24 +137,7 @@ __device__ __forceinline__ T st_restrict(int nx, int ny, int cnx, int cny, const
         }
         return s;
     }
-    const int x0 = 3 * Jx, x1 = Jx == cnx - 1 ? nx - 1 : 3 * Jx + 2;
-    const int y0 = 3 * Jy, y1 = Jy == cny - 1 ? ny - 1 : 3 * Jy + 2;
-    const int xa = x0 > 0 ? x0 - 1 : 0, xb = x1 < nx - 1 ? x1 + 1 : nx - 1;
-    const int ya = y0 > 0 ? y0 - 1 : 0, yb = y1 < ny - 1 ? y1 + 1 : ny - 1;
-    T s = 0;
-    for (int iy = ya; iy <= yb; ++iy) {
-        const StAxis ay = st_axis(iy, ny, cny);
-        // which of the row's aggregates along y is J's row: own (0) or the side (1)
-        const int ky = ay.a == Jy ? 0 : (ay.s && ay.a + ay.s == Jy ? 1 : -1);
-        if (ky < 0) continue;
-        for (int ix = xa; ix <= xb; ++ix) {
-            const StAxis ax = st_axis(ix, nx, cnx);
-            const int kx = ax.a == Jx ? 0 : (ax.s && ax.a + ax.s == Jx ? 1 : -1);
-            if (kx < 0) continue;
-            const int i = iy * nx + ix;
-            s += pw[(kx + 2 * ky) * n + i] * r(i);
-        }
-    }
+    for (int dy = 0; dy < 7; ++dy) s += st_restrict_row(nx, ny, cnx, cny, pw, J, r, dy);
     return s;
 }
 
