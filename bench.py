@@ -387,7 +387,9 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
     stream, the persistent solves' block count picked by the batch autotuner during
     warm-up), in plain FP64 and in mixed precision (the configuration's), and one
     instance after another in plain FP64 (each with the whole GPU), timed over the same
-    steps with wall-clock time around synchronised GPU work.  Aggregate Mcell-steps/s."""
+    steps with wall-clock time around synchronised GPU work.  Aggregate Mcell-steps/s.
+    solver_blocks is the autotuner's choice: a block count for every instance, or minus
+    the rows a thread of block counts sized per instance."""
     import time as _time
 
     import torch
@@ -403,7 +405,7 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
                 s.set_option("write_output", 0)
             b.initialise()
             b.stepTime(warm)
-            blocks = b.autotune(tune_steps)  # advances every instance by up to 10 x tune_steps
+            blocks = b.autotune(tune_steps)  # advances every instance by 18 x tune_steps
             warm_all = b.instances[0].timeStep
             cells = sum(s.info.numP for s in b.instances)
             torch.cuda.synchronize()

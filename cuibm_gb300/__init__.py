@@ -397,8 +397,9 @@ class Batch:
         self._check(self._L.cuibm_batch_step(self._h, int(nsteps)))
 
     def autotune(self, steps=2):
-        """Pick the persistent solves' block count by timing the batch (cuibm_batch_autotune;
-        every instance advances 10 x steps); returns the choice."""
+        """Pick the persistent solves' block counts by timing the batch (cuibm_batch_autotune;
+        every instance advances 18 x steps); returns the choice: one block count for all
+        instances, or minus the rows a thread of counts sized per instance."""
         nb = ctypes.c_int()
         self._check(self._L.cuibm_batch_autotune(self._h, int(steps), ctypes.byref(nb)))
         return nb.value

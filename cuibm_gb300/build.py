@@ -35,6 +35,10 @@ UNITS = {
     "krylov.cu": [],
     "amg.cu": [],
     "fused_solve.cu": [],
+    "fused_op1.cu": [],
+    "fused_op2.cu": [],
+    "fused_mixed_op1.cu": [],
+    "fused_mixed_op2.cu": [],
     "adjoint.cu": [],
     "fadlun.cu": ["-fmad=false"],
     "embedded.cu": ["-fmad=false"],

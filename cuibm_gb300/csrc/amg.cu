@@ -565,7 +565,9 @@ constexpr int kStructuredMin = 200000;
 static bool structured_applies(const Context &c, const LinearSystem &S)
 {
     const bool want = c.P.saStructured == 1 || (c.P.saStructured == -1 && S.n >= kStructuredMin);
-    return want && S.which == 2 && S.precond == PC_SMOOTHED_AGGREGATION && !S.sa_dynamic &&
+    // the persistent solves built for two blocks per SM (-solverPack 2, batches) leave the
+    // structured cycle out to keep their registers
+    return want && c.P.solverPack != 2 && S.which == 2 && S.precond == PC_SMOOTHED_AGGREGATION && !S.sa_dynamic &&
            (c.P.solverType == ST_NAVIERSTOKES || c.P.solverType == ST_LUO) && !c.l2.patch.pid &&
            S.n == c.g.nx * c.g.ny && S.n > kCoarse;
 }

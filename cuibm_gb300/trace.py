@@ -10,7 +10,7 @@ time without a profiler.
     python -m cuibm_gb300.trace CASE_FOLDER [--warm 20] [--system poisson] [--flags "-saStructured 0"]
 
 runs the case for --warm steps, traces the next step and prints, per barrier site
-of csrc/fused_solve.cu, the count, total and mean phase time.
+of csrc/fused_kernels.cuh, the count, total and mean phase time.
 """
 import argparse
 import collections
@@ -18,7 +18,7 @@ import os
 
 import numpy as np
 
-SRC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "fused_solve.cu")
+SRC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "fused_kernels.cuh")
 
 
 def phases(trace):

@@ -115,7 +115,7 @@ enum {
     CUIBM_F_SOLVE_TRACE,     /* uint64 2*4096: per-barrier timestamps (ns) of the last persistent
                                 velocity (first 4096) and Poisson solve: [count, start, ...], each
                                 entry the timer's low 48 bits with the barrier's source line of
-                                fused_solve.cu in the top 16; written only while the option
+                                fused_kernels.cuh in the top 16; written only while the option
                                 "trace_solve" is 1 */
     CUIBM_F_BODY_MOTION,     /* D 12: body centre x, y and centre velocity u, v; the same at the
                                 start of the step; the coupling tolerance and the sub-iterations
@@ -311,10 +311,13 @@ int cuibm_batch_create(int n, const char *const *case_folders, int argc, const c
 int cuibm_batch_initialise(cuibm_batch *b);
 int cuibm_batch_step(cuibm_batch *b, int nsteps);
 /* Autotuner of the batch's persistent-solve grid: times `steps` batch steps with each
- * candidate block count (a half, quarter, sixth, eighth and twelfth of the SMs),
- * in two passes of opposite order, and keeps the fastest for every instance
- * (option "solver_blocks").  The timed steps are steps of the simulation (each
- * instance advances at most 10 x steps).  *blocks_out (may be null) gets the choice. */
+ * candidate - one block count for every instance (a half, quarter, sixth, eighth and
+ * twelfth of the SMs) or a count per instance from its pressure unknowns at 4, 8, 16
+ * or 32 rows a thread (at least 2 blocks, at most half the SMs) - in two passes of
+ * opposite order, and keeps the fastest (option "solver_blocks" of every instance).
+ * The timed steps are steps of the simulation (each instance advances 18 x steps).
+ * *blocks_out (may be null) gets the choice: the block count, or minus the rows a
+ * thread of a per-instance choice. */
 int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out);
 int cuibm_batch_size(const cuibm_batch *b);
 cuibm_ctx *cuibm_batch_instance(cuibm_batch *b, int k);
