@@ -19,11 +19,62 @@
 #include <vector>
 
 #include "../../include/cuibm.h"
+#include "batch_member.h"
 
+// The batch step is one CUDA graph: every instance's step graph is a child of it, with
+// no edges between them (the instances are independent), launched once per batch step
+// on the batch's own stream.  It is rebuilt when an instance's step graph changes (a
+// new solver grid from the autotuner, an option).  Where an instance's steps need host
+// work between them (see cuibm_batch_member_graph), the batch steps the instances one
+// by one on their own streams instead.
 struct cuibm_batch {
     std::vector<cuibm_ctx *> ctx;
     std::string err;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaGraph_t> members;  // the instance graphs the batch graph was built from
 };
+
+static void drop_graph(cuibm_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->members.clear();
+}
+
+// the batch step graph for the instances' current step graphs; false where one of them
+// has none (the batch then steps the instances one by one)
+static bool batch_graph(cuibm_batch *b)
+{
+    std::vector<cudaGraph_t> cur(b->ctx.size());
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        cur[k] = cuibm_batch_member_graph(b->ctx[k]);
+        if (!cur[k]) {
+            drop_graph(b);
+            return false;
+        }
+    }
+    if (b->exec && cur == b->members) return true;
+    drop_graph(b);
+    if (!b->stream && cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaGraphCreate(&b->graph, 0) != cudaSuccess) return false;
+    for (cudaGraph_t g : cur) {
+        cudaGraphNode_t node;
+        if (cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, g) != cudaSuccess) {
+            drop_graph(b);
+            return false;
+        }
+    }
+    if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
+        drop_graph(b);
+        return false;
+    }
+    b->members = cur;
+    return true;
+}
 
 static std::string g_batch_create_error;
 
@@ -91,13 +142,27 @@ int cuibm_batch_step(cuibm_batch *b, int nsteps)
 {
     if (!b) return CUIBM_ERR_STATE;
     if (nsteps < 0) return batch_fail(b, CUIBM_ERR_BAD_INPUT, "batch: nsteps < 0");
-    for (int s = 0; s < nsteps; ++s)
-        for (size_t k = 0; k < b->ctx.size(); ++k) {
-            const int st = cuibm_step(b->ctx[k], 1);
-            if (st != CUIBM_OK)
-                return batch_fail(b, st,
-                                  "batch: instance " + std::to_string(k) + ": " + cuibm_last_error(b->ctx[k]));
-        }
+    if (nsteps > 0 && batch_graph(b)) {
+        // the instances' own streams may hold work enqueued before (initialisation,
+        // field writes): the batch stream starts after it
+        for (cuibm_ctx *c : b->ctx)
+            if (cudaStreamSynchronize(cuibm_batch_member_stream(c)) != cudaSuccess)
+                return batch_fail(b, CUIBM_ERR_CUDA, "batch: an instance's stream failed");
+        for (int s = 0; s < nsteps; ++s)
+            if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess)
+                return batch_fail(b, CUIBM_ERR_CUDA, "batch: the batch step graph did not launch");
+        if (cudaStreamSynchronize(b->stream) != cudaSuccess)
+            return batch_fail(b, CUIBM_ERR_CUDA, "batch: the batch step graph failed");
+        for (cuibm_ctx *c : b->ctx) cuibm_batch_member_advance(c, nsteps);
+    } else {
+        for (int s = 0; s < nsteps; ++s)
+            for (size_t k = 0; k < b->ctx.size(); ++k) {
+                const int st = cuibm_step(b->ctx[k], 1);
+                if (st != CUIBM_OK)
+                    return batch_fail(b, st,
+                                      "batch: instance " + std::to_string(k) + ": " + cuibm_last_error(b->ctx[k]));
+            }
+    }
     int first = CUIBM_OK;
     for (size_t k = 0; k < b->ctx.size(); ++k) {
         const int st = cuibm_step(b->ctx[k], 0);  // waits for the instance and checks its solves
@@ -182,6 +247,8 @@ const char *cuibm_batch_error(const cuibm_batch *b) { return b ? b->err.c_str() 
 void cuibm_batch_destroy(cuibm_batch *b)
 {
     if (!b) return;
+    drop_graph(b);
+    if (b->stream) cudaStreamDestroy(b->stream);
     for (cuibm_ctx *c : b->ctx) cuibm_destroy(c);
     delete b;
 }

@@ -18,6 +18,7 @@
 
 #include "../../include/cuibm.h"
 #include "solver.h"
+#include "batch_member.h"
 
 namespace cuibm {
 
@@ -641,6 +642,22 @@ int cuibm_step(cuibm_ctx *h, int nsteps)
         }
     });
     return CUIBM_OK;
+}
+
+// the batch's view of an instance (batch_member.h)
+cudaGraph_t cuibm_batch_member_graph(cuibm_ctx *h)
+{
+    if (!h) return nullptr;
+    const Context &c = h->c;
+    if (!c.initialised || !c.use_graph || c.profile_phases || c.sa_rebuild || !c.step_exec) return nullptr;
+    return c.step_graph;
+}
+
+cudaStream_t cuibm_batch_member_stream(cuibm_ctx *h) { return h ? h->c.stream : nullptr; }
+
+void cuibm_batch_member_advance(cuibm_ctx *h, int n)
+{
+    if (h) h->c.timeStep += n;
 }
 
 int cuibm_finished(const cuibm_ctx *h)
