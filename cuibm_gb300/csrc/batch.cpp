@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -21,12 +22,14 @@
 #include "../../include/cuibm.h"
 #include "batch_member.h"
 
-// The batch step is one CUDA graph: every instance's step graph is a child of it, with
-// no edges between them (the instances are independent), launched once per batch step
-// on the batch's own stream.  It is rebuilt when an instance's step graph changes (a
-// new solver grid from the autotuner, an option).  Where an instance's steps need host
-// work between them (see cuibm_batch_member_graph), the batch steps the instances one
-// by one on their own streams instead.
+// With CUIBM_BATCH_GRAPH=1 the batch step is one CUDA graph: every instance's step graph
+// is a child of it, with no edges between them (the instances are independent),
+// launched once per batch step on the batch's own stream, and rebuilt when an
+// instance's step graph changes (a new solver grid from the autotuner, an option).  It
+// is off by default: on the 64-instance benchmark it ran at 208 Mcell-steps/s against
+// 266 with every instance's step graph launched on the instance's own stream (the
+// default).  Where an instance's steps need host work between them (see
+// cuibm_batch_member_graph), the batch always steps the instances one by one.
 struct cuibm_batch {
     std::vector<cuibm_ctx *> ctx;
     std::string err;
@@ -142,7 +145,8 @@ int cuibm_batch_step(cuibm_batch *b, int nsteps)
 {
     if (!b) return CUIBM_ERR_STATE;
     if (nsteps < 0) return batch_fail(b, CUIBM_ERR_BAD_INPUT, "batch: nsteps < 0");
-    if (nsteps > 0 && batch_graph(b)) {
+    const char *eg = getenv("CUIBM_BATCH_GRAPH");
+    if (nsteps > 0 && eg && eg[0] == '1' && batch_graph(b)) {
         // the instances' own streams may hold work enqueued before (initialisation,
         // field writes): the batch stream starts after it
         for (cuibm_ctx *c : b->ctx)
