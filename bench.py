@@ -356,9 +356,10 @@ def batch_cases(tmp, n=64, seed=0, precision=None):
     lid-driven cavities (N from {96, 128, ..., 512}, Re log-uniform in [100, 1000]),
     half impulsively started cylinders (external method, the Re 40 case's stretching
     rule with core h from {0.04, 0.03, 0.02}, round(pi/h) body points made even, Re
-    log-uniform in [40, 300], dt 0.005).  The cavities' dt is 0.01 x 64/N (CFL 0.64,
-    as at 64 x 64): at dt 0.01 the finer cavities are unstable (CFL up to 5) and
-    overflow within a few dozen steps.  precision MIXED: both systems of every
+    log-uniform in [40, 300], dt 0.005).  The cavities' dt is 0.01 x 32/N (a lid CFL
+    number of 0.32): at dt 0.01 the finer cavities are unstable (CFL up to 5) and
+    overflow within a few dozen steps, and at 0.01 x 64/N (CFL 0.64) the 480 x 480
+    cavity at Re 130 still overflows by step 50.  precision MIXED: both systems of every
     instance in mixed precision (the same draws)."""
     import numpy as np
     from cuibm_gb300 import cases
@@ -368,7 +369,7 @@ def batch_cases(tmp, n=64, seed=0, precision=None):
         if k % 2 == 0:
             N = int(rng.choice(np.arange(96, 513, 32)))
             Re = float(np.exp(rng.uniform(np.log(100), np.log(1000))))
-            f = cases.cavity(os.path.join(tmp, "cav%02d" % k), n=N, nu=1.0 / Re, dt=0.01 * 64 / N, nt=1000000,
+            f = cases.cavity(os.path.join(tmp, "cav%02d" % k), n=N, nu=1.0 / Re, dt=0.01 * 32 / N, nt=1000000,
                              vel_tol=1e-8, pois_tol=1e-8, pois_pc="SMOOTHED_AGGREGATION", pois_krylov="CG",
                              precision=precision)
         else:
@@ -382,7 +383,7 @@ def batch_cases(tmp, n=64, seed=0, precision=None):
     return out
 
 
-def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
+def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=2):
     """The batched workload run as one batch (cuibm_batch_*: every instance on its own
     stream, the persistent solves' block count picked by the batch autotuner during
     warm-up), in plain FP64 and in mixed precision (the configuration's), and one
@@ -405,7 +406,7 @@ def batch_comparison(local, n=64, warm=3, steps=20, tune_steps=1):
                 s.set_option("write_output", 0)
             b.initialise()
             b.stepTime(warm)
-            blocks = b.autotune(tune_steps)  # advances every instance by 18 x tune_steps
+            blocks = b.autotune(tune_steps)  # advances every instance by 16 x tune_steps
             warm_all = b.instances[0].timeStep
             cells = sum(s.info.numP for s in b.instances)
             torch.cuda.synchronize()

@@ -398,7 +398,7 @@ class Batch:
 
     def autotune(self, steps=2):
         """Pick the persistent solves' block counts by timing the batch (cuibm_batch_autotune;
-        every instance advances 18 x steps); returns the choice: one block count for all
+        every instance advances 16 x steps); returns the choice: one block count for all
         instances, or minus the rows a thread of counts sized per instance."""
         nb = ctypes.c_int()
         self._check(self._L.cuibm_batch_autotune(self._h, int(steps), ctypes.byref(nb)))

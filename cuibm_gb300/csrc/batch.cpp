@@ -181,10 +181,10 @@ int cuibm_batch_step(cuibm_batch *b, int nsteps)
 // The best grid depends on the instances' sizes and count (fewer, larger blocks give
 // each solve more of the GPU; more, smaller shares let more solves run at once), so
 // it is measured on the batch itself.  Candidates: one block count for every instance
-// (a half ... a twelfth of the SMs), or a count per instance from its pressure
-// unknowns at 4, 8, 16 or 32 rows a thread (512 threads a block; at least 2 blocks, at
-// most half the SMs): at 8 rows a thread a 9k-cell cavity takes 3 blocks and a
-// 262k-cell one 64.
+// (a quarter, sixth or eighth of the SMs), or a count per instance from its pressure
+// unknowns at 6, 8, 12, 16 or 24 rows a thread (512 threads a block; at least 2 blocks,
+// at most half the SMs): at 16 rows a thread a 9k-cell cavity takes 2 blocks and a
+// 262k-cell one 32.
 int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out)
 {
     if (!b) return CUIBM_ERR_STATE;
@@ -194,11 +194,11 @@ int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return batch_fail(b, CUIBM_ERR_CUDA, "batch: cannot query the device");
     std::vector<int> cand;  // > 0: blocks for every instance; < 0: minus the rows a thread
-    for (int d : {2, 4, 6, 8, 12}) {
+    for (int d : {4, 6, 8}) {
         const int nb = sms / d > 0 ? sms / d : 1;
         if (cand.empty() || cand.back() != nb) cand.push_back(nb);
     }
-    for (int r : {4, 8, 16, 32}) cand.push_back(-r);
+    for (int r : {6, 8, 12, 16, 24}) cand.push_back(-r);
     std::vector<int> rows(b->ctx.size(), 1);
     for (size_t k = 0; k < b->ctx.size(); ++k) {
         cuibm_info info;

@@ -311,11 +311,11 @@ int cuibm_batch_create(int n, const char *const *case_folders, int argc, const c
 int cuibm_batch_initialise(cuibm_batch *b);
 int cuibm_batch_step(cuibm_batch *b, int nsteps);
 /* Autotuner of the batch's persistent-solve grid: times `steps` batch steps with each
- * candidate - one block count for every instance (a half, quarter, sixth, eighth and
- * twelfth of the SMs) or a count per instance from its pressure unknowns at 4, 8, 16
- * or 32 rows a thread (at least 2 blocks, at most half the SMs) - in two passes of
- * opposite order, and keeps the fastest (option "solver_blocks" of every instance).
- * The timed steps are steps of the simulation (each instance advances 18 x steps).
+ * candidate - one block count for every instance (a quarter, sixth or eighth of the
+ * SMs) or a count per instance from its pressure unknowns at 6, 8, 12, 16 or 24 rows a
+ * thread (at least 2 blocks, at most half the SMs) - in two passes of opposite order,
+ * and keeps the fastest (option "solver_blocks" of every instance).  The timed steps
+ * are steps of the simulation (each instance advances 16 x steps).
  * *blocks_out (may be null) gets the choice: the block count, or minus the rows a
  * thread of a per-instance choice. */
 int cuibm_batch_autotune(cuibm_batch *b, int steps, int *blocks_out);

@@ -62,15 +62,15 @@ def test_autotune_keeps_every_instance_exact(tmp_path):
         with cb.NavierStokesSolver(f) as s:
             s.set_option("write_output", 0)
             s.initialise()
-            s.stepTime(20)
+            s.stepTime(18)
             alone.append((s.get("u"), s.get("p")))
     with cb.Batch(folders) as b:
         for s in b.instances:
             s.set_option("write_output", 0)
         b.initialise()
-        nb = b.autotune(1)  # eighteen steps
-        assert 1 <= nb <= 76 or nb in (-4, -8, -16, -32)
-        assert all(s.timeStep == 18 for s in b.instances)
+        nb = b.autotune(1)  # sixteen steps
+        assert 1 <= nb <= 38 or nb in (-6, -8, -12, -16, -24)
+        assert all(s.timeStep == 16 for s in b.instances)
         b.stepTime(2)
         for s, (u, p) in zip(b.instances, alone):
             assert rel_l2(s.get("u"), u) < 1e-9
