@@ -455,22 +455,29 @@ def oscillating_case(folder, nt, tol=1e-8, nu=None, ucoef=None):
                           motion=motion, vel_tol=tol, pois_tol=tol)
 
 
-def adjoint_comparison(local, steps=40, snapshots=64, tol=1e-8, fd=False, also_snapshots=(8,)):
+def adjoint_comparison(local, steps=40, snapshots=64, tol=1e-8, fd=(), also_snapshots=(8,), run_adjoint=True):
     """The discrete adjoint on the oscillating cylinder at KC 10 (686 x 686, 314 points,
     embedded method): the gradient of the drag coefficient averaged over the first `steps`
     steps with respect to nu, the velocity amplitude and the per-point velocity offsets,
     against the forward run of the same steps (forward and transposed solves to tol).
-    Times are wall-clock.  With fd, central differences (relative step 1e-6) of the
-    forward run for nu and uCoefficient beside the gradient."""
+    Times are wall-clock.  fd names the central differences of the forward run to add
+    beside the gradient: "nu", "ucoef" (relative step 1e-6), "offset" (point 0's u
+    offset, step 1e-6).  run_adjoint False: the forward run and the differences only."""
+    import numpy as np
+
     import cuibm_gb300 as cb
     tmp = tempfile.mkdtemp(prefix="cuibm_adj_")
 
-    def fresh(nu=None, ucoef=None, name="kc10"):
+    def fresh(nu=None, ucoef=None, name="kc10", offset_u0=0.0):
         f = oscillating_case(os.path.join(tmp, name), steps, tol=tol, nu=nu, ucoef=ucoef)
         s = cb.NavierStokesSolver(f, ["-deviceNumber", str(local)])
         s.set_option("write_output", 0)
         s.set_option("adjoint_tolerance", tol)
         s.initialise()
+        if offset_u0:
+            off = np.zeros(2 * s.info.total_points)
+            off[0] = offset_u0
+            s.set("body_velocity_offset", off)
         return s
 
     def forward(**kw):
@@ -492,7 +499,7 @@ def adjoint_comparison(local, steps=40, snapshots=64, tol=1e-8, fd=False, also_s
                        % (info.nx, info.ny, info.total_points),
            "steps": steps, "tolerance": tol, "objective": "mean of C_D = 2 Fx over the steps", "J_forward": J,
            "forward_s": round(fwd, 3), "cells": info.nx * info.ny}
-    for snaps in (snapshots,) + tuple(also_snapshots):
+    for snaps in ((snapshots,) + tuple(also_snapshots)) if run_adjoint else ():
         s = fresh()
         t0 = time.perf_counter()
         Ja, grad, st = s.adjoint(steps, 2.0 / steps, snapshots=snaps)
@@ -504,12 +511,16 @@ def adjoint_comparison(local, steps=40, snapshots=64, tol=1e-8, fd=False, also_s
             "dJ_doffset_v0": grad[2 + info.total_points], "stats": st}
     if fd:
         h, nu0 = 1e-6, 1.0 / 200
-        g = out["snapshots_%d" % snapshots]
-        fd_nu = (forward(nu=nu0 * (1 + h), name="nup")[0] - forward(nu=nu0 * (1 - h), name="num")[0]) / (2 * h * nu0)
-        fd_uc = (forward(ucoef=1 + h, name="ucp")[0] - forward(ucoef=1 - h, name="ucm")[0]) / (2 * h)
-        out["central_differences"] = {"relative_step": h, "dJ_dnu": fd_nu, "dJ_duCoefficient": fd_uc,
-                                      "rel_err_nu": abs(g["dJ_dnu"] - fd_nu) / abs(fd_nu),
-                                      "rel_err_uCoefficient": abs(g["dJ_duCoefficient"] - fd_uc) / abs(fd_uc)}
+        g = out.get("snapshots_%d" % snapshots)
+        cd = out["central_differences"] = {"step": h}
+        pairs = {"nu": ("dJ_dnu", dict(nu=nu0 * (1 + h), name="nup"), dict(nu=nu0 * (1 - h), name="num"), h * nu0),
+                 "ucoef": ("dJ_duCoefficient", dict(ucoef=1 + h, name="ucp"), dict(ucoef=1 - h, name="ucm"), h),
+                 "offset": ("dJ_doffset_u0", dict(offset_u0=h, name="ofp"), dict(offset_u0=-h, name="ofm"), h)}
+        for name in fd:
+            key, plus, minus, step = pairs[name]
+            cd[key] = (forward(**plus)[0] - forward(**minus)[0]) / (2 * step)
+            if g is not None:
+                cd["rel_err_" + key] = abs(g[key] - cd[key]) / abs(cd[key])
     return out
 
 
@@ -626,9 +637,12 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the discrete-adjoint measurement")
     ap.add_argument("--adjoint-period", type=int, default=0, metavar="STEPS",
                     help="only the discrete-adjoint comparison over STEPS steps of the KC 10 case (4000: the "
-                         "whole period), solves to --adjoint-tol, with central differences if --adjoint-fd")
+                         "whole period), solves to --adjoint-tol, with the central differences --adjoint-fd names")
     ap.add_argument("--adjoint-tol", type=float, default=1e-10)
-    ap.add_argument("--adjoint-fd", action="store_true")
+    ap.add_argument("--adjoint-fd", default="", metavar="NAMES",
+                    help="central differences beside the gradient: a comma list of nu, ucoef, offset")
+    ap.add_argument("--no-adjoint-run", action="store_true",
+                    help="with --adjoint-period: the forward run and the central differences only")
     ap.add_argument("--kernel-timings", default=None, metavar="K1,K2,...",
                     help="only time these kernels (profile_kernel names) after the warm-up steps of the "
                          "workload, one JSON line each (the command the per-kernel ncu summaries capture)")
@@ -638,8 +652,9 @@ def main():
         kernel_timings(a)
         return
     if a.adjoint_period:
-        print(json.dumps(adjoint_comparison(0, steps=a.adjoint_period, tol=a.adjoint_tol, fd=a.adjoint_fd,
-                                            also_snapshots=())))
+        fd = tuple(x for x in a.adjoint_fd.split(",") if x)
+        print(json.dumps(adjoint_comparison(0, steps=a.adjoint_period, tol=a.adjoint_tol, fd=fd, also_snapshots=(),
+                                            run_adjoint=not a.no_adjoint_run)))
         return
     rank, world, local, pg = dist_setup(a.gpus)
     cfg = workload_config(a.workload)
