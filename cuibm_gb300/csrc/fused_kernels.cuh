@@ -521,8 +521,10 @@ __device__ __forceinline__ void dense_solve(const FLevel<T> &C, const T *b, T *x
     for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = (double)__ldcg(b + k);
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int row = warp; row < n; row += nwarps) {
+    // rows dealt to the blocks in turn (row r to block r mod grid), so that every SM
+    // streams its share of the inverse rather than the first n / 16 blocks all of it
+    const int nw = blockDim.x >> 5;
+    for (int row = blockIdx.x + gridDim.x * (threadIdx.x >> 5); row < n; row += gridDim.x * nw) {
         const double *a = C.inv + (size_t)row * n;
         double acc0 = 0, acc1 = 0;
         int k = lane;
