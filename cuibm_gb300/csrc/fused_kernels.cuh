@@ -123,6 +123,10 @@ struct FArgs {
     // inside the phase that writes them (large FP64 systems: the recomputation costs
     // more FP64 issue than the extra barrier)
     int split0;
+    // Jacobi BiCGSTAB: the direction and the half step folded into the phases that apply
+    // A to their scaled values, recomputed at the stencil points (FP32 solves; FP64 below
+    // kFoldMax unknowns, none by default)
+    int fold1;
     FLevel<T> lev[kMaxLevels];
     // mixed precision, float side: the FP32 cycle's input (SA) or the inner system's
     // right-hand side and solution (refinement)
@@ -348,6 +352,10 @@ struct V2 {
 template <class T>
 struct V3 {
     T a, b, c;
+};
+template <class T>
+struct V4 {
+    T a, b, c, d;
 };
 #define FOR_GROUP_ROWS(G, i, n) \
     for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); i < (n); i += (int)((gridDim.x * blockDim.x) / G))
@@ -1174,12 +1182,13 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
         }
         T v1[1] = {0};
         double v1d[1], o1[1];
-        if (PC != 2) {
-            // Jacobi or none: the new direction and M p are stored in one phase and A M p
-            // read back in the next.  Folding them into one phase recomputed the direction
-            // and its scaling at the four stencil neighbours, about 22 FP64 operations a
-            // row against 9, and FP64 issue bounds these phases (the values are the same:
-            // M p_j = D^-1_j p_j either way)
+        // Jacobi or none: the new direction and M p are stored in one phase and A M p read
+        // back in the next; or (fold1: the FP32 solves) one phase that recomputes the
+        // direction and its scaling at the four stencil neighbours - about 22 operations
+        // a row against 9, which FP64 issue does not repay (the values are the same:
+        // M p_j = D^-1_j p_j either way)
+        const bool fold = PC != 2 && a.fold1;
+        if (PC != 2 && !fold) {
             FOR_ROWS(i, a.n)
             {
                 const T pi = first ? __ldcg(p + i) : dir(i);
@@ -1188,7 +1197,25 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
             }
             if (!grid_sync(a.sync, a.trace)) return false;
         }
-        if (PC == 2 && (MX || defl)) {
+        if (fold) {
+            auto mp = [&](int j) {
+                const T pj = first ? __ldcg(p + j) : dir(j);
+                return PC == 1 ? a.dinv[j] * pj : pj;
+            };
+            rows2(
+                a.n,
+                [&](int i) {
+                    const T pi = first ? __ldcg(p + i) : dir(i);
+                    const T mi = PC == 1 ? a.dinv[i] * pi : pi;
+                    return V4<T>{pi, mi, A.row_x(i, mi, mp), __ldcg(a.rs + i)};
+                },
+                [&](int i, const V4<T> &u) {
+                    if (!first) pn[i] = u.a;
+                    a.Mp[i] = u.b;
+                    ampn[i] = u.c;
+                    v1[0] += u.d * u.c;
+                });
+        } else if (PC == 2 && (MX || defl)) {
             rows2(
                 a.n,
                 [&](int i) {
@@ -1319,22 +1346,45 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
         } else {
             T v3[3] = {0, 0, 0};
             double v3d[3];
-            // as for the direction: s and M s stored, then A M s in the next phase
-            FOR_ROWS(i, a.n)
-            {
-                const T si = snew(i);
-                a.s[i] = si;
-                a.Ms[i] = PC == 1 ? a.dinv[i] * si : si;
-            }
-            if (!grid_sync(a.sync, a.trace)) return false;
-            FOR_ROWS(i, a.n)
-            {
-                const T si = __ldcg(a.s + i);
-                const T ai = A.row(i, acc((const T *)a.Ms));
-                a.AMs[i] = ai;
-                v3[0] += ai * si;
-                v3[1] += ai * ai;
-                v3[2] += si * si;
+            // as for the direction: s and M s stored, then A M s in the next phase; or (fold1)
+            // one phase with s and its scaling recomputed at the stencil points
+            if (fold) {
+                auto ms = [&](int j) {
+                    const T sj = snew(j);
+                    return PC == 1 ? a.dinv[j] * sj : sj;
+                };
+                rows2(
+                    a.n,
+                    [&](int i) {
+                        const T si = snew(i);
+                        const T mi = PC == 1 ? a.dinv[i] * si : si;
+                        return V3<T>{si, mi, A.row_x(i, mi, ms)};
+                    },
+                    [&](int i, const V3<T> &u) {
+                        a.s[i] = u.a;
+                        a.Ms[i] = u.b;
+                        a.AMs[i] = u.c;
+                        v3[0] += u.c * u.a;
+                        v3[1] += u.c * u.c;
+                        v3[2] += u.a * u.a;
+                    });
+            } else {
+                FOR_ROWS(i, a.n)
+                {
+                    const T si = snew(i);
+                    a.s[i] = si;
+                    a.Ms[i] = PC == 1 ? a.dinv[i] * si : si;
+                }
+                if (!grid_sync(a.sync, a.trace)) return false;
+                FOR_ROWS(i, a.n)
+                {
+                    const T si = __ldcg(a.s + i);
+                    const T ai = A.row(i, acc((const T *)a.Ms));
+                    a.AMs[i] = ai;
+                    v3[0] += ai * si;
+                    v3[1] += ai * ai;
+                    v3[2] += si * si;
+                }
             }
             to_double(v3, v3d);
             if (!grid_reduce<3, 3>(v3d, a, parity, [&](const double (&t)[3], double (&q)[3]) {

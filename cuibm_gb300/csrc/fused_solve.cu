@@ -126,6 +126,13 @@ static void launch_fused_mixed(Context &c, LinearSystem &S, Op64 A, Op32 A32, co
     CUIBM_TRY(cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(S.fused_fn), A, A32, args, fargs, b, x));
 }
 
+// Below this many unknowns the FP64 Jacobi BiCGSTAB folds its direction and half step
+// into the phases that apply A (FArgs::fold1; CUIBM_FOLD1=0 or 1 overrides).  None by
+// default: at the Re 40 cylinder's 145k velocity unknowns the folded solve took 153 us
+// in 14 phases against 149 us in 22 (the recomputation's FP64 issue costs what the
+// barriers save); the FP32 inner solves of iterative refinement always fold.
+constexpr int kFoldMax = 0;
+
 // Structured restrictions into coarse levels up to this size take 8 lanes a coarse node
 constexpr int kRestrictGroupMax = 20000;
 
@@ -185,6 +192,10 @@ static void upload_fargs(Context &c, LinearSystem &S)
     }
     a.st = S.sa_structured;
     a.split0 = S.n >= kSplitMin && !(getenv("CUIBM_SPLIT0") && getenv("CUIBM_SPLIT0")[0] == '0');
+    {
+        const char *e = getenv("CUIBM_FOLD1");
+        a.fold1 = e && (e[0] == '0' || e[0] == '1') ? e[0] == '1' : S.n < kFoldMax;
+    }
     a.ym = S.ym;
     a.wdef = S.wdef;
     a.aedef = S.aedef;
@@ -271,6 +282,7 @@ static void setup_mixed(Context &c, LinearSystem &S)
         F.rg = L->nx > 0 && l + 1 < f.nlev && S.amg[l + 1]->n <= kRestrictGroupMax;
     }
     f.st = S.sa_structured;
+    f.fold1 = 1;
     m->dev = c.carve<FArgs<float>>(1);
     CUIBM_TRY(cudaMemcpyAsync(m->dev, &f, sizeof(f), cudaMemcpyHostToDevice, c.stream));
     CUIBM_TRY(cudaStreamSynchronize(c.stream));
