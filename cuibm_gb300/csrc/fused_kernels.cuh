@@ -581,17 +581,22 @@ __device__ __forceinline__ bool cycle_end(const FArgs<T> &a, T v0, double vw, bo
 // out_l = x_l + w D^-1 (b_l - A_l x_l) reads its stencil values from there.
 constexpr int kTW = 32, kTH = 16, kTP = kTW + 2;
 
-// a tile's x_l as the stencil of node i (tile slot li) sees it: neighbours j = i + dy nx
-// + dx with |dx|, |dy| <= 1 (nx >= 3 on every level with a coarser one)
+// a tile's x_l as the stencil of node i (tile slot li) sees it: a neighbour j = i + dy nx
+// + dx, |dx|, |dy| <= 1, told from the index difference where nx >= 3 and from j's
+// coordinates otherwise (a level one or two nodes wide; the tile's first node (x0, y0))
 template <class T>
 struct TileAcc {
     const T *xs;
-    int li, i, nx;
+    int li, i, nx, x0, y0;
     __device__ __forceinline__ T operator()(int j) const
     {
-        const int d = j - i;
-        const int dy = d >= nx - 1 ? 1 : (d <= 1 - nx ? -1 : 0);
-        return xs[li + dy * kTP + (d - dy * nx)];
+        if (nx >= 3) {
+            const int d = j - i;
+            const int dy = d >= nx - 1 ? 1 : (d <= 1 - nx ? -1 : 0);
+            return xs[li + dy * kTP + (d - dy * nx)];
+        }
+        const int jy = j / nx, jx = j - jy * nx;
+        return xs[(jy - y0 + 1) * kTP + (jx - x0 + 1)];
     }
 };
 
@@ -623,7 +628,7 @@ __device__ __forceinline__ void st_up_tiles(const FLevel<T> &V, int cnx, int cny
             if (ix < nx && iy < ny) {
                 const int i = iy * nx + ix, li = (ly + 1) * kTP + lx + 1;
                 const T xi = xs[li];
-                out(i, xi + V.wd[i] * (__ldcg(bb + i) - row(i, xi, TileAcc<T>{xs, li, i, nx})));
+                out(i, xi + V.wd[i] * (__ldcg(bb + i) - row(i, xi, TileAcc<T>{xs, li, i, nx, x0, y0})));
             }
         }
         __syncthreads();
