@@ -66,3 +66,30 @@ def test_cycle_preconditions_bicgstab(tmp_path):
     # a random right-hand side (the worst case: the time loop's solves start from the last
     # pressure); diagonal scaling alone does not reach 1e-8 in 2000 iterations
     assert its[0] < 200, its[0]
+
+
+@pytest.mark.parametrize("nx,ny,sizes", [(600, 5, [3000, 200]), (5, 600, [3000, 200]), (97, 47, [4559, 480]),
+                                         (1000, 13, [13000, 1332])])
+def test_narrow_and_odd_grids(tmp_path, nx, ny, sizes):
+    """Aggregates at the remainder rules' corners (a coarse direction of one node,
+    aggregates 4 or 5 wide): the coarse operators stay 9-point and the cycle still
+    preconditions BiCGSTAB on a plain channel's pressure operator."""
+    h = 0.01
+    sim = {"type": "simulation", "dt": 0.001, "nt": 10, "nsave": 10, "SolverType": "NAVIER_STOKES_SOLVER",
+           "linearSolvers": cases.solvers("DIAGONAL", 1e-8, "SMOOTHED_AGGREGATION", 1e-8, pois_krylov="BICGSTAB")}
+    flow = [{"type": "flow", "nu": 0.01, "initialVelocity": [0.0, 0.0], "initialPerturbation": [0.0, 0.0],
+             "boundaryConditions": cases.bcs((0, 0), (0, 0), (0, 0), (1.0, 0))}]
+    dom = [cases.axis("x", 0.0, h, [(nx * h, 1.0)]), cases.axis("y", 0.0, h, [(ny * h, 1.0)])]
+    f = cases.write_case(os.path.join(str(tmp_path), "c"), [sim], flow, dom, [])
+    g = oracle.PlainSolver(f, solve="none").g
+    r, c, v = oracle.lhs2_coo(g, 0.001, centre_pin=True)[:3]
+    A = sp.coo_matrix((v, (r, c)), shape=(g.nP, g.nP)).tocsr()
+    levels = ref.hierarchy(A, g.nx, g.ny)
+    assert [L["A"].shape[0] for L in levels] == sizes
+    for L in levels[1:]:
+        assert ref.stencil_offsets(L["A"], L["nx"], L["ny"]) <= NINE
+    n = A.shape[0]
+    M = spla.LinearOperator((n, n), matvec=lambda b: ref.vcycle(levels, b))
+    b = A @ np.random.default_rng(1).standard_normal(n)
+    x, info = spla.bicgstab(A, b, M=M, rtol=1e-8, maxiter=300)
+    assert info == 0 and np.linalg.norm(b - A @ x) <= 1e-8 * np.linalg.norm(b)
