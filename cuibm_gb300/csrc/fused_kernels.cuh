@@ -851,6 +851,18 @@ __device__ __forceinline__ bool first_sweep(const Op &A, const FArgs<T> &a, cons
     return grid_sync(a.sync, a.trace);
 }
 
+// The same first phase when the phase that wrote b also wrote t_0 = w D^-1 b (level 0's
+// t): r_0 = b - A t_0, without scaling b at every stencil point again (FP64 issue)
+template <int U = 4, class Op, class T>
+__device__ __forceinline__ bool first_sweep_scaled(const Op &A, const FArgs<T> &a, const T *b)
+{
+    const FLevel<T> &V = a.lev[0];
+    rows2<U>(
+        V.n, [&](int i) { return __ldcg(b + i) - A.row_x(i, __ldcg(V.t + i), acc((const T *)V.t)); },
+        [&](int i, T r) { V.r[i] = r; });
+    return grid_sync(a.sync, a.trace);
+}
+
 // z = V(b) for a stored input; with dot also rz = b . z and beta = rz / rho_prev.
 // A one-level hierarchy is the dense solve alone.
 template <int U = 4, class Op, class T>
@@ -1148,6 +1160,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                         pn[i] = pi;
                         if (!a.split0) vcycle_residual0_row(A, a.lev[0], i, dir, pi);
                     }
+                    if (a.split0) a.lev[0].t[i] = a.lev[0].wd[i] * pi;  // the first sweep's w D^-1 b
                     ve[0] += pi;
                 }
                 double eb[1] = {0};
@@ -1165,7 +1178,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                     p = pn;
                     pn = tmp;
                 }
-                if (a.split0 && !first_sweep<U>(A, a, (const T *)p)) return false;
+                if (a.split0 && !first_sweep_scaled<U>(A, a, (const T *)p)) return false;
                 if (defl) {
                     double wy = 0;
                     if (!vcycle_rest<U>(A, a, (const T *)p, a.ym, false, 1.0, dummy, dummy2, parity, a.wdef, &wy))
@@ -1283,6 +1296,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                     v2[0] += si * si;
                     v2[1] += si;
                     if (!a.split0) vcycle_residual0_row(A, a.lev[0], i, snew, si);
+                    else a.lev[0].t[i] = a.lev[0].wd[i] * si;
                 }
             } else {
                 FOR_ROWS(i, a.n)
@@ -1306,7 +1320,7 @@ __device__ __forceinline__ bool bicg_solve(const Op &A, const FArgs<T> &a, const
                 status = KS_CONVERGED;
                 break;
             }
-            if (sa_multi && !MX && a.split0 && !first_sweep<U>(A, a, (const T *)a.s)) return false;
+            if (sa_multi && !MX && a.split0 && !first_sweep_scaled<U>(A, a, (const T *)a.s)) return false;
             if (MX) {
                 if (!vcycle_mixed(*A32, *f, f->bin, a.ym, a.wdef, a.Edef, o2[1], cmx, parity)) return false;
             } else if (defl) {
